@@ -1,0 +1,302 @@
+"""Python binding (ctypes) of the CSMV GB300 C ABI (include/csmv.h).
+
+Mirrors the reference's host interface for the commit path: ``Bank`` stands in for the
+TXInit / parent_kernel / TXEnd sequence of bank/csmv_sh/exe.cu:340-529 (create + load, run,
+read back), with statistics named after the reference's Statistics struct
+(bank/csmv_sh/API.cuh:112-119). There is no CPU fallback: every call goes through
+``lib/libcsmv.so`` and raises when the library is missing or a call fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+PKG_ROOT = Path(__file__).resolve().parent.parent
+LIB_PATH = PKG_ROOT / "lib" / "libcsmv.so"
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory",
+          4: "bounded device wait timed out", 5: "capacity exceeded", 6: "no sm_103 device",
+          7: "call out of order"}
+
+KIND_READONLY, KIND_TRANSFER, KIND_TRANSFER_ALWAYS = 0, 1, 2
+DIST_UNIFORM, DIST_ZIPF, DIST_HOTSPOT = 0, 1, 2
+VALIDATE_STAMP, VALIDATE_RING, VALIDATE_RING_LANE = 0, 1, 2
+WRITEBACK_CLIENT, WRITEBACK_SERVER = 0, 1
+BATCH_LANE, BATCH_WARP, BATCH_CTA, BATCH_CLUSTER = 0, 1, 2, 3
+SNAP_FLAG = 0x80000000
+
+
+class CsmvError(RuntimeError):
+    def __init__(self, status: int, where: str, detail: str):
+        super().__init__(f"{where}: {STATUS.get(status, status)} ({detail})")
+        self.status = status
+
+
+class BankWorkload(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("n_accounts", C.c_uint32), ("n_txn", C.c_uint32),
+                ("pr_read_pct", C.c_uint32), ("ro_reads", C.c_uint32), ("up_reads", C.c_uint32),
+                ("kind", C.c_uint32), ("amt_lo", C.c_uint32), ("amt_hi", C.c_uint32),
+                ("dist", C.c_uint32), ("zipf_theta", C.c_double), ("hot_frac", C.c_double),
+                ("hot_prob", C.c_double), ("shift_every", C.c_uint32)]
+
+
+class BankStream(C.Structure):
+    _fields_ = [("n_txn", C.c_uint32), ("op", C.c_void_p), ("off", C.c_void_p),
+                ("addr", C.c_void_p), ("n_addr", C.c_uint64)]
+
+
+class BankConfig(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in ("n_accounts",)] + [("init_value", C.c_int32)] + [
+        (n, C.c_uint32) for n in ("version_depth", "ring_size", "client_warps", "ctas",
+                                  "cluster_size", "validate", "writeback", "batch",
+                                  "prevalidate", "log_commits", "max_txn", "spin_limit_log2")
+    ] + [("device", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in (
+        "commits_update", "commits_readonly", "commits_nowrite", "aborts_data_age",
+        "aborts_record_age", "aborts_read_write", "aborts_prevalid", "sections", "rounds")] + [
+        ("final_ts", C.c_uint32), ("error", C.c_uint32), ("kernel_ms", C.c_double),
+        ("total_ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+    @property
+    def commits(self) -> int:
+        return self.commits_update + self.commits_readonly + self.commits_nowrite
+
+    @property
+    def aborts(self) -> int:
+        return (self.aborts_data_age + self.aborts_record_age + self.aborts_read_write +
+                self.aborts_prevalid)
+
+    @property
+    def abort_rate(self) -> float:
+        """aborts / (aborts + commits), as the reference prints it (bank/csmv_sh/exe.cu:467-471)."""
+        tot = self.aborts + self.commits
+        return self.aborts / tot if tot else 0.0
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libcsmv.so (raises when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with csmv_gb300.build.build() "
+                           "(the CSMV path has no CPU fallback)")
+    L = C.CDLL(str(LIB_PATH))
+    P, U32, I32 = C.c_void_p, C.c_uint32, C.c_int
+    sigs = {
+        "csmv_bank_config_default": (None, [C.POINTER(BankConfig)]),
+        "csmv_bank_stream_size": (I32, [C.POINTER(BankWorkload), C.POINTER(C.c_uint64)]),
+        "csmv_bank_generate": (I32, [C.POINTER(BankWorkload), P, P, P]),
+        "csmv_bank_create": (I32, [C.POINTER(BankConfig), C.POINTER(P)]),
+        "csmv_bank_load": (I32, [P, P]),
+        "csmv_bank_run": (I32, [P, C.POINTER(BankStream), C.POINTER(Stats)]),
+        "csmv_bank_run_device": (I32, [P, C.POINTER(BankStream), C.POINTER(Stats)]),
+        "csmv_bank_read_values": (I32, [P, P]),
+        "csmv_bank_read_versions": (I32, [P, P]),
+        "csmv_bank_read_log": (I32, [P, P, U32, P, P, U32]),
+        "csmv_bank_device_info": (I32, [P, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_int), C.POINTER(C.c_size_t)]),
+        "csmv_bank_destroy": (None, [P]),
+        "csmv_pinned_alloc": (I32, [C.c_size_t, C.POINTER(P)]),
+        "csmv_pinned_free": (None, [P]),
+        "csmv_last_error": (C.c_char_p, []),
+        "csmv_status_str": (C.c_char_p, [I32]),
+        "csmv_abi_version": (I32, []),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(st: int, where: str) -> None:
+    if st != 0:
+        raise CsmvError(st, where, lib().csmv_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray) -> int:
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data
+
+
+# ---------------------------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------------------------
+
+def bank_workload(n_accounts: int, n_txn: int, *, seed: int = 1, pr_read_pct: int = 10,
+                  ro_reads: int = 8, up_reads: int = 2, kind: int = KIND_TRANSFER,
+                  amt_lo: int = 1, amt_hi: int = 10, dist: int = DIST_UNIFORM,
+                  zipf_theta: float = 0.99, hot_frac: float = 0.01, hot_prob: float = 0.9,
+                  shift_every: int = 1 << 20) -> BankWorkload:
+    return BankWorkload(seed, n_accounts, n_txn, pr_read_pct, ro_reads, up_reads, kind, amt_lo,
+                        amt_hi, dist, zipf_theta, hot_frac, hot_prob, shift_every)
+
+
+@dataclass
+class Stream:
+    op: np.ndarray
+    off: np.ndarray
+    addr: np.ndarray
+
+    @property
+    def n_txn(self) -> int:
+        return int(self.op.shape[0])
+
+    def c_struct(self) -> BankStream:
+        return BankStream(self.n_txn, _ptr(self.op), _ptr(self.off), _ptr(self.addr),
+                          int(self.addr.shape[0]))
+
+
+class PinnedArray:
+    """numpy view over page-locked host memory (freed with the object)."""
+
+    def __init__(self, n: int, dtype=np.uint32):
+        self.dtype = np.dtype(dtype)
+        p = C.c_void_p()
+        _check(lib().csmv_pinned_alloc(max(1, n) * self.dtype.itemsize, C.byref(p)),
+               "csmv_pinned_alloc")
+        self._p = p
+        buf = (C.c_char * (max(1, n) * self.dtype.itemsize)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=self.dtype)[:n]
+
+    def __del__(self):
+        if getattr(self, "_p", None) is not None and _lib is not None:
+            _lib.csmv_pinned_free(self._p)
+            self._p = None
+
+
+def generate(w: BankWorkload, pinned: bool = False) -> Stream:
+    """Host generator of the library (csmv_bank_generate)."""
+    n_addr = C.c_uint64()
+    _check(lib().csmv_bank_stream_size(C.byref(w), C.byref(n_addr)), "csmv_bank_stream_size")
+    if pinned:
+        holders = [PinnedArray(w.n_txn), PinnedArray(w.n_txn), PinnedArray(n_addr.value)]
+        op, off, addr = (h.array for h in holders)
+    else:
+        holders = []
+        op = np.empty(w.n_txn, np.uint32)
+        off = np.empty(w.n_txn, np.uint32)
+        addr = np.empty(n_addr.value, np.uint32)
+    _check(lib().csmv_bank_generate(C.byref(w), _ptr(op), _ptr(off), _ptr(addr)),
+           "csmv_bank_generate")
+    s = Stream(op, off, addr)
+    s._holders = holders  # keep pinned memory alive
+    return s
+
+
+# ---------------------------------------------------------------------------------------------
+# bank engine
+# ---------------------------------------------------------------------------------------------
+
+def bank_config(**kw) -> BankConfig:
+    cfg = BankConfig()
+    lib().csmv_bank_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        if not hasattr(cfg, k):
+            raise KeyError(f"unknown bank config field {k}")
+        setattr(cfg, k, v)
+    return cfg
+
+
+class Bank:
+    """One CSMV bank instance on one GPU (TXInit ... TXEnd of the reference)."""
+
+    def __init__(self, cfg: BankConfig | None = None, **kw):
+        self.cfg = cfg if cfg is not None else bank_config(**kw)
+        h = C.c_void_p()
+        _check(lib().csmv_bank_create(C.byref(self.cfg), C.byref(h)), "csmv_bank_create")
+        self._h = h
+        self.last_stats: Stats | None = None
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            lib().csmv_bank_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def load(self, values: np.ndarray | None = None) -> None:
+        if values is not None:
+            values = np.ascontiguousarray(values, dtype=np.int32)
+            assert values.shape[0] == self.cfg.n_accounts
+        _check(lib().csmv_bank_load(self._h, _ptr(values) if values is not None else None),
+               "csmv_bank_load")
+
+    def run(self, stream: Stream) -> Stats:
+        """Host buffers in: copies the stream to the device inside the call."""
+        st = Stats()
+        s = stream.c_struct()
+        rc = lib().csmv_bank_run(self._h, C.byref(s), C.byref(st))
+        self.last_stats = st
+        _check(rc, "csmv_bank_run")
+        return st
+
+    def run_device(self, dev_stream: BankStream) -> Stats:
+        st = Stats()
+        rc = lib().csmv_bank_run_device(self._h, C.byref(dev_stream), C.byref(st))
+        self.last_stats = st
+        _check(rc, "csmv_bank_run_device")
+        return st
+
+    def values(self) -> np.ndarray:
+        out = np.empty(self.cfg.n_accounts, np.int32)
+        _check(lib().csmv_bank_read_values(self._h, _ptr(out)), "csmv_bank_read_values")
+        return out
+
+    def versions(self) -> np.ndarray:
+        out = np.empty(self.cfg.n_accounts * self.cfg.version_depth, np.uint64)
+        _check(lib().csmv_bank_read_versions(self._h, _ptr(out)), "csmv_bank_read_versions")
+        return out
+
+    def log(self, n_txn: int, n_commits: int):
+        log_txn = np.empty(max(1, n_commits), np.uint32)
+        outcome = np.empty(n_txn, np.uint32)
+        result = np.empty(n_txn, np.int32)
+        _check(lib().csmv_bank_read_log(self._h, _ptr(log_txn), max(1, n_commits), _ptr(outcome),
+                                        _ptr(result), n_txn), "csmv_bank_read_log")
+        return log_txn[:n_commits], outcome, result
+
+    def device_info(self) -> dict:
+        a, b, c_, d = C.c_int(), C.c_int(), C.c_int(), C.c_size_t()
+        _check(lib().csmv_bank_device_info(self._h, C.byref(a), C.byref(b), C.byref(c_),
+                                           C.byref(d)), "csmv_bank_device_info")
+        return {"n_sms": a.value, "ctas": b.value, "threads_per_cta": c_.value,
+                "device_bytes": d.value}
+
+
+def cuda_device_present() -> bool:
+    """True when a CUDA device is visible (checked through the library, no torch needed)."""
+    try:
+        cfg = bank_config(n_accounts=64, max_txn=32, ctas=1, client_warps=1)
+        Bank(cfg).close()
+        return True
+    except CsmvError as e:
+        return e.status not in (6,)
+    except RuntimeError:
+        return False
+
+

@@ -1,0 +1,396 @@
+// bank_engine.cu - C-ABI host side of the bank commit engine (include/csmv.h).
+//
+// Data layout in HBM (all item-major, allocated once per handle):
+//   slots  n_accounts * depth * 8 B   packed (ts << 32 | value) versions; depth 4 = one sector
+//   stamp  n_accounts * 4 B           commit timestamp of the latest committed writer
+//   ring   ring_size * 16 B           commit records {ts, n_writes, w0, w1}
+//   logs   max_txn * 12 B             log_txn[ts-1], outcome[txn], result[txn]
+//   sync   5 x 128 B lines            turn / ticket / clock / round cursor / error word
+#include <chrono>
+#include <cstring>
+#include <vector>
+
+#include "bank_kernel.cuh"
+#include "common.h"
+
+using namespace csmv;
+
+namespace {
+constexpr int kMaxR = 8;
+constexpr int kMaxW = 2;
+using KernelFn = void (*)(BankParams);
+
+KernelFn pick_kernel(uint32_t depth) {
+  switch (depth) {
+    case 2: return bank_kernel<2, kMaxR, kMaxW>;
+    case 4: return bank_kernel<4, kMaxR, kMaxW>;
+    case 8: return bank_kernel<8, kMaxR, kMaxW>;
+    case 16: return bank_kernel<16, kMaxR, kMaxW>;
+    default: return nullptr;
+  }
+}
+}  // namespace
+
+struct csmv_bank_t {
+  csmv_bank_config cfg{};
+  int n_sms = 0, ctas = 0, threads = 0;
+  size_t smem = 0, device_bytes = 0;
+  KernelFn kernel = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  unsigned long long* slots = nullptr;
+  uint32_t* stamp = nullptr;
+  uint4* ring = nullptr;
+  GlobalSync* gs = nullptr;
+  uint32_t* log_txn = nullptr;
+  uint32_t* outcome = nullptr;
+  int32_t* result = nullptr;
+  unsigned long long* stats = nullptr;
+  uint32_t* d_op = nullptr;
+  uint32_t* d_off = nullptr;
+  uint32_t* d_addr = nullptr;
+  uint64_t addr_cap = 0;
+  bool loaded = false;
+  uint32_t last_final_ts = 0, last_n_txn = 0, run_base_ts = 0;
+};
+
+extern "C" void csmv_bank_config_default(csmv_bank_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->n_accounts = 4096;
+  c->init_value = 1000;
+  c->version_depth = 4;
+  c->ring_size = 1u << 16;
+  c->client_warps = 15;
+  c->ctas = 0;
+  c->cluster_size = 2;
+  c->validate = CSMV_VALIDATE_STAMP;
+  c->writeback = CSMV_WRITEBACK_CLIENT;
+  c->batch = CSMV_BATCH_CTA;
+  c->prevalidate = 1;
+  c->log_commits = 1;
+  c->max_txn = 1u << 20;
+  c->spin_limit_log2 = 24;
+  c->device = 0;
+}
+
+static csmv_status validate_config(const csmv_bank_config* c) {
+  auto bad = [](const char* why) {
+    set_error("invalid bank config: %s", why);
+    return CSMV_ERR_INVALID_ARG;
+  };
+  if (!c) return bad("null");
+  if (c->n_accounts < 2) return bad("n_accounts < 2");
+  if (!pick_kernel(c->version_depth)) return bad("version_depth must be 2, 4, 8 or 16");
+  if (c->ring_size < 64 || (c->ring_size & (c->ring_size - 1))) return bad("ring_size");
+  if (c->client_warps < 1 || c->client_warps > (uint32_t)kMaxClientWarps) return bad("client_warps");
+  if (c->validate > CSMV_VALIDATE_RING_LANE) return bad("validate");
+  if (c->writeback > CSMV_WRITEBACK_SERVER) return bad("writeback");
+  if (c->batch > CSMV_BATCH_CTA) return bad("batch (cluster batching is not built)");
+  if (c->batch == CSMV_BATCH_LANE && c->writeback != CSMV_WRITEBACK_SERVER)
+    return bad("per-transaction sections need server write-back");
+  if (c->max_txn == 0 || c->max_txn % 32) return bad("max_txn must be a positive multiple of 32");
+  if (c->spin_limit_log2 < 10 || c->spin_limit_log2 > 30) return bad("spin_limit_log2");
+  return CSMV_OK;
+}
+
+static void free_all(csmv_bank_t* h) {
+  cudaFree(h->slots);
+  cudaFree(h->stamp);
+  cudaFree(h->ring);
+  cudaFree(h->gs);
+  cudaFree(h->log_txn);
+  cudaFree(h->outcome);
+  cudaFree(h->result);
+  cudaFree(h->stats);
+  cudaFree(h->d_op);
+  cudaFree(h->d_off);
+  cudaFree(h->d_addr);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+extern "C" csmv_status csmv_bank_create(const csmv_bank_config* cfg, csmv_bank_t** out) {
+  if (!out) return CSMV_ERR_INVALID_ARG;
+  *out = nullptr;
+  csmv_status st = validate_config(cfg);
+  if (st != CSMV_OK) return st;
+  int n_sms = 0;
+  if ((st = check_device(cfg->device, &n_sms)) != CSMV_OK) return st;
+  CSMV_CUDA(cudaSetDevice(cfg->device));
+  int coop = 0;
+  CSMV_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, cfg->device));
+  if (!coop) {
+    set_error("device does not support cooperative launch");
+    return CSMV_ERR_NO_DEVICE;
+  }
+  csmv_bank_t* h = new csmv_bank_t;
+  h->cfg = *cfg;
+  h->n_sms = n_sms;
+  h->kernel = pick_kernel(cfg->version_depth);
+  h->threads = (int)(cfg->client_warps + 1) * 32;
+  h->smem = cta_shared_bytes<kMaxR, kMaxW>(cfg->client_warps);
+  auto fail = [&](csmv_status s) {
+    free_all(h);
+    delete h;
+    return s;
+  };
+  if ((st = cuda_status(cudaFuncSetAttribute((const void*)h->kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)h->smem),
+                        "cudaFuncSetAttribute")) != CSMV_OK)
+    return fail(st);
+  int per_sm = 0;
+  if ((st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, h->kernel,
+                                                                       h->threads, h->smem),
+                        "occupancy")) != CSMV_OK)
+    return fail(st);
+  const int max_ctas = per_sm * n_sms;
+  if (max_ctas <= 0) {
+    set_error("kernel does not fit on an SM (threads %d, smem %zu)", h->threads, h->smem);
+    return fail(CSMV_ERR_INVALID_ARG);
+  }
+  h->ctas = cfg->ctas ? (int)cfg->ctas : max_ctas;
+  if (h->ctas > max_ctas) {
+    set_error("%d CTAs requested, only %d can be co-resident", h->ctas, max_ctas);
+    return fail(CSMV_ERR_INVALID_ARG);
+  }
+  const size_t n = cfg->n_accounts, D = cfg->version_depth;
+  struct {
+    void** p;
+    size_t bytes;
+  } allocs[] = {
+      {(void**)&h->slots, n * D * 8},       {(void**)&h->stamp, n * 4},
+      {(void**)&h->ring, (size_t)cfg->ring_size * 16}, {(void**)&h->gs, sizeof(GlobalSync)},
+      {(void**)&h->log_txn, (size_t)cfg->max_txn * 4}, {(void**)&h->outcome, (size_t)cfg->max_txn * 4},
+      {(void**)&h->result, (size_t)cfg->max_txn * 4},  {(void**)&h->stats, ST_COUNT * 8},
+      {(void**)&h->d_op, (size_t)cfg->max_txn * 4},    {(void**)&h->d_off, (size_t)cfg->max_txn * 4},
+  };
+  for (auto& a : allocs) {
+    if ((st = cuda_status(cudaMalloc(a.p, a.bytes), "cudaMalloc")) != CSMV_OK) return fail(st);
+    h->device_bytes += a.bytes;
+  }
+  if ((st = cuda_status(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream")) != CSMV_OK ||
+      (st = cuda_status(cudaEventCreate(&h->ev0), "event")) != CSMV_OK ||
+      (st = cuda_status(cudaEventCreate(&h->ev1), "event")) != CSMV_OK)
+    return fail(st);
+  *out = h;
+  return CSMV_OK;
+}
+
+extern "C" csmv_status csmv_bank_load(csmv_bank_t* h, const int32_t* host_values) {
+  if (!h) return CSMV_ERR_INVALID_ARG;
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  const size_t n = h->cfg.n_accounts, D = h->cfg.version_depth;
+  std::vector<unsigned long long> slots(n * D, 0xFFFFFFFFull << 32);
+  for (size_t i = 0; i < n; i++)
+    slots[i * D] = (uint32_t)(host_values ? host_values[i] : h->cfg.init_value);  // ts 0
+  CSMV_CUDA(cudaMemcpyAsync(h->slots, slots.data(), n * D * 8, cudaMemcpyHostToDevice, h->stream));
+  CSMV_CUDA(cudaMemsetAsync(h->stamp, 0, n * 4, h->stream));
+  CSMV_CUDA(cudaMemsetAsync(h->ring, 0, (size_t)h->cfg.ring_size * 16, h->stream));
+  CSMV_CUDA(cudaMemsetAsync(h->gs, 0, sizeof(GlobalSync), h->stream));
+  CSMV_CUDA(cudaStreamSynchronize(h->stream));
+  h->loaded = true;
+  h->last_final_ts = 0;
+  h->last_n_txn = 0;
+  return CSMV_OK;
+}
+
+static csmv_status check_stream(const csmv_bank_t* h, const csmv_bank_stream* s) {
+  if (!s || !s->op || !s->off || !s->addr || s->n_txn == 0 || s->n_txn % 32) {
+    set_error("stream: n_txn must be a positive multiple of 32 with op/off/addr set");
+    return CSMV_ERR_INVALID_ARG;
+  }
+  if (s->n_txn > h->cfg.max_txn) {
+    set_error("stream of %u transactions exceeds max_txn %u", s->n_txn, h->cfg.max_txn);
+    return CSMV_ERR_CAPACITY;
+  }
+  return CSMV_OK;
+}
+
+static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* off,
+                          const uint32_t* addr, uint32_t n_txn, csmv_stats* out) {
+  const csmv_bank_config& c = h->cfg;
+  BankParams p{};
+  p.op = op;
+  p.off = off;
+  p.addr = addr;
+  p.n_rounds = n_txn / 32;
+  p.n_items = c.n_accounts;
+  p.slots = h->slots;
+  p.stamp = h->stamp;
+  p.ring = h->ring;
+  p.ring_mask = c.ring_size - 1;
+  p.gs = h->gs;
+  p.log_txn = h->log_txn;
+  p.outcome = h->outcome;
+  p.result = h->result;
+  p.stats = h->stats;
+  p.log = c.log_commits;
+  p.log_base = h->last_final_ts;
+  p.nc = c.client_warps;
+  p.validate = c.validate;
+  p.writeback = c.writeback;
+  p.batch = c.batch;
+  p.prevalidate = c.prevalidate;
+  p.spin_log2 = c.spin_limit_log2;
+  // the commit order carries on from the previous run: only the cursor and error reset
+  CSMV_CUDA(cudaMemsetAsync(&h->gs->round_next, 0, 4, h->stream));
+  CSMV_CUDA(cudaMemsetAsync(&h->gs->error, 0, 4, h->stream));
+  CSMV_CUDA(cudaMemsetAsync(h->stats, 0, ST_COUNT * 8, h->stream));
+  void* args[] = {&p};
+  CSMV_CUDA(cudaEventRecord(h->ev0, h->stream));
+  CSMV_CUDA(cudaLaunchCooperativeKernel((const void*)h->kernel, dim3(h->ctas), dim3(h->threads),
+                                        args, h->smem, h->stream));
+  CSMV_CUDA(cudaEventRecord(h->ev1, h->stream));
+  unsigned long long st[ST_COUNT];
+  GlobalSync gs;
+  CSMV_CUDA(cudaMemcpyAsync(st, h->stats, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  CSMV_CUDA(cudaMemcpyAsync(&gs, h->gs, sizeof(gs), cudaMemcpyDeviceToHost, h->stream));
+  CSMV_CUDA(cudaStreamSynchronize(h->stream));
+  float ms = 0;
+  CSMV_CUDA(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+  const uint32_t final_ts = (uint32_t)(gs.turn >> 32);
+  h->last_n_txn = n_txn;
+  h->run_base_ts = h->last_final_ts;
+  h->last_final_ts = final_ts;
+  if (out) {
+    out->commits_update = st[ST_COMMIT_UPDATE];
+    out->commits_readonly = st[ST_COMMIT_RO];
+    out->commits_nowrite = st[ST_COMMIT_NOWRITE];
+    out->aborts_data_age = st[ST_ABORT_DATA_AGE];
+    out->aborts_record_age = st[ST_ABORT_RECORD_AGE];
+    out->aborts_read_write = st[ST_ABORT_READ_WRITE];
+    out->aborts_prevalid = st[ST_ABORT_PREVALID];
+    out->sections = st[ST_SECTIONS];
+    out->rounds = st[ST_ROUNDS];
+    out->final_ts = final_ts;
+    out->error = gs.error;
+    out->kernel_ms = ms;
+  }
+  if (gs.error) {
+    set_error("device error %u (1 turn, 2 clock, 3 reply, 4 request, 5 capacity, 6 data)",
+              gs.error);
+    return gs.error == ERR_DATA ? CSMV_ERR_INVALID_ARG : CSMV_ERR_TIMEOUT;
+  }
+  return CSMV_OK;
+}
+
+extern "C" csmv_status csmv_bank_run_device(csmv_bank_t* h, const csmv_bank_stream* s,
+                                            csmv_stats* out) {
+  if (!h) return CSMV_ERR_INVALID_ARG;
+  if (!h->loaded) {
+    set_error("csmv_bank_load must come first");
+    return CSMV_ERR_STATE;
+  }
+  csmv_status st = check_stream(h, s);
+  if (st != CSMV_OK) return st;
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  auto t0 = std::chrono::steady_clock::now();
+  st = launch(h, s->op, s->off, s->addr, s->n_txn, out);
+  if (out)
+    out->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return st;
+}
+
+extern "C" csmv_status csmv_bank_run(csmv_bank_t* h, const csmv_bank_stream* s, csmv_stats* out) {
+  if (!h) return CSMV_ERR_INVALID_ARG;
+  if (!h->loaded) {
+    set_error("csmv_bank_load must come first");
+    return CSMV_ERR_STATE;
+  }
+  csmv_status st = check_stream(h, s);
+  if (st != CSMV_OK) return st;
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  auto t0 = std::chrono::steady_clock::now();
+  if (s->n_addr > h->addr_cap) {
+    cudaFree(h->d_addr);
+    h->d_addr = nullptr;
+    h->addr_cap = 0;
+    CSMV_CUDA(cudaMalloc(&h->d_addr, s->n_addr * 4));
+    h->addr_cap = s->n_addr;
+  }
+  CSMV_CUDA(cudaMemcpyAsync(h->d_op, s->op, (size_t)s->n_txn * 4, cudaMemcpyHostToDevice, h->stream));
+  CSMV_CUDA(cudaMemcpyAsync(h->d_off, s->off, (size_t)s->n_txn * 4, cudaMemcpyHostToDevice, h->stream));
+  CSMV_CUDA(cudaMemcpyAsync(h->d_addr, s->addr, s->n_addr * 4, cudaMemcpyHostToDevice, h->stream));
+  st = launch(h, h->d_op, h->d_off, h->d_addr, s->n_txn, out);
+  if (out)
+    out->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return st;
+}
+
+extern "C" csmv_status csmv_bank_read_versions(csmv_bank_t* h, uint64_t* host_slots) {
+  if (!h || !host_slots) return CSMV_ERR_INVALID_ARG;
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  CSMV_CUDA(cudaMemcpy(host_slots, h->slots, (size_t)h->cfg.n_accounts * h->cfg.version_depth * 8,
+                       cudaMemcpyDeviceToHost));
+  return CSMV_OK;
+}
+
+extern "C" csmv_status csmv_bank_read_values(csmv_bank_t* h, int32_t* host_values) {
+  if (!h || !host_values) return CSMV_ERR_INVALID_ARG;
+  const size_t n = h->cfg.n_accounts, D = h->cfg.version_depth;
+  std::vector<uint64_t> slots(n * D);
+  csmv_status st = csmv_bank_read_versions(h, slots.data());
+  if (st != CSMV_OK) return st;
+  for (size_t i = 0; i < n; i++) {  // newest version = largest ts (the reference's head)
+    uint32_t best_ts = 0;
+    int32_t v = 0;
+    bool any = false;
+    for (size_t d = 0; d < D; d++) {
+      const uint64_t s = slots[i * D + d];
+      const uint32_t ts = (uint32_t)(s >> 32);
+      if (ts == 0xFFFFFFFFu) continue;
+      if (!any || ts > best_ts) {
+        any = true;
+        best_ts = ts;
+        v = (int32_t)(uint32_t)s;
+      }
+    }
+    host_values[i] = v;
+  }
+  return CSMV_OK;
+}
+
+extern "C" csmv_status csmv_bank_read_log(csmv_bank_t* h, uint32_t* host_log_txn, uint32_t n_log,
+                                          uint32_t* host_outcome, int32_t* host_result,
+                                          uint32_t n_txn) {
+  if (!h) return CSMV_ERR_INVALID_ARG;
+  if (!h->cfg.log_commits) {
+    set_error("handle was created with log_commits = 0");
+    return CSMV_ERR_STATE;
+  }
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  const uint32_t commits = h->last_final_ts - h->run_base_ts;
+  if (host_log_txn) {
+    if (n_log < commits) {
+      set_error("log buffer holds %u entries, run committed %u", n_log, commits);
+      return CSMV_ERR_CAPACITY;
+    }
+    // entry k holds the transaction that committed with ts = run_base_ts + k + 1
+    CSMV_CUDA(cudaMemcpy(host_log_txn, h->log_txn, (size_t)commits * 4,
+                         cudaMemcpyDeviceToHost));
+  }
+  if (n_txn > h->last_n_txn) n_txn = h->last_n_txn;
+  if (host_outcome) CSMV_CUDA(cudaMemcpy(host_outcome, h->outcome, (size_t)n_txn * 4, cudaMemcpyDeviceToHost));
+  if (host_result) CSMV_CUDA(cudaMemcpy(host_result, h->result, (size_t)n_txn * 4, cudaMemcpyDeviceToHost));
+  return CSMV_OK;
+}
+
+extern "C" csmv_status csmv_bank_device_info(csmv_bank_t* h, int* n_sms, int* ctas,
+                                             int* threads_per_cta, size_t* device_bytes) {
+  if (!h) return CSMV_ERR_INVALID_ARG;
+  if (n_sms) *n_sms = h->n_sms;
+  if (ctas) *ctas = h->ctas;
+  if (threads_per_cta) *threads_per_cta = h->threads;
+  if (device_bytes) *device_bytes = h->device_bytes + h->addr_cap * 4;
+  return CSMV_OK;
+}
+
+extern "C" void csmv_bank_destroy(csmv_bank_t* h) {
+  if (!h) return;
+  cudaSetDevice(h->cfg.device);
+  free_all(h);
+  delete h;
+}

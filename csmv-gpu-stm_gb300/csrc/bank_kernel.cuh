@@ -1,0 +1,703 @@
+// bank_kernel.cuh - persistent CSMV commit kernel for the bank workload (sm_103a).
+//
+// Reference structure (bank/csmv_sh/exe.cu:89-338, sync_lib/*): client warps in many blocks send
+// (tid, snapshot) messages through a global-memory ring to ONE server block; a leader warp hands
+// 32-message chunks to worker warps, which validate against a commit-record ring in that block's
+// shared memory, take a commit timestamp with a CAS on w_hp, answer through a global scoreboard,
+// and client warps write back and advance a global clock one warp at a time.
+//
+// GB300 structure (one kernel, every CTA alike, all CTAs co-resident via cooperative launch):
+//  * warps 1..nc of a CTA are client warps; warp 0 is that CTA's commit server;
+//  * a client warp posts its candidates' read/write sets straight into a shared-memory mailbox
+//    slot (the csmv_sh form: no global message ring, no leader dispatch) and waits on a
+//    shared-memory reply word;
+//  * the server drains every ready mailbox into one batch, removes intra-batch conflicts with a
+//    shared-memory hash of the batch's writes, takes a ticket on the global commit order and,
+//    when its turn comes, validates the survivors against everything committed meanwhile
+//    (per-item commit stamps, or the commit-record ring), gives them consecutive timestamps,
+//    publishes stamps/records/log and passes the turn on with a single release store that also
+//    carries the next free timestamp;
+//  * client warps write back, and the last warp of a batch advances the global clock once for the
+//    whole batch (the reference advances it once per warp).
+#pragma once
+#include <cstdint>
+
+#include "../../include/csmv.h"
+#include "../../include/csmv_tx.cuh"
+#include "csmv_prims.cuh"
+
+namespace csmv {
+
+constexpr uint32_t kSnapFlag = 0x80000000u;
+constexpr int kMaxClientWarps = 31;
+constexpr int kHashSize = 4096;  // shared-memory hash entries (power of two)
+constexpr int kBatchDescs = 32;
+
+enum StatIdx {
+  ST_COMMIT_UPDATE,
+  ST_COMMIT_RO,
+  ST_COMMIT_NOWRITE,
+  ST_ABORT_DATA_AGE,
+  ST_ABORT_RECORD_AGE,
+  ST_ABORT_READ_WRITE,
+  ST_ABORT_PREVALID,
+  ST_SECTIONS,
+  ST_ROUNDS,
+  ST_COUNT
+};
+
+// Global words of the commit order. Each hot word sits on its own 128-byte line so pollers of
+// one do not contend with writers of another.
+struct alignas(128) GlobalSync {
+  alignas(128) unsigned long long turn;  // low 32: ticket now served, high 32: last commit ts
+  alignas(128) uint32_t ticket;          // next ticket
+  alignas(128) uint32_t clock;           // every commit with ts <= clock is written back
+  alignas(128) uint32_t round_next;      // next unclaimed round of the stream
+  alignas(128) uint32_t error;           // first device error (ERR_*)
+};
+
+struct BankParams {
+  const uint32_t* op;
+  const uint32_t* off;
+  const uint32_t* addr;
+  uint32_t n_rounds;
+  uint32_t n_items;
+  unsigned long long* slots;
+  uint32_t* stamp;
+  uint4* ring;  // {ts, n_writes, w0, w1}
+  uint32_t ring_mask;
+  GlobalSync* gs;
+  uint32_t* log_txn;
+  uint32_t* outcome;
+  int32_t* result;
+  unsigned long long* stats;  // [ST_COUNT]
+  uint32_t log;
+  uint32_t log_base;  // last commit ts before this run: log_txn is indexed by ts-1-log_base
+  uint32_t nc;  // client warps per CTA
+  uint32_t validate, writeback, batch, prevalidate;
+  uint32_t spin_log2;
+};
+
+template <int MAXR, int MAXW>
+struct MailSlot {
+  uint32_t req, rep;       // request / reply sequence numbers
+  uint32_t snap, cand;     // request: snapshot, candidate lanes
+  uint32_t ok, bid;        // reply: committed lanes, batch descriptor of the clock advance
+  uint32_t tsl[32];        // reply: commit timestamp of each committed lane
+  uint32_t rs[MAXR][32];   // read sets, transposed (lane-contiguous: no bank conflicts)
+  uint32_t ws[MAXW][32];
+  int32_t wv[MAXW][32];
+  uint32_t n[32];          // nreads | nwrites << 8
+  uint32_t txn[32];
+};
+
+struct BatchDesc {
+  uint32_t first_ts, last_ts, remaining, pad;
+};
+
+template <int MAXR, int MAXW>
+struct CtaShared {
+  uint32_t done_warps;
+  uint32_t next_bid;
+  uint32_t pad[2];
+  unsigned long long stat[ST_COUNT];
+  BatchDesc batch[kBatchDescs];
+  uint32_t hkey[kHashSize];
+  uint32_t hval[kHashSize];
+  uint32_t conflict[32];  // ring mode: per-warp conflict lanes
+  uint32_t recage[32];    // ring mode: per-warp record-age lanes
+  uint32_t snaps[32];     // snapshot of each batch warp
+  MailSlot<MAXR, MAXW> mail[1];        // nc slots (dynamic shared memory)
+};
+
+template <int MAXR, int MAXW>
+__host__ __device__ constexpr size_t cta_shared_bytes(uint32_t nc) {
+  return sizeof(CtaShared<MAXR, MAXW>) + (nc - 1) * sizeof(MailSlot<MAXR, MAXW>);
+}
+
+__device__ __forceinline__ uint32_t hash_addr(uint32_t a) {
+  a *= 0x9E3779B1u;
+  return (a ^ (a >> 15)) & (kHashSize - 1);
+}
+
+__device__ __forceinline__ void stat_add(unsigned long long* s, int idx, uint32_t v) {
+  if (v) atomicAdd(&s[idx], (unsigned long long)v);
+}
+
+// ---------------------------------------------------------------------------------------------
+// client side
+// ---------------------------------------------------------------------------------------------
+
+// Last client warp of a batch publishes the batch on the clock, after every earlier batch.
+// (The reference: each warp leader spins until globalClock == ts-1, then adds its commits,
+// batchedAtrInsert/csmv_sh/API.cu:257-261.)
+template <int MAXR, int MAXW>
+__device__ __forceinline__ void batch_done(const BankParams& p, CtaShared<MAXR, MAXW>& sm,
+                                           uint32_t bid) {
+  BatchDesc& d = sm.batch[bid];
+  const uint32_t first = d.first_ts, last = d.last_ts;
+  __threadfence();
+  if (atomicSub(&d.remaining, 1u) == 1u) {
+    __threadfence();
+    if (bounded_wait([&] { return ld_acquire_gpu(&p.gs->clock) == first - 1u; }, &p.gs->error,
+                     ERR_WAIT_CLOCK, p.spin_log2))
+      st_release_gpu(&p.gs->clock, last);
+  }
+}
+
+template <int DEPTH, int MAXR, int MAXW>
+__device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint32_t w) {
+  MailSlot<MAXR, MAXW>& ms = sm.mail[w];
+  const uint32_t lane = lane_id();
+  const VersionStore vs{p.slots, p.n_items};
+  uint32_t seq = 0;
+  bool failed = false;
+  for (;;) {
+    uint32_t g = 0;
+    if (lane == 0) g = atomicAdd(&p.gs->round_next, 1u);
+    g = __shfl_sync(0xFFFFFFFFu, g, 0);
+    if (g >= p.n_rounds) break;
+    const uint32_t t = g * 32u + lane;
+    const uint32_t op = p.op[t];
+    const uint32_t kind = CSMV_OP_KIND(op), nr = CSMV_OP_NREADS(op);
+    const uint32_t off = p.off[t];
+    const bool ro = (kind == CSMV_KIND_READONLY);
+    if (!ro && (nr < 2 || nr > (uint32_t)MAXR)) {
+      raise_error(&p.gs->error, ERR_DATA);
+      failed = true;
+    }
+    if (__any_sync(0xFFFFFFFFu, failed)) break;
+    uint32_t a[MAXR];
+    bool bad_addr = false;
+#pragma unroll
+    for (int k = 0; k < MAXR; k++) {
+      a[k] = (!ro && k < (int)nr) ? p.addr[off + k] : 0u;
+      bad_addr |= a[k] >= p.n_items;
+    }
+    if (ro)
+      for (uint32_t k = 0; k < nr; k++) bad_addr |= p.addr[off + k] >= p.n_items;
+    if (bad_addr) raise_error(&p.gs->error, ERR_DATA);  // no access outside the accounts
+    if (__any_sync(0xFFFFFFFFu, bad_addr)) {
+      failed = true;
+      break;
+    }
+
+    uint32_t pending = 0xFFFFFFFFu;
+    while (pending) {
+      if (lane == 0) atomicAdd(&sm.stat[ST_ROUNDS], 1ull);
+      const bool mine = (pending >> lane) & 1u;
+      ReadSet<MAXR> rs;
+      WriteSet<MAXW> ws;
+      uint32_t snap = 0;
+      if (lane == 0) snap = TXBegin(&p.gs->clock, rs, ws);
+      rs.n = 0;
+      ws.n = 0;
+      snap = __shfl_sync(0xFFFFFFFFu, snap, 0);
+      bool aborted = false;
+
+      if (ro) {  // read-only: consistent snapshot read, commits without validation
+        uint32_t s = 0;
+        if (mine)
+          for (uint32_t k0 = 0; k0 < nr; k0 += 8) {  // 8 independent version loads in flight
+            uint32_t ad[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) ad[j] = k0 + j < nr ? p.addr[off + k0 + j] : 0u;
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+              if (k0 + j < nr) s += (uint32_t)TXReadOnly<DEPTH>(vs, ad[j], snap, &aborted);
+          }
+        const bool done = mine && !aborted;
+        if (done && p.log) {
+          p.outcome[t] = snap | kSnapFlag;
+          p.result[t] = (int32_t)s;
+        }
+        const uint32_t dm = __ballot_sync(0xFFFFFFFFu, done);
+        const uint32_t am = __ballot_sync(0xFFFFFFFFu, mine && aborted);
+        if (lane == 0) {
+          stat_add(sm.stat, ST_COMMIT_RO, __popc(dm));
+          stat_add(sm.stat, ST_ABORT_DATA_AGE, __popc(am));
+        }
+        pending &= ~dm;
+        continue;
+      }
+
+      // transfer: read everything at the snapshot, then compute the writes
+      int32_t v[MAXR];
+#pragma unroll
+      for (int k = 0; k < MAXR; k++) {
+        v[k] = 0;
+        if (mine && k < (int)nr) v[k] = TXRead<DEPTH>(vs, a[k], snap, rs, ws, &aborted);
+      }
+      bool has_w = false;
+      if (mine && !aborted) {
+        uint32_t acc = CSMV_OP_AMT0(op) - 1u;
+#pragma unroll
+        for (int k = 2; k < MAXR; k++)
+          if (k < (int)nr) acc += (uint32_t)v[k];
+        const uint32_t amt = 1u + acc % CSMV_OP_AMOD(op);
+        if (kind == CSMV_KIND_TRANSFER_ALWAYS || v[0] >= (int32_t)amt) {
+          TXWrite(a[0], (int32_t)((uint32_t)v[0] - amt), ws);
+          TXWrite(a[1], (int32_t)((uint32_t)v[1] + amt), ws);
+          has_w = true;
+        }
+      }
+      const bool nowrite = mine && !aborted && !has_w;
+      if (nowrite && p.log) {
+        p.outcome[t] = snap | kSnapFlag;
+        p.result[t] = 0;
+      }
+      const uint32_t nwm = __ballot_sync(0xFFFFFFFFu, nowrite);
+      const uint32_t am = __ballot_sync(0xFFFFFFFFu, mine && aborted);
+      uint32_t cand = __ballot_sync(0xFFFFFFFFu, mine && !aborted && has_w);
+      if (lane == 0) {
+        stat_add(sm.stat, ST_COMMIT_NOWRITE, __popc(nwm));
+        stat_add(sm.stat, ST_ABORT_DATA_AGE, __popc(am));
+      }
+      pending &= ~nwm;
+      if (cand == 0) continue;
+      if (p.prevalidate) {
+        const uint32_t pass = TXPreValidation(rs, ws, (cand >> lane) & 1u);
+        if (lane == 0) stat_add(sm.stat, ST_ABORT_PREVALID, __popc(cand & ~pass));
+        cand = pass;
+        if (cand == 0) continue;
+      }
+      // post the request into the shared-memory mailbox
+      if ((cand >> lane) & 1u) {
+#pragma unroll
+        for (int k = 0; k < MAXR; k++) ms.rs[k][lane] = rs.addr[k];
+#pragma unroll
+        for (int k = 0; k < MAXW; k++) {
+          ms.ws[k][lane] = ws.addr[k];
+          ms.wv[k][lane] = ws.val[k];
+        }
+        ms.n[lane] = rs.n | (ws.n << 8);
+        ms.txn[lane] = t;
+      }
+      seq++;
+      __syncwarp();
+      if (lane == 0) {
+        ms.snap = snap;
+        ms.cand = cand;
+        st_release_cta(&ms.req, seq);
+      }
+      bool ok_wait = true;
+      if (lane == 0)
+        ok_wait = bounded_wait([&] { return ld_acquire_cta(&ms.rep) == seq; }, &p.gs->error,
+                               ERR_WAIT_REPLY, p.spin_log2);
+      ok_wait = __shfl_sync(0xFFFFFFFFu, ok_wait, 0);
+      if (!ok_wait) {
+        failed = true;
+        break;
+      }
+      (void)ld_acquire_cta(&ms.rep);
+      const uint32_t okm = ms.ok, bid = ms.bid;
+      const bool committed = (okm >> lane) & 1u;
+      const uint32_t my_ts = committed ? ms.tsl[lane] : 0u;
+      if (committed && p.log) {
+        p.outcome[t] = my_ts;
+        p.result[t] = 0;
+      }
+      if (p.writeback == CSMV_WRITEBACK_CLIENT && okm) {
+        if (committed) TXWriteBack<DEPTH>(my_ts, vs, ws);
+        __syncwarp();
+        if (lane == 0) batch_done(p, sm, bid);
+      }
+      __syncwarp();
+      if (lane == 0) stat_add(sm.stat, ST_COMMIT_UPDATE, __popc(okm));
+      pending &= ~okm;
+      if (ld_relaxed_gpu(&p.gs->error) != 0) {
+        failed = true;
+        break;
+      }
+    }
+    if (failed) break;
+  }
+  __syncwarp();
+  if (lane == 0) atomicAdd(&sm.done_warps, 1u);
+}
+
+// ---------------------------------------------------------------------------------------------
+// server side (TXAddToRecord)
+// ---------------------------------------------------------------------------------------------
+
+// Intra-warp resolution on the server when clients skip pre-validation: the same lane-order rule
+// as TXPreValidation, over the sets in the mailbox.
+template <int MAXR, int MAXW>
+__device__ __forceinline__ uint32_t server_lane_order(const MailSlot<MAXR, MAXW>& ms,
+                                                      uint32_t cand) {
+  const uint32_t lane = lane_id();
+  const bool active = (cand >> lane) & 1u;
+  const uint32_t nrs = ms.n[lane] & 0xFFu;
+  uint32_t conflict = 0;
+  for (uint32_t i = 0; i < lane; i++) {
+    if (!((cand >> i) & 1u)) continue;
+    const uint32_t nw = ms.n[i] >> 8;
+    for (uint32_t j = 0; j < nw; j++) {
+      const uint32_t a = ms.ws[j][i];
+      for (uint32_t k = 0; k < nrs; k++)
+        if (ms.rs[k][lane] == a) conflict |= 1u << i;
+    }
+  }
+  uint32_t commit = 0;
+  for (uint32_t i = 0; i < 32; i++)
+    commit |= __ballot_sync(0xFFFFFFFFu, lane == i && active && (conflict & commit) == 0);
+  return commit;
+}
+
+template <int MAXR, int MAXW>
+__device__ __forceinline__ void hash_clear(CtaShared<MAXR, MAXW>& sm) {
+  uint4* k = reinterpret_cast<uint4*>(sm.hkey);
+  for (uint32_t i = lane_id(); i < kHashSize / 4; i += 32) k[i] = make_uint4(~0u, ~0u, ~0u, ~0u);
+  __syncwarp();
+}
+
+// set insert (write addresses of the batch's survivors); __match_any_sync lets one lane insert
+// per distinct address when several lanes write the same (hot) item.
+template <int MAXR, int MAXW>
+__device__ __forceinline__ void hash_insert_set(CtaShared<MAXR, MAXW>& sm, uint32_t a, bool act) {
+  const uint32_t peers = __match_any_sync(0xFFFFFFFFu, act ? a : 0xFFFFFFFFu);
+  if (!act || (__ffs(peers) - 1) != (int)lane_id()) return;
+  uint32_t h = hash_addr(a);
+  for (uint32_t probe = 0; probe < kHashSize; probe++) {
+    const uint32_t prev = atomicCAS(&sm.hkey[h], 0xFFFFFFFFu, a);
+    if (prev == 0xFFFFFFFFu || prev == a) return;
+    h = (h + 1) & (kHashSize - 1);
+  }
+}
+
+template <int MAXR, int MAXW>
+__device__ __forceinline__ bool hash_contains(const CtaShared<MAXR, MAXW>& sm, uint32_t a) {
+  uint32_t h = hash_addr(a);
+  for (uint32_t probe = 0; probe < kHashSize; probe++) {
+    const uint32_t k = sm.hkey[h];
+    if (k == a) return true;
+    if (k == 0xFFFFFFFFu) return false;
+    h = (h + 1) & (kHashSize - 1);
+  }
+  return false;
+}
+
+// multimap insert for the ring-mode read hash: (address -> candidate id), duplicates kept
+template <int MAXR, int MAXW>
+__device__ __forceinline__ bool hash_insert_multi(CtaShared<MAXR, MAXW>& sm, uint32_t a,
+                                                  uint32_t cid) {
+  uint32_t h = hash_addr(a);
+  for (uint32_t probe = 0; probe < kHashSize; probe++) {
+    if (atomicCAS(&sm.hkey[h], 0xFFFFFFFFu, a) == 0xFFFFFFFFu) {
+      sm.hval[h] = cid;
+      return true;
+    }
+    h = (h + 1) & (kHashSize - 1);
+  }
+  return false;
+}
+
+// Ring-mode scan of committed records with ts in (lo, hi]: lanes stride over records; each
+// record's write addresses probe the batch read hash; a hit on a candidate whose snapshot is
+// older than the record marks a conflict (collabValidation/csmv_sh/API.cu:212-253, with one scan
+// per batch instead of one per lane). A record overwritten since (ts mismatch) marks RecordAge
+// for every candidate older than it.
+template <int MAXR, int MAXW>
+__device__ void ring_scan(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint32_t lo,
+                          uint32_t hi, const uint32_t* snaps /* per batch warp, smem */,
+                          uint32_t bwarps) {
+  for (uint32_t t = lo + 1 + lane_id(); t <= hi; t += 32) {
+    const uint4 r = p.ring[t & p.ring_mask];
+    if (r.x != t) {  // overwritten: every candidate older than t loses its proof
+      for (uint32_t m = bwarps; m; m &= m - 1) {
+        const uint32_t w = __ffs(m) - 1;
+        if (snaps[w] < t) atomicOr(&sm.recage[w], 0xFFFFFFFFu);
+      }
+      continue;
+    }
+    for (uint32_t j = 0; j < r.y && j < 2; j++) {
+      const uint32_t a = j == 0 ? r.z : r.w;
+      uint32_t h = hash_addr(a);
+      for (uint32_t probe = 0; probe < kHashSize; probe++) {
+        const uint32_t k = sm.hkey[h];
+        if (k == 0xFFFFFFFFu) break;
+        if (k == a) {
+          const uint32_t cid = sm.hval[h], w = cid >> 5;
+          if (snaps[w] < t) atomicOr(&sm.conflict[w], 1u << (cid & 31u));
+        }
+        h = (h + 1) & (kHashSize - 1);
+      }
+    }
+  }
+  __syncwarp();
+}
+
+template <int DEPTH, int MAXR, int MAXW>
+__device__ void server_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
+  const uint32_t lane = lane_id();
+  const uint32_t nc = p.nc;
+  uint32_t seen = 0;  // lane w < nc: last request seq handled for client warp w
+  uint32_t* snaps = sm.snaps;
+  uint64_t idle = 0;
+  const uint64_t idle_limit = 1ull << (p.spin_log2 + 2);
+  const VersionStore vs{p.slots, p.n_items};
+
+  for (;;) {
+    uint32_t req = 0;
+    if (lane < nc) req = ld_acquire_cta(&sm.mail[lane].req);
+    uint32_t ready = __ballot_sync(0xFFFFFFFFu, lane < nc && req != seen);
+    if (ready == 0) {
+      uint32_t done = 0, err = 0;
+      if (lane == 0) {
+        done = *(volatile uint32_t*)&sm.done_warps;
+        err = ld_relaxed_gpu(&p.gs->error);
+      }
+      done = __shfl_sync(0xFFFFFFFFu, done, 0);
+      err = __shfl_sync(0xFFFFFFFFu, err, 0);
+      if (done == nc || err) break;
+      if (++idle > idle_limit) {
+        if (lane == 0) raise_error(&p.gs->error, ERR_WAIT_REQUEST);
+        break;
+      }
+      __nanosleep(64);
+      continue;
+    }
+    idle = 0;
+    if (p.batch != CSMV_BATCH_CTA) ready &= (0u - ready);  // lowest ready warp only
+    if (p.validate != CSMV_VALIDATE_STAMP) {                // read hash must fit: cap the batch
+      uint32_t capped = 0, entries = 0;
+      for (uint32_t m = ready; m; m &= m - 1) {
+        const uint32_t w = __ffs(m) - 1;
+        if (capped && entries + 32u * MAXR > kHashSize / 2) break;
+        capped |= 1u << w;
+        entries += 32u * MAXR;
+      }
+      ready = capped;
+    }
+    if (lane < nc && ((ready >> lane) & 1u)) {
+      seen = req;
+      snaps[lane] = sm.mail[lane].snap;
+    }
+    __syncwarp();
+    // every lane reads every batch mailbox: each takes its own acquire on the request word
+    for (uint32_t m = ready; m; m &= m - 1) (void)ld_acquire_cta(&sm.mail[__ffs(m) - 1].req);
+
+    // ---- phase A: candidates, intra-batch conflicts (outside the commit section) ----
+    uint32_t surv_of_me = 0;  // lane w: survivors of client warp w
+    const bool multi = __popc(ready) > 1;
+    if (multi) hash_clear(sm);
+    uint32_t stat_rw = 0;
+    for (uint32_t m = ready; m; m &= m - 1) {
+      const uint32_t w = __ffs(m) - 1;
+      const MailSlot<MAXR, MAXW>& ms = sm.mail[w];
+      uint32_t cand = ms.cand;
+      if (!p.prevalidate) {
+        const uint32_t pass = server_lane_order(ms, cand);
+        stat_rw += __popc(cand & ~pass);
+        cand = pass;
+      }
+      const bool c = (cand >> lane) & 1u;
+      const uint32_t n = ms.n[lane], nrs = n & 0xFFu, nws = n >> 8;
+      bool hit = false;
+      if (multi && c)
+        for (uint32_t k = 0; k < nrs && !hit; k++) hit = hash_contains(sm, ms.rs[k][lane]);
+      const uint32_t s = __ballot_sync(0xFFFFFFFFu, c && !hit);
+      stat_rw += __popc(cand & ~s);
+      if (multi) {
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < MAXW; k++) hash_insert_set(sm, ms.ws[k][lane], ((s >> lane) & 1u) && k < (int)nws);
+        __syncwarp();
+      }
+      if (lane == w) surv_of_me = s;
+    }
+
+    // ring modes: build the batch read hash and pre-scan up to the current frontier
+    uint32_t pre_hi = 0;
+    const bool ring = p.validate != CSMV_VALIDATE_STAMP;
+    if (ring) {
+      hash_clear(sm);
+      if (lane < nc) {
+        sm.conflict[lane] = 0;
+        sm.recage[lane] = 0;
+      }
+      __syncwarp();
+      for (uint32_t m = ready; m; m &= m - 1) {
+        const uint32_t w = __ffs(m) - 1;
+        const uint32_t s = __shfl_sync(0xFFFFFFFFu, surv_of_me, w);
+        const MailSlot<MAXR, MAXW>& ms = sm.mail[w];
+        if ((s >> lane) & 1u) {
+          const uint32_t nrs = ms.n[lane] & 0xFFu;
+          for (uint32_t k = 0; k < nrs; k++) hash_insert_multi(sm, ms.rs[k][lane], w * 32 + lane);
+        }
+      }
+      __syncwarp();
+      uint32_t lo = 0xFFFFFFFFu;
+      for (uint32_t m = ready; m; m &= m - 1) lo = min(lo, snaps[__ffs(m) - 1]);
+      if (lane == 0) pre_hi = (uint32_t)(ld_acquire_gpu(&p.gs->turn) >> 32);
+      pre_hi = __shfl_sync(0xFFFFFFFFu, pre_hi, 0);
+      const uint32_t floor_ts = pre_hi > p.ring_mask ? pre_hi - p.ring_mask : 0u;
+      if (lo < floor_ts) lo = floor_ts;  // older snapshots fail the RecordAge rule anyway
+      if (lo < pre_hi) ring_scan(p, sm, lo, pre_hi, snaps, ready);
+    }
+
+    // ---- phases B-E, once per commit section: a CTA/warp batch is one section; the plain
+    // form (CSMV_BATCH_LANE) commits one transaction per section like the reference's per-lane
+    // CAS loop (bank/csmv_sh/API.cu:218-265) ----
+    const bool lane_sections = p.batch == CSMV_BATCH_LANE;
+    uint32_t todo_of_me = surv_of_me, done_of_me = 0;
+    uint32_t scanned_hi = pre_hi;
+    uint32_t stat_ra = 0, bid = 0;
+    bool aborted_run = false;
+    while (__any_sync(0xFFFFFFFFu, todo_of_me != 0)) {
+      uint32_t sec_of_me = lane_sections ? (todo_of_me & (0u - todo_of_me)) : todo_of_me;
+      todo_of_me &= ~sec_of_me;
+      // phase B: ticket, then wait for the turn (bounded)
+      uint32_t ticket = 0;
+      if (lane == 0) ticket = atomicAdd(&p.gs->ticket, 1u);
+      ticket = __shfl_sync(0xFFFFFFFFu, ticket, 0);
+      unsigned long long turn = 0;
+      bool got = true;
+      if (lane == 0)
+        got = bounded_wait(
+            [&] {
+              turn = ld_acquire_gpu(&p.gs->turn);
+              return (uint32_t)turn == ticket;
+            },
+            &p.gs->error, ERR_WAIT_TURN, p.spin_log2);
+      got = __shfl_sync(0xFFFFFFFFu, got, 0);
+      if (!got) {
+        aborted_run = true;
+        break;
+      }
+      const uint32_t C = (uint32_t)(__shfl_sync(0xFFFFFFFFu, turn, 0) >> 32);
+      fence_acq_rel_gpu();
+
+      // phase C: validate against everything committed since the snapshot
+      if (ring && scanned_hi < C) {
+        ring_scan(p, sm, scanned_hi, C, snaps, ready);
+        scanned_hi = C;
+      }
+      for (uint32_t m = ready; m; m &= m - 1) {
+        const uint32_t w = __ffs(m) - 1;
+        const MailSlot<MAXR, MAXW>& ms = sm.mail[w];
+        const uint32_t s = __shfl_sync(0xFFFFFFFFu, sec_of_me, w);
+        const uint32_t snap = snaps[w];
+        bool bad = false, aged = false;
+        if ((s >> lane) & 1u) {
+          const uint32_t nrs = ms.n[lane] & 0xFFu;
+          if (!ring) {
+            uint32_t st[MAXR];
+#pragma unroll
+            for (int k = 0; k < MAXR; k++)
+              st[k] = k < (int)nrs ? ld_relaxed_gpu(&p.stamp[ms.rs[k][lane]]) : 0u;
+#pragma unroll
+            for (int k = 0; k < MAXR; k++) bad |= st[k] > snap;
+          } else if (p.validate == CSMV_VALIDATE_RING) {
+            aged = (uint64_t)snap + (p.ring_mask + 1) <= C || ((sm.recage[w] >> lane) & 1u);
+            bad = !aged && ((sm.conflict[w] >> lane) & 1u);
+          } else {  // plain per-lane scan of (snap, C]
+            aged = (uint64_t)snap + (p.ring_mask + 1) <= C;
+            for (uint32_t t = snap + 1; t <= C && !aged && !bad; t++) {
+              const uint4 r = p.ring[t & p.ring_mask];
+              if (r.x != t) {
+                aged = true;
+                break;
+              }
+              for (uint32_t k = 0; k < nrs; k++) {
+                const uint32_t x = ms.rs[k][lane];
+                bad |= (r.y > 0 && x == r.z) || (r.y > 1 && x == r.w);
+              }
+            }
+          }
+        }
+        const uint32_t f = __ballot_sync(0xFFFFFFFFu, bad || aged);
+        const uint32_t ag = __ballot_sync(0xFFFFFFFFu, aged);
+        stat_ra += __popc(ag);
+        stat_rw += __popc(f & ~ag);
+        if (lane == w) sec_of_me = s & ~f;
+      }
+
+      // phase D/E: consecutive timestamps in (warp, lane) order; stamps, records, log
+      uint32_t base = C;
+      for (uint32_t m = ready; m; m &= m - 1) {
+        const uint32_t w = __ffs(m) - 1;
+        MailSlot<MAXR, MAXW>& ms = sm.mail[w];
+        const uint32_t s = __shfl_sync(0xFFFFFFFFu, sec_of_me, w);
+        if ((s >> lane) & 1u) {
+          const uint32_t ts = base + 1 + __popc(s & lanemask_lt());
+          const uint32_t nws = ms.n[lane] >> 8;
+          WriteSet<MAXW> ws;
+          ws.n = nws;
+#pragma unroll
+          for (int k = 0; k < MAXW; k++) {
+            ws.addr[k] = ms.ws[k][lane];
+            ws.val[k] = ms.wv[k][lane];
+            if (k < (int)nws) st_relaxed_gpu(&p.stamp[ws.addr[k]], ts);
+          }
+          p.ring[ts & p.ring_mask] = make_uint4(ts, nws, ws.addr[0], ws.addr[MAXW - 1]);
+          if (p.log) p.log_txn[ts - 1 - p.log_base] = ms.txn[lane];
+          if (p.writeback == CSMV_WRITEBACK_SERVER) TXWriteBack<DEPTH>(ts, vs, ws);
+          ms.tsl[lane] = ts;
+        }
+        base += __popc(s);
+      }
+      const uint32_t ncommit = base - C;
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) {
+        if (p.writeback == CSMV_WRITEBACK_SERVER && ncommit) st_release_gpu(&p.gs->clock, base);
+        st_release_gpu(&p.gs->turn, ((unsigned long long)base << 32) | (ticket + 1u));
+      }
+      done_of_me |= sec_of_me;
+      // client write-back: the last client warp of the section publishes it on the clock
+      if (p.writeback == CSMV_WRITEBACK_CLIENT && ncommit) {
+        const uint32_t nw = __popc(__ballot_sync(0xFFFFFFFFu, lane < nc && sec_of_me != 0));
+        if (lane == 0) {
+          bid = sm.next_bid;
+          sm.next_bid = (bid + 1) % kBatchDescs;
+          sm.batch[bid].first_ts = C + 1;
+          sm.batch[bid].last_ts = base;
+          sm.batch[bid].remaining = nw;
+        }
+        bid = __shfl_sync(0xFFFFFFFFu, bid, 0);
+      }
+    }
+    if (aborted_run) break;
+
+    // ---- phase F: replies ----
+    __syncwarp();
+    if (lane < nc && ((ready >> lane) & 1u)) {
+      MailSlot<MAXR, MAXW>& ms = sm.mail[lane];
+      ms.ok = done_of_me;
+      ms.bid = bid;
+      st_release_cta(&ms.rep, seen);
+    }
+    if (lane == 0) {
+      stat_add(sm.stat, ST_ABORT_READ_WRITE, stat_rw);
+      stat_add(sm.stat, ST_ABORT_RECORD_AGE, stat_ra);
+      stat_add(sm.stat, ST_SECTIONS, 1);
+    }
+  }
+}
+
+template <int DEPTH, int MAXR, int MAXW>
+__global__ void __launch_bounds__(1024, 1) bank_kernel(BankParams p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  CtaShared<MAXR, MAXW>& sm = *reinterpret_cast<CtaShared<MAXR, MAXW>*>(smem_raw);
+  const uint32_t warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    sm.done_warps = 0;
+    sm.next_bid = 0;
+  }
+  for (uint32_t i = threadIdx.x; i < ST_COUNT; i += blockDim.x) sm.stat[i] = 0;
+  for (uint32_t i = threadIdx.x; i < p.nc; i += blockDim.x) {
+    sm.mail[i].req = 0;
+    sm.mail[i].rep = 0;
+  }
+  __syncthreads();
+  if (warp == 0)
+    server_warp<DEPTH, MAXR, MAXW>(p, sm);
+  else
+    client_warp<DEPTH, MAXR, MAXW>(p, sm, warp - 1);
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < ST_COUNT; i += blockDim.x)
+    if (sm.stat[i]) atomicAdd(&p.stats[i], sm.stat[i]);
+}
+
+}  // namespace csmv

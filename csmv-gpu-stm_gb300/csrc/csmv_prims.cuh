@@ -1,0 +1,113 @@
+// csmv_prims.cuh - memory-model primitives and bounded waits for the sm_103a commit path.
+//
+// The reference (sync_lib/common.h:12-173) wraps pre-Volta PTX (bfind, fns, popc, shfl.sync
+// with a full mask from divergent code, ld/st.global.cg). Here every cross-warp hand-off is an
+// explicit acquire/release pair at the narrowest scope that covers it (.cta for the
+// shared-memory mailbox, .gpu for the commit order and the clock), and every spin has an
+// iteration budget after which it records an error and returns instead of hanging the GPU.
+#pragma once
+#include <cstdint>
+
+namespace csmv {
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// ---- global (gpu scope) -------------------------------------------------------------------
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long ld_acquire_gpu(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu(uint32_t* p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_release_gpu(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_relaxed_gpu(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_gpu(uint32_t* p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_gpu(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_gpu(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+// two 8-byte version slots in one 16-byte access; each element is single-copy atomic
+__device__ __forceinline__ void ld_relaxed_gpu_v2(const unsigned long long* p,
+                                                  unsigned long long& a,
+                                                  unsigned long long& b) {
+  asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];"
+               : "=l"(a), "=l"(b)
+               : "l"(p)
+               : "memory");
+}
+__device__ __forceinline__ void fence_acq_rel_gpu() {
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+}
+
+// ---- shared (cta scope) -------------------------------------------------------------------
+__device__ __forceinline__ uint32_t ld_acquire_cta(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.cta.shared.u32 %0, [%1];"
+               : "=r"(v)
+               : "r"((uint32_t)__cvta_generic_to_shared(p))
+               : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_cta(uint32_t* p, uint32_t v) {
+  asm volatile("st.release.cta.shared.u32 [%0], %1;" ::"r"((uint32_t)__cvta_generic_to_shared(p)),
+               "r"(v)
+               : "memory");
+}
+
+// ---- device error word ----------------------------------------------------------------------
+enum : uint32_t {
+  ERR_NONE = 0,
+  ERR_WAIT_TURN = 1,     // commit-order turn never came
+  ERR_WAIT_CLOCK = 2,    // clock never reached the predecessor's timestamp
+  ERR_WAIT_REPLY = 3,    // a client warp's request got no reply
+  ERR_WAIT_REQUEST = 4,  // the server saw no progress from its clients
+  ERR_CAPACITY = 5,      // read/write set or batch capacity exceeded
+  ERR_DATA = 6           // malformed transaction (bad size / address)
+};
+
+__device__ __forceinline__ void raise_error(uint32_t* err, uint32_t code) {
+  atomicCAS(err, 0u, code);
+}
+
+// Bounded poll: returns true when pred() holds, false when the budget ran out or another warp
+// raised an error (which is then left in *err). Backs off with nanosleep.
+template <class Pred>
+__device__ __forceinline__ bool bounded_wait(Pred pred, uint32_t* err, uint32_t code,
+                                             uint32_t limit_log2) {
+  uint32_t ns = 32;
+  const uint64_t limit = 1ull << limit_log2;
+  for (uint64_t it = 0; it < limit; ++it) {
+    if (pred()) return true;
+    if ((it & 15u) == 15u && ld_relaxed_gpu(err) != 0) return false;
+    __nanosleep(ns);
+    if (ns < 1024) ns <<= 1;
+  }
+  raise_error(err, code);
+  return false;
+}
+
+}  // namespace csmv

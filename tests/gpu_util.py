@@ -1,0 +1,36 @@
+"""Shared helpers of the GPU tests: run a stream through the C ABI and check it with the oracle."""
+import numpy as np
+
+import csmv_gb300 as cg
+import oracle as orc
+
+
+def c1_workload(n_txn=8 * 128 * 256, seed=1, **kw):
+    """4096 accounts at 1000, 90% transfers of 1..10 between 2 distinct uniform accounts (skip
+    if insufficient), 10% read-only sums of 8 uniform accounts."""
+    d = dict(seed=seed, pr_read_pct=10, ro_reads=8, up_reads=2, kind=cg.KIND_TRANSFER, amt_lo=1,
+             amt_hi=10, dist=cg.DIST_UNIFORM)
+    d.update(kw)
+    n_acc = d.pop("n_accounts", 4096)
+    return cg.bank_workload(n_acc, n_txn, **d)
+
+
+def run_checked(w, *, init_value=1000, check=True, **cfg):
+    """Run workload w on a fresh bank; returns (stats, stream, bank outputs); asserts exactness."""
+    s = cg.generate(w)
+    cfg.setdefault("max_txn", w.n_txn)
+    depth = cfg.setdefault("version_depth", 4)
+    with cg.Bank(n_accounts=w.n_accounts, init_value=init_value, **cfg) as bank:
+        bank.load()
+        st = bank.run(s)
+        log_txn, outcome, result = bank.log(w.n_txn, st.final_ts)
+        slots = bank.versions()
+    assert st.error == 0
+    assert st.commits == w.n_txn, (st.commits, w.n_txn)
+    assert st.commits_update == st.final_ts
+    if check:
+        init = np.full(w.n_accounts, init_value, np.int32)
+        err = orc.check(s.op, s.off, s.addr, w.n_accounts, init, depth, st.final_ts, log_txn,
+                        outcome, result, slots)
+        assert err is None, err
+    return st, s, (log_txn, outcome, result, slots)

@@ -1,0 +1,84 @@
+"""CPU tests of the C-ABI boundary: the libraries load, export every declared symbol, validate
+their arguments, and report a missing GPU as a status (never a crash). No compute calls."""
+import ctypes as C
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+import csmv_gb300 as cg
+from csmv_gb300 import build as b
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared(header: Path) -> set[str]:
+    text = re.sub(r"/\*.*?\*/", "", header.read_text(), flags=re.S)
+    return set(re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(csmv_\w+)\s*\(", text, flags=re.M))
+
+
+def exported(lib: Path) -> set[str]:
+    out = subprocess.run(["nm", "-D", "--defined-only", str(lib)], capture_output=True, text=True,
+                         check=True).stdout
+    return {ln.split()[-1] for ln in out.splitlines() if ln.strip()}
+
+
+def test_every_declared_symbol_is_exported():
+    names = declared(ROOT / "include" / "csmv.h")
+    assert {"csmv_bank_create", "csmv_bank_run", "csmv_bank_read_log", "csmv_last_error"} <= names
+    missing = names - exported(b.LIB)
+    assert not missing, missing
+
+
+def test_library_loads_and_reports_version():
+    L = cg.lib()
+    assert L.csmv_abi_version() == 1
+    assert L.csmv_status_str(4) == b"bounded device wait timed out"
+
+
+def test_config_validation_is_a_status():
+    for bad in (dict(version_depth=3), dict(ring_size=100), dict(client_warps=0),
+                dict(client_warps=32), dict(batch=0, writeback=0), dict(max_txn=33),
+                dict(spin_limit_log2=2), dict(n_accounts=1), dict(batch=9)):
+        with pytest.raises(cg.CsmvError) as e:
+            cg.Bank(cg.bank_config(**bad))
+        assert e.value.status == 1, bad
+
+
+def test_workload_validation_is_a_status():
+    for bad in (dict(n_txn=33), dict(up_reads=1), dict(amt_lo=0), dict(amt_hi=5000),
+                dict(pr_read_pct=101), dict(kind=0), dict(dist=7)):
+        kw = dict(n_accounts=100, n_txn=64)
+        kw.update(bad)
+        with pytest.raises(cg.CsmvError) as e:
+            cg.generate(cg.bank_workload(**kw))
+        assert e.value.status == 1, bad
+
+
+def test_null_handles_are_rejected():
+    L = cg.lib()
+    assert L.csmv_bank_load(None, None) == 1
+    assert L.csmv_bank_run(None, None, None) == 1
+    assert L.csmv_bank_read_values(None, None) == 1
+    L.csmv_bank_destroy(None)
+
+
+@pytest.mark.skipif(cg.cuda_device_present(), reason="a GPU is present")
+def test_create_without_gpu_is_no_device():
+    with pytest.raises(cg.CsmvError) as e:
+        cg.Bank(n_accounts=64, max_txn=64)
+    assert e.value.status == 6
+
+
+def test_driver_keeps_reference_cli():
+    exe = b.BIN / "csmv_bank"
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0 and "argument order" in out.stdout and "8) verbose" in out.stdout
+
+
+def test_devtest_library_exports():
+    names = exported(b.DEVTEST_LIB)
+    assert {"csmv_devtest_read", "csmv_devtest_prevalidate", "csmv_devtest_writeback",
+            "csmv_devtest_bounded_wait"} <= names
+    C.CDLL(str(b.DEVTEST_LIB))

@@ -1,0 +1,164 @@
+"""GPU parity tests of the bank commit path, through the C ABI, against the CPU oracle.
+
+Exactness bar (integer path, bit-exact): every run's commit log replayed serially in commit-ts
+order reproduces the device's final version slots bit for bit, every read-only and no-write
+transaction saw the state at its snapshot, commit timestamps are unique and dense, the total
+balance is conserved. With one client warp the run is deterministic and must equal the oracle's
+model of the engine exactly (log, outcomes, versions, abort counts)."""
+import subprocess
+
+import numpy as np
+import pytest
+
+import csmv_gb300 as cg
+import oracle as orc
+from gpu_util import c1_workload, run_checked
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("prevalidate", [1, 0])
+@pytest.mark.parametrize("validate", [cg.VALIDATE_STAMP, cg.VALIDATE_RING, cg.VALIDATE_RING_LANE])
+def test_one_client_warp_equals_oracle_model(prevalidate, validate):
+    w = c1_workload(n_txn=32 * 96, n_accounts=40, pr_read_pct=20, up_reads=3, seed=11)
+    st, s, (log_txn, outcome, result, slots) = run_checked(
+        w, ctas=1, client_warps=1, prevalidate=prevalidate, validate=validate, batch=cg.BATCH_WARP,
+        init_value=100)
+    init = np.full(40, 100, np.int32)
+    mslots, mlog, mout, mres, ms = orc.sim_1warp(s.op, s.off, s.addr, 40, init, 4, bool(prevalidate))
+    np.testing.assert_array_equal(log_txn, mlog)
+    np.testing.assert_array_equal(outcome, mout)
+    np.testing.assert_array_equal(result, mres)
+    np.testing.assert_array_equal(slots, mslots)
+    assert (st.commits_update, st.commits_readonly, st.commits_nowrite) == (
+        ms.commits_update, ms.commits_readonly, ms.commits_nowrite)
+    assert (st.aborts_prevalid, st.aborts_read_write, st.rounds) == (
+        ms.aborts_prevalid, ms.aborts_read_write, ms.rounds)
+    assert st.aborts_data_age == 0 and st.aborts_record_age == 0
+
+
+VARIANTS = {
+    "stamp-cta-client": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CTA),
+    "stamp-warp-client": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_WARP),
+    "stamp-cta-server": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CTA, writeback=cg.WRITEBACK_SERVER),
+    "stamp-lane-server": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_LANE, writeback=cg.WRITEBACK_SERVER),
+    "ring-cta-client": dict(validate=cg.VALIDATE_RING, batch=cg.BATCH_CTA),
+    "ring-warp-server": dict(validate=cg.VALIDATE_RING, batch=cg.BATCH_WARP, writeback=cg.WRITEBACK_SERVER),
+    "ringlane-warp-client": dict(validate=cg.VALIDATE_RING_LANE, batch=cg.BATCH_WARP),
+    "stamp-cta-noprevalid": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CTA, prevalidate=0),
+}
+
+
+@pytest.mark.parametrize("variant", list(VARIANTS))
+def test_c1_plain_bank_exact(variant):
+    """4096 accounts, 8 blocks x 128 client threads, 256 transactions each, depth 4."""
+    st, _, _ = run_checked(c1_workload(), ctas=8, client_warps=4, **VARIANTS[variant])
+    assert st.commits_readonly > 0 and st.commits_update > 0
+
+
+@pytest.mark.parametrize("depth", [2, 4, 16])
+def test_high_contention_small_ring_exact(depth):
+    """16 accounts, 32 client warps: most attempts conflict; a 64-record ring forces RecordAge,
+    depth 2 forces DataAge on read-only scans."""
+    w = c1_workload(n_txn=32 * 600, n_accounts=16, pr_read_pct=30, ro_reads=8, up_reads=3, seed=3)
+    st, _, _ = run_checked(w, ctas=4, client_warps=8, version_depth=depth, ring_size=64,
+                           validate=cg.VALIDATE_RING)
+    assert st.aborts_read_write + st.aborts_prevalid > 0
+    if depth == 2:
+        assert st.aborts_data_age > 0
+
+
+def test_two_accounts_extreme():
+    w = c1_workload(n_txn=32 * 40, n_accounts=2, pr_read_pct=0, up_reads=2, seed=5)
+    run_checked(w, ctas=2, client_warps=2, init_value=50)
+
+
+def test_single_round():
+    run_checked(c1_workload(n_txn=32, n_accounts=100), ctas=1, client_warps=1)
+
+
+def test_zipf_contended_full_gpu_exact():
+    """1M accounts, Zipf 0.99, read 4 / write 2, 20% read-only scans of 32, persistent grid."""
+    w = cg.bank_workload(1 << 20, 1 << 18, seed=9, pr_read_pct=20, ro_reads=32, up_reads=4,
+                         kind=cg.KIND_TRANSFER, amt_lo=1, amt_hi=10, dist=cg.DIST_ZIPF,
+                         zipf_theta=0.99)
+    st, _, _ = run_checked(w, ctas=0, client_warps=15)
+    assert st.aborts > 0
+
+
+def test_hotspot_full_gpu_exact():
+    w = cg.bank_workload(1 << 20, 1 << 18, seed=4, pr_read_pct=10, ro_reads=8, up_reads=4,
+                         dist=cg.DIST_HOTSPOT, hot_frac=0.01, hot_prob=0.9, shift_every=1 << 16)
+    run_checked(w, ctas=0, client_warps=15)
+
+
+def test_runs_continue_the_commit_order():
+    w = c1_workload(n_txn=32 * 256)
+    s = cg.generate(w)
+    with cg.Bank(n_accounts=4096, max_txn=w.n_txn, ctas=8, client_warps=4) as bank:
+        bank.load()
+        st1 = bank.run(s)
+        v1 = bank.values()
+        st2 = bank.run(s)
+        log2, out2, res2 = bank.log(w.n_txn, st2.final_ts - st1.final_ts)
+        v2 = bank.values()
+    assert v1.sum() == v2.sum() == 4096 * 1000
+    assert st2.final_ts > st1.final_ts
+    # replay run 2 from the state after run 1, timestamps shifted to start at 1
+    f1 = np.uint32(st1.final_ts)
+    out = out2.copy()
+    snap = (out & np.uint32(cg.SNAP_FLAG)) != 0
+    out[~snap] -= f1
+    out[snap] = ((out[snap] & np.uint32(0x7FFFFFFF)) - f1) | np.uint32(cg.SNAP_FLAG)
+    err = orc.check(s.op, s.off, s.addr, 4096, v1, 4, st2.final_ts - st1.final_ts, log2, out, res2)
+    assert err is None, err
+    assert np.array_equal(v2, _replay_values(s, v1, log2))
+
+
+def _replay_values(s, init, log):
+    import ctypes as C
+
+    vals = init.copy()
+    L = orc.lib()
+    wa, wv, r = np.zeros(2, np.uint32), np.zeros(2, np.int32), C.c_int32()
+    for t in log:
+        nr = (int(s.op[t]) >> 2) & 63
+        a = s.addr[s.off[t]:s.off[t] + nr].copy()
+        v = vals[a].astype(np.int32)
+        nw = L.orc_bank_exec(C.c_uint32(int(s.op[t])), orc.p(a), orc.p(v), orc.p(wa), orc.p(wv), C.byref(r))
+        for k in range(nw):
+            vals[wa[k]] = wv[k]
+    return vals
+
+
+def test_run_device_matches_run():
+    torch = pytest.importorskip("torch")
+    w = c1_workload(n_txn=32 * 512)
+    s = cg.generate(w)
+    dop = torch.from_numpy(s.op.view(np.int32)).cuda()
+    doff = torch.from_numpy(s.off.view(np.int32)).cuda()
+    daddr = torch.from_numpy(s.addr.view(np.int32)).cuda()
+    ds = cg.BankStream(w.n_txn, dop.data_ptr(), doff.data_ptr(), daddr.data_ptr(), s.addr.shape[0])
+    with cg.Bank(n_accounts=4096, max_txn=w.n_txn, ctas=8, client_warps=4) as bank:
+        bank.load()
+        st = bank.run_device(ds)
+        torch.cuda.synchronize()
+        log_txn, outcome, result = bank.log(w.n_txn, st.final_ts)
+        slots = bank.versions()
+    assert st.commits == w.n_txn
+    err = orc.check(s.op, s.off, s.addr, 4096, np.full(4096, 1000, np.int32), 4, st.final_ts,
+                    log_txn, outcome, result, slots)
+    assert err is None, err
+
+
+def test_driver_reference_command_line():
+    from csmv_gb300 import build as b
+
+    out = subprocess.run([str(b.BIN / "csmv_bank"), "4096", "128", "8", "128", "10", "8", "1", "0"],
+                         capture_output=True, text=True, timeout=300,
+                         env={"CSMV_TX_PER_THREAD": "64", "PATH": "/usr/bin:/bin"})
+    assert out.returncode == 0, out.stderr
+    assert "Consistency fail" not in out.stdout
+    fields = out.stdout.strip().split("\t")
+    assert len(fields) == 6 + 17 + 4
+    assert float(fields[1]) > 0 and 0.0 <= float(fields[0]) < 100.0
