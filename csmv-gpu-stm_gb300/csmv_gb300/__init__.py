@@ -59,7 +59,8 @@ class BankConfig(C.Structure):
 class Stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "commits_update", "commits_readonly", "commits_nowrite", "aborts_data_age",
-        "aborts_record_age", "aborts_read_write", "aborts_prevalid", "sections", "rounds")] + [
+        "aborts_record_age", "aborts_read_write", "aborts_prevalid", "aborts_write_write",
+        "sections", "rounds")] + [
         ("final_ts", C.c_uint32), ("error", C.c_uint32), ("kernel_ms", C.c_double),
         ("total_ms", C.c_double)]
 
@@ -73,7 +74,7 @@ class Stats(C.Structure):
     @property
     def aborts(self) -> int:
         return (self.aborts_data_age + self.aborts_record_age + self.aborts_read_write +
-                self.aborts_prevalid)
+                self.aborts_prevalid + self.aborts_write_write)
 
     @property
     def abort_rate(self) -> float:

@@ -2,10 +2,12 @@
 //
 // Data layout in HBM (all item-major, allocated once per handle):
 //   slots  n_accounts * depth * 8 B   packed (ts << 32 | value) versions; depth 4 = one sector
-//   stamp  n_accounts * 4 B           commit timestamp of the latest committed writer
+//   cw     n_accounts * 8 B           commit word: stamp (ts of the last committed writer) and
+//                                      write-lock owner, one 8-byte word per account
 //   ring   ring_size * 16 B           commit records {ts, n_writes, w0, w1}
-//   logs   max_txn * 12 B             log_txn[ts-1], outcome[txn], result[txn]
-//   sync   5 x 128 B lines            turn / ticket / clock / round cursor / error word
+//   done   256 KB                     completion bitmap, one bit per commit timestamp
+//   logs   8*max_txn*4 + max_txn*8 B  log_txn[ts-1] (holes included), outcome[txn], result[txn]
+//   sync   6 x 128 B lines            turn / ticket / clock / ts cursor / round cursor / error
 #include <chrono>
 #include <cstring>
 #include <vector>
@@ -18,6 +20,7 @@ using namespace csmv;
 namespace {
 constexpr int kMaxR = 8;
 constexpr int kMaxW = 2;
+constexpr uint32_t kDoneWords = 1u << 16;  // 2^21 timestamps in flight at most
 using KernelFn = void (*)(BankParams);
 
 KernelFn pick_kernel(uint32_t depth) {
@@ -39,8 +42,10 @@ struct csmv_bank_t {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   unsigned long long* slots = nullptr;
-  uint32_t* stamp = nullptr;
+  unsigned long long* cw = nullptr;
   uint4* ring = nullptr;
+  uint32_t* done = nullptr;
+  uint32_t log_cap = 0;
   GlobalSync* gs = nullptr;
   uint32_t* log_txn = nullptr;
   uint32_t* outcome = nullptr;
@@ -87,7 +92,8 @@ static csmv_status validate_config(const csmv_bank_config* c) {
   if (c->validate > CSMV_VALIDATE_RING_LANE) return bad("validate");
   if (c->writeback > CSMV_WRITEBACK_SERVER) return bad("writeback");
   if (c->batch > CSMV_BATCH_CTA) return bad("batch (cluster batching is not built)");
-  if (c->batch == CSMV_BATCH_LANE && c->writeback != CSMV_WRITEBACK_SERVER)
+  if (c->validate != CSMV_VALIDATE_STAMP && c->batch == CSMV_BATCH_LANE &&
+      c->writeback != CSMV_WRITEBACK_SERVER)
     return bad("per-transaction sections need server write-back");
   if (c->max_txn == 0 || c->max_txn % 32) return bad("max_txn must be a positive multiple of 32");
   if (c->spin_limit_log2 < 10 || c->spin_limit_log2 > 30) return bad("spin_limit_log2");
@@ -96,8 +102,9 @@ static csmv_status validate_config(const csmv_bank_config* c) {
 
 static void free_all(csmv_bank_t* h) {
   cudaFree(h->slots);
-  cudaFree(h->stamp);
+  cudaFree(h->cw);
   cudaFree(h->ring);
+  cudaFree(h->done);
   cudaFree(h->gs);
   cudaFree(h->log_txn);
   cudaFree(h->outcome);
@@ -157,13 +164,15 @@ extern "C" csmv_status csmv_bank_create(const csmv_bank_config* cfg, csmv_bank_t
     return fail(CSMV_ERR_INVALID_ARG);
   }
   const size_t n = cfg->n_accounts, D = cfg->version_depth;
+  h->log_cap = cfg->log_commits ? (cfg->max_txn > 0x1FFFFFFFu ? 0xFFFFFFFFu : cfg->max_txn * 8u) : 1u;
   struct {
     void** p;
     size_t bytes;
   } allocs[] = {
-      {(void**)&h->slots, n * D * 8},       {(void**)&h->stamp, n * 4},
+      {(void**)&h->slots, n * D * 8},       {(void**)&h->cw, n * 8},
       {(void**)&h->ring, (size_t)cfg->ring_size * 16}, {(void**)&h->gs, sizeof(GlobalSync)},
-      {(void**)&h->log_txn, (size_t)cfg->max_txn * 4}, {(void**)&h->outcome, (size_t)cfg->max_txn * 4},
+      {(void**)&h->done, (size_t)kDoneWords * 4},
+      {(void**)&h->log_txn, (size_t)h->log_cap * 4}, {(void**)&h->outcome, (size_t)cfg->max_txn * 4},
       {(void**)&h->result, (size_t)cfg->max_txn * 4},  {(void**)&h->stats, ST_COUNT * 8},
       {(void**)&h->d_op, (size_t)cfg->max_txn * 4},    {(void**)&h->d_off, (size_t)cfg->max_txn * 4},
   };
@@ -187,8 +196,9 @@ extern "C" csmv_status csmv_bank_load(csmv_bank_t* h, const int32_t* host_values
   for (size_t i = 0; i < n; i++)
     slots[i * D] = (uint32_t)(host_values ? host_values[i] : h->cfg.init_value);  // ts 0
   CSMV_CUDA(cudaMemcpyAsync(h->slots, slots.data(), n * D * 8, cudaMemcpyHostToDevice, h->stream));
-  CSMV_CUDA(cudaMemsetAsync(h->stamp, 0, n * 4, h->stream));
+  CSMV_CUDA(cudaMemsetAsync(h->cw, 0, n * 8, h->stream));
   CSMV_CUDA(cudaMemsetAsync(h->ring, 0, (size_t)h->cfg.ring_size * 16, h->stream));
+  CSMV_CUDA(cudaMemsetAsync(h->done, 0, (size_t)kDoneWords * 4, h->stream));
   CSMV_CUDA(cudaMemsetAsync(h->gs, 0, sizeof(GlobalSync), h->stream));
   CSMV_CUDA(cudaStreamSynchronize(h->stream));
   h->loaded = true;
@@ -219,9 +229,11 @@ static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* of
   p.n_rounds = n_txn / 32;
   p.n_items = c.n_accounts;
   p.slots = h->slots;
-  p.stamp = h->stamp;
+  p.cw = h->cw;
   p.ring = h->ring;
   p.ring_mask = c.ring_size - 1;
+  p.done = h->done;
+  p.done_mask = kDoneWords - 1;
   p.gs = h->gs;
   p.log_txn = h->log_txn;
   p.outcome = h->outcome;
@@ -229,6 +241,7 @@ static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* of
   p.stats = h->stats;
   p.log = c.log_commits;
   p.log_base = h->last_final_ts;
+  p.log_cap = h->log_cap;
   p.nc = c.client_warps;
   p.validate = c.validate;
   p.writeback = c.writeback;
@@ -251,7 +264,7 @@ static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* of
   CSMV_CUDA(cudaStreamSynchronize(h->stream));
   float ms = 0;
   CSMV_CUDA(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
-  const uint32_t final_ts = (uint32_t)(gs.turn >> 32);
+  const uint32_t final_ts = c.validate == CSMV_VALIDATE_STAMP ? gs.ts_next : (uint32_t)(gs.turn >> 32);
   h->last_n_txn = n_txn;
   h->run_base_ts = h->last_final_ts;
   h->last_final_ts = final_ts;
@@ -263,6 +276,7 @@ static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* of
     out->aborts_record_age = st[ST_ABORT_RECORD_AGE];
     out->aborts_read_write = st[ST_ABORT_READ_WRITE];
     out->aborts_prevalid = st[ST_ABORT_PREVALID];
+    out->aborts_write_write = st[ST_ABORT_WRITE_WRITE];
     out->sections = st[ST_SECTIONS];
     out->rounds = st[ST_ROUNDS];
     out->final_ts = final_ts;
@@ -362,10 +376,10 @@ extern "C" csmv_status csmv_bank_read_log(csmv_bank_t* h, uint32_t* host_log_txn
     return CSMV_ERR_STATE;
   }
   CSMV_CUDA(cudaSetDevice(h->cfg.device));
-  const uint32_t commits = h->last_final_ts - h->run_base_ts;
+  const uint32_t commits = h->last_final_ts - h->run_base_ts;  // timestamps, holes included
   if (host_log_txn) {
     if (n_log < commits) {
-      set_error("log buffer holds %u entries, run committed %u", n_log, commits);
+      set_error("log buffer holds %u entries, run used %u timestamps", n_log, commits);
       return CSMV_ERR_CAPACITY;
     }
     // entry k holds the transaction that committed with ts = run_base_ts + k + 1

@@ -7,19 +7,25 @@
 // and client warps write back and advance a global clock one warp at a time.
 //
 // GB300 structure (one kernel, every CTA alike, all CTAs co-resident via cooperative launch):
-//  * warps 1..nc of a CTA are client warps; warp 0 is that CTA's commit server;
-//  * a client warp posts its candidates' read/write sets straight into a shared-memory mailbox
-//    slot (the csmv_sh form: no global message ring, no leader dispatch) and waits on a
-//    shared-memory reply word;
-//  * the server drains every ready mailbox into one batch, removes intra-batch conflicts with a
-//    shared-memory hash of the batch's writes, takes a ticket on the global commit order and,
-//    when its turn comes, validates the survivors against everything committed meanwhile
-//    (per-item commit stamps, or the commit-record ring), gives them consecutive timestamps,
-//    publishes stamps/records/log and passes the turn on with a single release store that also
-//    carries the next free timestamp;
-//  * client warps write back, and the last warp of a batch advances the global clock once for the
-//    whole batch (the reference advances it once per warp).
+//  * warps 1..nc of a CTA are client warps, warp 0 is that CTA's commit server; client and server
+//    talk through shared-memory mailboxes (the csmv_sh form: no global message ring, no leader);
+//  * two commit protocols share the kernel:
+//    - stamp (CSMV_VALIDATE_STAMP, the default): every item carries a 64-bit commit word
+//      {stamp = ts of its last committed writer, owner = warp holding its write lock}. A client
+//      warp locks its candidates' write items (one CAS each), posts the count to its server, which
+//      draws consecutive commit timestamps for every ready warp of the CTA with ONE atomicAdd and
+//      replies; the client then validates its reads against the commit words (stamp <= snapshot,
+//      no foreign lock), writes back, and releases each lock by publishing the new stamp. Lock ->
+//      timestamp -> validate is the order that makes this serialisable (the TL2 argument); no
+//      warp waits for any other CTA, so there is no global serial section;
+//    - ring (CSMV_VALIDATE_RING / RING_LANE, the reference algorithm): the server takes a ticket
+//      on a global commit order, and when its turn comes validates its batch against the
+//      commit-record ring (snapshot, frontier], gives survivors consecutive timestamps, appends
+//      their records and passes the turn on with one release store;
+//  * the clock (snapshot source) covers every timestamp whose write-back is complete: a
+//    completion bitmap indexed by timestamp, advanced by whichever warp completes the prefix.
 #pragma once
+#include <cstddef>
 #include <cstdint>
 
 #include "../../include/csmv.h"
@@ -29,6 +35,7 @@
 namespace csmv {
 
 constexpr uint32_t kSnapFlag = 0x80000000u;
+constexpr uint32_t kHole = 0xFFFFFFFFu;  // log entry of a timestamp whose transaction aborted
 constexpr int kMaxClientWarps = 31;
 constexpr int kHashSize = 4096;  // shared-memory hash entries (power of two)
 constexpr int kBatchDescs = 32;
@@ -41,17 +48,18 @@ enum StatIdx {
   ST_ABORT_RECORD_AGE,
   ST_ABORT_READ_WRITE,
   ST_ABORT_PREVALID,
+  ST_ABORT_WRITE_WRITE,
   ST_SECTIONS,
   ST_ROUNDS,
   ST_COUNT
 };
 
-// Global words of the commit order. Each hot word sits on its own 128-byte line so pollers of
-// one do not contend with writers of another.
+// Global words of the commit order, each on its own 128-byte line.
 struct alignas(128) GlobalSync {
-  alignas(128) unsigned long long turn;  // low 32: ticket now served, high 32: last commit ts
-  alignas(128) uint32_t ticket;          // next ticket
+  alignas(128) unsigned long long turn;  // ring protocol: low 32 ticket served, high 32 last ts
+  alignas(128) uint32_t ticket;          // ring protocol: next ticket
   alignas(128) uint32_t clock;           // every commit with ts <= clock is written back
+  alignas(128) uint32_t ts_next;         // stamp protocol: last timestamp handed out
   alignas(128) uint32_t round_next;      // next unclaimed round of the stream
   alignas(128) uint32_t error;           // first device error (ERR_*)
 };
@@ -63,9 +71,11 @@ struct BankParams {
   uint32_t n_rounds;
   uint32_t n_items;
   unsigned long long* slots;
-  uint32_t* stamp;
-  uint4* ring;  // {ts, n_writes, w0, w1}
+  unsigned long long* cw;  // per item: stamp | owner << 32
+  uint4* ring;             // {ts, n_writes, w0, w1}
   uint32_t ring_mask;
+  uint32_t* done;          // completion bitmap, one bit per timestamp (ring of done_mask+1 words)
+  uint32_t done_mask;
   GlobalSync* gs;
   uint32_t* log_txn;
   uint32_t* outcome;
@@ -73,21 +83,23 @@ struct BankParams {
   unsigned long long* stats;  // [ST_COUNT]
   uint32_t log;
   uint32_t log_base;  // last commit ts before this run: log_txn is indexed by ts-1-log_base
-  uint32_t nc;  // client warps per CTA
+  uint32_t log_cap;   // entries of log_txn (aborted stamp-protocol commits leave holes)
+  uint32_t nc;        // client warps per CTA
   uint32_t validate, writeback, batch, prevalidate;
   uint32_t spin_log2;
 };
 
 template <int MAXR, int MAXW>
 struct MailSlot {
-  uint32_t req, rep;       // request / reply sequence numbers
-  uint32_t snap, cand;     // request: snapshot, candidate lanes
-  uint32_t ok, bid;        // reply: committed lanes, batch descriptor of the clock advance
-  uint32_t tsl[32];        // reply: commit timestamp of each committed lane
-  uint32_t rs[MAXR][32];   // read sets, transposed (lane-contiguous: no bank conflicts)
+  uint32_t req, rep;      // request / reply sequence numbers
+  uint32_t snap, cand;    // request: snapshot, candidate lanes (stamp: locked lanes)
+  uint32_t ok, bid;       // reply: committed lanes (ring), batch descriptor of the clock advance
+  uint32_t base, pad;     // reply (stamp): last timestamp before this warp's range
+  uint32_t tsl[32];       // reply (ring): commit timestamp of each committed lane
+  uint32_t rs[MAXR][32];  // read sets, transposed (lane-contiguous: no bank conflicts)
   uint32_t ws[MAXW][32];
   int32_t wv[MAXW][32];
-  uint32_t n[32];          // nreads | nwrites << 8
+  uint32_t n[32];         // nreads | nwrites << 8
   uint32_t txn[32];
 };
 
@@ -102,13 +114,16 @@ struct CtaShared {
   uint32_t pad[2];
   unsigned long long stat[ST_COUNT];
   BatchDesc batch[kBatchDescs];
-  uint32_t hkey[kHashSize];
-  uint32_t hval[kHashSize];
-  uint32_t conflict[32];  // ring mode: per-warp conflict lanes
-  uint32_t recage[32];    // ring mode: per-warp record-age lanes
-  uint32_t snaps[32];     // snapshot of each batch warp
-  MailSlot<MAXR, MAXW> mail[1];        // nc slots (dynamic shared memory)
+  alignas(16) uint32_t hkey[kHashSize];  // cleared with 16-byte stores
+  alignas(16) uint32_t hval[kHashSize];
+  uint32_t conflict[32];  // ring: per-warp conflict lanes
+  uint32_t recage[32];    // ring: per-warp record-age lanes
+  uint32_t snaps[32];     // ring: snapshot of each batch warp
+  MailSlot<MAXR, MAXW> mail[1];  // nc slots (dynamic shared memory)
 };
+
+using CtaShared8x2 = CtaShared<8, 2>;
+static_assert(offsetof(CtaShared8x2, hkey) % 16 == 0, "hash table must be 16-byte aligned");
 
 template <int MAXR, int MAXW>
 __host__ __device__ constexpr size_t cta_shared_bytes(uint32_t nc) {
@@ -124,13 +139,51 @@ __device__ __forceinline__ void stat_add(unsigned long long* s, int idx, uint32_
   if (v) atomicAdd(&s[idx], (unsigned long long)v);
 }
 
+__device__ __forceinline__ uint32_t* owner_word(unsigned long long* cw, uint32_t x) {
+  return reinterpret_cast<uint32_t*>(cw + x) + 1;  // high half of the little-endian word
+}
+
 // ---------------------------------------------------------------------------------------------
-// client side
+// clock: completion bitmap
 // ---------------------------------------------------------------------------------------------
 
-// Last client warp of a batch publishes the batch on the clock, after every earlier batch.
-// (The reference: each warp leader spins until globalClock == ts-1, then adds its commits,
-// batchedAtrInsert/csmv_sh/API.cu:257-261.)
+// Mark timestamps [lo, hi] complete (their write-back is visible), then move the clock over the
+// longest complete prefix. Any warp may advance: a CAS keeps the clock monotonic, and the warp
+// that passes the end of a bitmap word clears it for the next lap. Called by one lane.
+__device__ void complete_range(const BankParams& p, uint32_t lo, uint32_t hi) {
+  __threadfence();
+  for (uint32_t t = lo; t <= hi;) {
+    const uint32_t bit = t & 31u, span = min(32u - bit, hi - t + 1);
+    const uint32_t m = (span == 32u ? 0xFFFFFFFFu : ((1u << span) - 1u)) << bit;
+    atomicOr(&p.done[(t >> 5) & p.done_mask], m);
+    t += span;
+  }
+  __threadfence();
+  for (uint32_t attempt = 0; attempt < 4096; attempt++) {
+    const uint32_t c = ld_acquire_gpu(&p.gs->clock);
+    uint32_t n = c;
+    for (uint32_t words = 0; words < 64; words++) {  // bounded scan per attempt
+      const uint32_t t = n + 1, bit = t & 31u;
+      const uint32_t w = ld_relaxed_gpu(&p.done[(t >> 5) & p.done_mask]) >> bit;
+      const uint32_t ones = (w == 0xFFFFFFFFu) ? 32u : (uint32_t)(__ffs(~w) - 1);
+      const uint32_t run = min(ones, 32u - bit);
+      n += run;
+      if (run < 32u - bit) break;
+    }
+    if (n == c) return;  // c+1 not complete yet: its owner will advance past us
+    __threadfence();
+    if (atomicCAS(&p.gs->clock, c, n) == c) {
+      // clear every word whose last timestamp this advance passed
+      for (uint32_t wd = (c + 1) >> 5; wd <= (n >> 5); wd++)
+        if (wd * 32u + 31u <= n) st_relaxed_gpu(&p.done[wd & p.done_mask], 0u);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// ring protocol: per-batch clock advance in timestamp order (the reference's leader spin,
+// batchedAtrInsert/csmv_sh/API.cu:257-261, once per batch instead of once per warp)
+// ---------------------------------------------------------------------------------------------
 template <int MAXR, int MAXW>
 __device__ __forceinline__ void batch_done(const BankParams& p, CtaShared<MAXR, MAXW>& sm,
                                            uint32_t bid) {
@@ -145,11 +198,16 @@ __device__ __forceinline__ void batch_done(const BankParams& p, CtaShared<MAXR, 
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// client side
+// ---------------------------------------------------------------------------------------------
 template <int DEPTH, int MAXR, int MAXW>
 __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint32_t w) {
   MailSlot<MAXR, MAXW>& ms = sm.mail[w];
   const uint32_t lane = lane_id();
   const VersionStore vs{p.slots, p.n_items};
+  const bool stamp = p.validate == CSMV_VALIDATE_STAMP;
+  const uint32_t me = blockIdx.x * p.nc + w + 1;  // lock owner id of this warp
   uint32_t seq = 0;
   bool failed = false;
   for (;;) {
@@ -162,22 +220,17 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
     const uint32_t kind = CSMV_OP_KIND(op), nr = CSMV_OP_NREADS(op);
     const uint32_t off = p.off[t];
     const bool ro = (kind == CSMV_KIND_READONLY);
-    if (!ro && (nr < 2 || nr > (uint32_t)MAXR)) {
-      raise_error(&p.gs->error, ERR_DATA);
-      failed = true;
-    }
-    if (__any_sync(0xFFFFFFFFu, failed)) break;
+    bool bad = !ro && (nr < 2 || nr > (uint32_t)MAXR);
     uint32_t a[MAXR];
-    bool bad_addr = false;
 #pragma unroll
     for (int k = 0; k < MAXR; k++) {
-      a[k] = (!ro && k < (int)nr) ? p.addr[off + k] : 0u;
-      bad_addr |= a[k] >= p.n_items;
+      a[k] = (!ro && !bad && k < (int)nr) ? p.addr[off + k] : 0u;
+      bad |= a[k] >= p.n_items;
     }
     if (ro)
-      for (uint32_t k = 0; k < nr; k++) bad_addr |= p.addr[off + k] >= p.n_items;
-    if (bad_addr) raise_error(&p.gs->error, ERR_DATA);  // no access outside the accounts
-    if (__any_sync(0xFFFFFFFFu, bad_addr)) {
+      for (uint32_t k = 0; k < nr; k++) bad |= p.addr[off + k] >= p.n_items;
+    if (bad) raise_error(&p.gs->error, ERR_DATA);  // no access outside the accounts
+    if (__any_sync(0xFFFFFFFFu, bad)) {
       failed = true;
       break;
     }
@@ -221,15 +274,26 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
         continue;
       }
 
-      // transfer: read everything at the snapshot, then compute the writes
+      // transfer: read everything at the snapshot; in the stamp protocol each item's commit
+      // word is loaded alongside its versions, so a read already overwritten by a later commit
+      // aborts here instead of reaching the commit step
       int32_t v[MAXR];
+      uint32_t stv[MAXR];
 #pragma unroll
       for (int k = 0; k < MAXR; k++) {
         v[k] = 0;
-        if (mine && k < (int)nr) v[k] = TXRead<DEPTH>(vs, a[k], snap, rs, ws, &aborted);
+        stv[k] = 0;
+        if (mine && k < (int)nr) {
+          v[k] = TXRead<DEPTH>(vs, a[k], snap, rs, ws, &aborted);
+          if (stamp) stv[k] = (uint32_t)ld_relaxed_gpu(&p.cw[a[k]]);
+        }
       }
+      bool stale = false;
+#pragma unroll
+      for (int k = 0; k < MAXR; k++) stale |= stv[k] > snap;
+      stale = stale && !aborted;
       bool has_w = false;
-      if (mine && !aborted) {
+      if (mine && !aborted && !stale) {
         uint32_t acc = CSMV_OP_AMT0(op) - 1u;
 #pragma unroll
         for (int k = 2; k < MAXR; k++)
@@ -241,28 +305,56 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
           has_w = true;
         }
       }
-      const bool nowrite = mine && !aborted && !has_w;
+      const bool nowrite = mine && !aborted && !stale && !has_w;
       if (nowrite && p.log) {
         p.outcome[t] = snap | kSnapFlag;
         p.result[t] = 0;
       }
       const uint32_t nwm = __ballot_sync(0xFFFFFFFFu, nowrite);
-      const uint32_t am = __ballot_sync(0xFFFFFFFFu, mine && aborted);
-      uint32_t cand = __ballot_sync(0xFFFFFFFFu, mine && !aborted && has_w);
+      const uint32_t agm = __ballot_sync(0xFFFFFFFFu, mine && aborted);
+      const uint32_t stm = __ballot_sync(0xFFFFFFFFu, mine && stale);
+      uint32_t cand = __ballot_sync(0xFFFFFFFFu, has_w);
       if (lane == 0) {
         stat_add(sm.stat, ST_COMMIT_NOWRITE, __popc(nwm));
-        stat_add(sm.stat, ST_ABORT_DATA_AGE, __popc(am));
+        stat_add(sm.stat, ST_ABORT_DATA_AGE, __popc(agm));
+        stat_add(sm.stat, ST_ABORT_READ_WRITE, __popc(stm));
       }
       pending &= ~nwm;
       if (cand == 0) continue;
-      if (p.prevalidate) {
+      // intra-warp resolution; the stamp protocol always needs it (a lane must not commit after
+      // a lower lane of its own warp wrote what it read: both hold locks of the same owner)
+      if (p.prevalidate || stamp) {
         const uint32_t pass = TXPreValidation(rs, ws, (cand >> lane) & 1u);
-        if (lane == 0) stat_add(sm.stat, ST_ABORT_PREVALID, __popc(cand & ~pass));
+        if (lane == 0)
+          stat_add(sm.stat, p.prevalidate ? ST_ABORT_PREVALID : ST_ABORT_READ_WRITE,
+                   __popc(cand & ~pass));
         cand = pass;
         if (cand == 0) continue;
       }
-      // post the request into the shared-memory mailbox
-      if ((cand >> lane) & 1u) {
+      bool cand_me = (cand >> lane) & 1u;
+
+      if (stamp) {  // lock the write items before asking for timestamps
+        bool got[MAXW];
+        bool all = true;
+#pragma unroll
+        for (int k = 0; k < MAXW; k++) {
+          got[k] = false;
+          if (cand_me && k < (int)ws.n) {
+            got[k] = atomicCAS(owner_word(p.cw, ws.addr[k]), 0u, me) == 0u;
+            all &= got[k];
+          }
+        }
+        if (cand_me && !all) {
+#pragma unroll
+          for (int k = 0; k < MAXW; k++)
+            if (got[k]) st_relaxed_gpu(owner_word(p.cw, ws.addr[k]), 0u);
+        }
+        const uint32_t locked = __ballot_sync(0xFFFFFFFFu, cand_me && all);
+        if (lane == 0) stat_add(sm.stat, ST_ABORT_WRITE_WRITE, __popc(cand & ~locked));
+        cand = locked;
+        cand_me = (cand >> lane) & 1u;
+        if (cand == 0) continue;
+      } else if (cand_me) {  // ring protocol: the server validates from the mailbox
 #pragma unroll
         for (int k = 0; k < MAXR; k++) ms.rs[k][lane] = rs.addr[k];
 #pragma unroll
@@ -273,6 +365,7 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
         ms.n[lane] = rs.n | (ws.n << 8);
         ms.txn[lane] = t;
       }
+      // post the request into the shared-memory mailbox, wait for the reply
       seq++;
       __syncwarp();
       if (lane == 0) {
@@ -290,17 +383,67 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
         break;
       }
       (void)ld_acquire_cta(&ms.rep);
-      const uint32_t okm = ms.ok, bid = ms.bid;
-      const bool committed = (okm >> lane) & 1u;
-      const uint32_t my_ts = committed ? ms.tsl[lane] : 0u;
-      if (committed && p.log) {
-        p.outcome[t] = my_ts;
-        p.result[t] = 0;
-      }
-      if (p.writeback == CSMV_WRITEBACK_CLIENT && okm) {
-        if (committed) TXWriteBack<DEPTH>(my_ts, vs, ws);
+
+      uint32_t okm = 0, my_ts = 0;
+      if (stamp) {
+        // timestamps base+1.. in lane order over the locked lanes; validate the reads now
+        const uint32_t base = ms.base;
+        my_ts = base + 1 + __popc(cand & lanemask_lt());
+        fence_acq_rel_gpu();
+        bool valid = cand_me;
+        if (cand_me) {
+          unsigned long long word[MAXR];
+#pragma unroll
+          for (int k = 0; k < MAXR; k++)
+            word[k] = k < (int)rs.n ? ld_relaxed_gpu(&p.cw[rs.addr[k]]) : 0ull;
+#pragma unroll
+          for (int k = 0; k < MAXR; k++) {
+            const uint32_t own = (uint32_t)(word[k] >> 32), st = (uint32_t)word[k];
+            if (k < (int)rs.n) valid &= (own == 0u || own == me) && st <= snap;
+          }
+        }
+        okm = __ballot_sync(0xFFFFFFFFu, valid);
+        if (lane == 0) stat_add(sm.stat, ST_ABORT_READ_WRITE, __popc(cand & ~okm));
+        if (p.log && cand_me) {
+          const uint32_t li = my_ts - 1 - p.log_base;
+          if (li < p.log_cap)
+            p.log_txn[li] = valid ? t : kHole;
+          else
+            raise_error(&p.gs->error, ERR_CAPACITY);
+        }
+        if (valid) {
+          TXWriteBack<DEPTH>(my_ts, vs, ws);
+          if (p.log) {
+            p.outcome[t] = my_ts;
+            p.result[t] = 0;
+          }
+        }
+        __threadfence();  // write-back visible before the stamps and the completion bits
+#pragma unroll
+        for (int k = 0; k < MAXW; k++) {
+          if (cand_me && k < (int)ws.n) {
+            if (valid)
+              st_release_gpu(&p.cw[ws.addr[k]], (unsigned long long)my_ts);  // stamp, unlock
+            else
+              st_relaxed_gpu(owner_word(p.cw, ws.addr[k]), 0u);
+          }
+        }
         __syncwarp();
-        if (lane == 0) batch_done(p, sm, bid);
+        if (lane == 0) complete_range(p, base + 1, base + __popc(cand));
+      } else {
+        okm = ms.ok;
+        const uint32_t bid = ms.bid;
+        const bool committed = (okm >> lane) & 1u;
+        my_ts = committed ? ms.tsl[lane] : 0u;
+        if (committed && p.log) {
+          p.outcome[t] = my_ts;
+          p.result[t] = 0;
+        }
+        if (p.writeback == CSMV_WRITEBACK_CLIENT && okm) {
+          if (committed) TXWriteBack<DEPTH>(my_ts, vs, ws);
+          __syncwarp();
+          if (lane == 0) batch_done(p, sm, bid);
+        }
       }
       __syncwarp();
       if (lane == 0) stat_add(sm.stat, ST_COMMIT_UPDATE, __popc(okm));
@@ -317,11 +460,83 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
 }
 
 // ---------------------------------------------------------------------------------------------
-// server side (TXAddToRecord)
+// server side
 // ---------------------------------------------------------------------------------------------
 
-// Intra-warp resolution on the server when clients skip pre-validation: the same lane-order rule
-// as TXPreValidation, over the sets in the mailbox.
+// Polls the mailboxes of the CTA's client warps; returns the ready mask (0 = none), sets
+// *stop when every client finished or an error was raised.
+template <int MAXR, int MAXW>
+__device__ __forceinline__ uint32_t poll_mailboxes(const BankParams& p, CtaShared<MAXR, MAXW>& sm,
+                                                   uint32_t seen, uint32_t* req, bool* stop) {
+  const uint32_t lane = lane_id();
+  *req = 0;
+  if (lane < p.nc) *req = ld_acquire_cta(&sm.mail[lane].req);
+  const uint32_t ready = __ballot_sync(0xFFFFFFFFu, lane < p.nc && *req != seen);
+  *stop = false;
+  if (ready == 0) {
+    uint32_t done = 0, err = 0;
+    if (lane == 0) {
+      done = *(volatile uint32_t*)&sm.done_warps;
+      err = ld_relaxed_gpu(&p.gs->error);
+    }
+    done = __shfl_sync(0xFFFFFFFFu, done, 0);
+    err = __shfl_sync(0xFFFFFFFFu, err, 0);
+    *stop = (done == p.nc) || err;
+  }
+  return ready;
+}
+
+// Stamp protocol server: one atomicAdd draws consecutive timestamps for every ready warp
+// (batched commit-timestamp assignment, batchedAtrInsert/csmv_sh/API.cu:331-361, here per CTA
+// batch instead of per warp); warp w gets (base_w, base_w + count_w].
+template <int MAXR, int MAXW>
+__device__ void server_warp_stamp(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
+  const uint32_t lane = lane_id();
+  uint32_t seen = 0;
+  uint64_t idle = 0;
+  const uint64_t idle_limit = 1ull << (p.spin_log2 + 2);
+  for (;;) {
+    uint32_t req;
+    bool stop;
+    uint32_t ready = poll_mailboxes(p, sm, seen, &req, &stop);
+    if (ready == 0) {
+      if (stop) break;
+      if (++idle > idle_limit) {
+        if (lane == 0) raise_error(&p.gs->error, ERR_WAIT_REQUEST);
+        break;
+      }
+      __nanosleep(32);
+      continue;
+    }
+    idle = 0;
+    if (p.batch != CSMV_BATCH_CTA) ready &= (0u - ready);  // one warp per assignment
+    const bool mine = lane < p.nc && ((ready >> lane) & 1u);
+    uint32_t cnt = 0;
+    if (mine) {
+      seen = req;
+      cnt = __popc(sm.mail[lane].cand);
+    }
+    // inclusive prefix over the ready warps in warp order
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+      if (lane >= (uint32_t)d) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    uint32_t t0 = 0;
+    if (lane == 0) t0 = atomicAdd(&p.gs->ts_next, total);
+    t0 = __shfl_sync(0xFFFFFFFFu, t0, 0);
+    if (mine) {
+      sm.mail[lane].base = t0 + incl - cnt;
+      st_release_cta(&sm.mail[lane].rep, seen);
+    }
+    if (lane == 0) stat_add(sm.stat, ST_SECTIONS, 1);
+  }
+}
+
+// Intra-warp resolution on the server when clients skip pre-validation (ring protocol): the
+// same lane-order rule as TXPreValidation, over the sets in the mailbox.
 template <int MAXR, int MAXW>
 __device__ __forceinline__ uint32_t server_lane_order(const MailSlot<MAXR, MAXW>& ms,
                                                       uint32_t cand) {
@@ -399,11 +614,10 @@ __device__ __forceinline__ bool hash_insert_multi(CtaShared<MAXR, MAXW>& sm, uin
 // for every candidate older than it.
 template <int MAXR, int MAXW>
 __device__ void ring_scan(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint32_t lo,
-                          uint32_t hi, const uint32_t* snaps /* per batch warp, smem */,
-                          uint32_t bwarps) {
+                          uint32_t hi, const uint32_t* snaps, uint32_t bwarps) {
   for (uint32_t t = lo + 1 + lane_id(); t <= hi; t += 32) {
     const uint4 r = p.ring[t & p.ring_mask];
-    if (r.x != t) {  // overwritten: every candidate older than t loses its proof
+    if (r.x != t) {
       for (uint32_t m = bwarps; m; m &= m - 1) {
         const uint32_t w = __ffs(m) - 1;
         if (snaps[w] < t) atomicOr(&sm.recage[w], 0xFFFFFFFFu);
@@ -427,29 +641,24 @@ __device__ void ring_scan(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint32
   __syncwarp();
 }
 
+// Ring protocol server (TXAddToRecord of the reference): batch, intra-batch conflicts, then one
+// commit section per batch (per transaction for CSMV_BATCH_LANE) in ticket order.
 template <int DEPTH, int MAXR, int MAXW>
-__device__ void server_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
+__device__ void server_warp_ring(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
   const uint32_t lane = lane_id();
   const uint32_t nc = p.nc;
-  uint32_t seen = 0;  // lane w < nc: last request seq handled for client warp w
+  uint32_t seen = 0;
   uint32_t* snaps = sm.snaps;
   uint64_t idle = 0;
   const uint64_t idle_limit = 1ull << (p.spin_log2 + 2);
   const VersionStore vs{p.slots, p.n_items};
 
   for (;;) {
-    uint32_t req = 0;
-    if (lane < nc) req = ld_acquire_cta(&sm.mail[lane].req);
-    uint32_t ready = __ballot_sync(0xFFFFFFFFu, lane < nc && req != seen);
+    uint32_t req;
+    bool stop;
+    uint32_t ready = poll_mailboxes(p, sm, seen, &req, &stop);
     if (ready == 0) {
-      uint32_t done = 0, err = 0;
-      if (lane == 0) {
-        done = *(volatile uint32_t*)&sm.done_warps;
-        err = ld_relaxed_gpu(&p.gs->error);
-      }
-      done = __shfl_sync(0xFFFFFFFFu, done, 0);
-      err = __shfl_sync(0xFFFFFFFFu, err, 0);
-      if (done == nc || err) break;
+      if (stop) break;
       if (++idle > idle_limit) {
         if (lane == 0) raise_error(&p.gs->error, ERR_WAIT_REQUEST);
         break;
@@ -459,7 +668,7 @@ __device__ void server_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
     }
     idle = 0;
     if (p.batch != CSMV_BATCH_CTA) ready &= (0u - ready);  // lowest ready warp only
-    if (p.validate != CSMV_VALIDATE_STAMP) {                // read hash must fit: cap the batch
+    {  // the batch read hash must fit: cap the batch
       uint32_t capped = 0, entries = 0;
       for (uint32_t m = ready; m; m &= m - 1) {
         const uint32_t w = __ffs(m) - 1;
@@ -507,38 +716,33 @@ __device__ void server_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
       if (lane == w) surv_of_me = s;
     }
 
-    // ring modes: build the batch read hash and pre-scan up to the current frontier
-    uint32_t pre_hi = 0;
-    const bool ring = p.validate != CSMV_VALIDATE_STAMP;
-    if (ring) {
-      hash_clear(sm);
-      if (lane < nc) {
-        sm.conflict[lane] = 0;
-        sm.recage[lane] = 0;
-      }
-      __syncwarp();
-      for (uint32_t m = ready; m; m &= m - 1) {
-        const uint32_t w = __ffs(m) - 1;
-        const uint32_t s = __shfl_sync(0xFFFFFFFFu, surv_of_me, w);
-        const MailSlot<MAXR, MAXW>& ms = sm.mail[w];
-        if ((s >> lane) & 1u) {
-          const uint32_t nrs = ms.n[lane] & 0xFFu;
-          for (uint32_t k = 0; k < nrs; k++) hash_insert_multi(sm, ms.rs[k][lane], w * 32 + lane);
-        }
-      }
-      __syncwarp();
-      uint32_t lo = 0xFFFFFFFFu;
-      for (uint32_t m = ready; m; m &= m - 1) lo = min(lo, snaps[__ffs(m) - 1]);
-      if (lane == 0) pre_hi = (uint32_t)(ld_acquire_gpu(&p.gs->turn) >> 32);
-      pre_hi = __shfl_sync(0xFFFFFFFFu, pre_hi, 0);
-      const uint32_t floor_ts = pre_hi > p.ring_mask ? pre_hi - p.ring_mask : 0u;
-      if (lo < floor_ts) lo = floor_ts;  // older snapshots fail the RecordAge rule anyway
-      if (lo < pre_hi) ring_scan(p, sm, lo, pre_hi, snaps, ready);
+    // the batch read hash and a pre-scan up to the current frontier
+    hash_clear(sm);
+    if (lane < nc) {
+      sm.conflict[lane] = 0;
+      sm.recage[lane] = 0;
     }
+    __syncwarp();
+    for (uint32_t m = ready; m; m &= m - 1) {
+      const uint32_t w = __ffs(m) - 1;
+      const uint32_t s = __shfl_sync(0xFFFFFFFFu, surv_of_me, w);
+      const MailSlot<MAXR, MAXW>& ms = sm.mail[w];
+      if ((s >> lane) & 1u) {
+        const uint32_t nrs = ms.n[lane] & 0xFFu;
+        for (uint32_t k = 0; k < nrs; k++) hash_insert_multi(sm, ms.rs[k][lane], w * 32 + lane);
+      }
+    }
+    __syncwarp();
+    uint32_t pre_hi = 0, lo = 0xFFFFFFFFu;
+    for (uint32_t m = ready; m; m &= m - 1) lo = min(lo, snaps[__ffs(m) - 1]);
+    if (lane == 0) pre_hi = (uint32_t)(ld_acquire_gpu(&p.gs->turn) >> 32);
+    pre_hi = __shfl_sync(0xFFFFFFFFu, pre_hi, 0);
+    const uint32_t floor_ts = pre_hi > p.ring_mask ? pre_hi - p.ring_mask : 0u;
+    if (lo < floor_ts) lo = floor_ts;  // older snapshots fail the RecordAge rule anyway
+    if (p.validate == CSMV_VALIDATE_RING && lo < pre_hi) ring_scan(p, sm, lo, pre_hi, snaps, ready);
 
-    // ---- phases B-E, once per commit section: a CTA/warp batch is one section; the plain
-    // form (CSMV_BATCH_LANE) commits one transaction per section like the reference's per-lane
-    // CAS loop (bank/csmv_sh/API.cu:218-265) ----
+    // ---- one commit section per batch (per transaction for CSMV_BATCH_LANE, like the
+    // reference's per-lane CAS loop, bank/csmv_sh/API.cu:218-265) ----
     const bool lane_sections = p.batch == CSMV_BATCH_LANE;
     uint32_t todo_of_me = surv_of_me, done_of_me = 0;
     uint32_t scanned_hi = pre_hi;
@@ -547,7 +751,6 @@ __device__ void server_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
     while (__any_sync(0xFFFFFFFFu, todo_of_me != 0)) {
       uint32_t sec_of_me = lane_sections ? (todo_of_me & (0u - todo_of_me)) : todo_of_me;
       todo_of_me &= ~sec_of_me;
-      // phase B: ticket, then wait for the turn (bounded)
       uint32_t ticket = 0;
       if (lane == 0) ticket = atomicAdd(&p.gs->ticket, 1u);
       ticket = __shfl_sync(0xFFFFFFFFu, ticket, 0);
@@ -567,9 +770,7 @@ __device__ void server_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
       }
       const uint32_t C = (uint32_t)(__shfl_sync(0xFFFFFFFFu, turn, 0) >> 32);
       fence_acq_rel_gpu();
-
-      // phase C: validate against everything committed since the snapshot
-      if (ring && scanned_hi < C) {
+      if (p.validate == CSMV_VALIDATE_RING && scanned_hi < C) {
         ring_scan(p, sm, scanned_hi, C, snaps, ready);
         scanned_hi = C;
       }
@@ -581,17 +782,10 @@ __device__ void server_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
         bool bad = false, aged = false;
         if ((s >> lane) & 1u) {
           const uint32_t nrs = ms.n[lane] & 0xFFu;
-          if (!ring) {
-            uint32_t st[MAXR];
-#pragma unroll
-            for (int k = 0; k < MAXR; k++)
-              st[k] = k < (int)nrs ? ld_relaxed_gpu(&p.stamp[ms.rs[k][lane]]) : 0u;
-#pragma unroll
-            for (int k = 0; k < MAXR; k++) bad |= st[k] > snap;
-          } else if (p.validate == CSMV_VALIDATE_RING) {
+          if (p.validate == CSMV_VALIDATE_RING) {
             aged = (uint64_t)snap + (p.ring_mask + 1) <= C || ((sm.recage[w] >> lane) & 1u);
             bad = !aged && ((sm.conflict[w] >> lane) & 1u);
-          } else {  // plain per-lane scan of (snap, C]
+          } else {  // plain per-lane scan of (snap, C], bank/csmv_sh/API.cu:88-144
             aged = (uint64_t)snap + (p.ring_mask + 1) <= C;
             for (uint32_t t = snap + 1; t <= C && !aged && !bad; t++) {
               const uint4 r = p.ring[t & p.ring_mask];
@@ -612,8 +806,7 @@ __device__ void server_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
         stat_rw += __popc(f & ~ag);
         if (lane == w) sec_of_me = s & ~f;
       }
-
-      // phase D/E: consecutive timestamps in (warp, lane) order; stamps, records, log
+      // consecutive timestamps in (warp, lane) order; records and log
       uint32_t base = C;
       for (uint32_t m = ready; m; m &= m - 1) {
         const uint32_t w = __ffs(m) - 1;
@@ -628,10 +821,15 @@ __device__ void server_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
           for (int k = 0; k < MAXW; k++) {
             ws.addr[k] = ms.ws[k][lane];
             ws.val[k] = ms.wv[k][lane];
-            if (k < (int)nws) st_relaxed_gpu(&p.stamp[ws.addr[k]], ts);
           }
           p.ring[ts & p.ring_mask] = make_uint4(ts, nws, ws.addr[0], ws.addr[MAXW - 1]);
-          if (p.log) p.log_txn[ts - 1 - p.log_base] = ms.txn[lane];
+          if (p.log) {
+            const uint32_t li = ts - 1 - p.log_base;
+            if (li < p.log_cap)
+              p.log_txn[li] = ms.txn[lane];
+            else
+              raise_error(&p.gs->error, ERR_CAPACITY);
+          }
           if (p.writeback == CSMV_WRITEBACK_SERVER) TXWriteBack<DEPTH>(ts, vs, ws);
           ms.tsl[lane] = ts;
         }
@@ -643,9 +841,9 @@ __device__ void server_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
       if (lane == 0) {
         if (p.writeback == CSMV_WRITEBACK_SERVER && ncommit) st_release_gpu(&p.gs->clock, base);
         st_release_gpu(&p.gs->turn, ((unsigned long long)base << 32) | (ticket + 1u));
+        stat_add(sm.stat, ST_SECTIONS, 1);
       }
       done_of_me |= sec_of_me;
-      // client write-back: the last client warp of the section publishes it on the clock
       if (p.writeback == CSMV_WRITEBACK_CLIENT && ncommit) {
         const uint32_t nw = __popc(__ballot_sync(0xFFFFFFFFu, lane < nc && sec_of_me != 0));
         if (lane == 0) {
@@ -659,8 +857,6 @@ __device__ void server_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
       }
     }
     if (aborted_run) break;
-
-    // ---- phase F: replies ----
     __syncwarp();
     if (lane < nc && ((ready >> lane) & 1u)) {
       MailSlot<MAXR, MAXW>& ms = sm.mail[lane];
@@ -671,7 +867,6 @@ __device__ void server_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
     if (lane == 0) {
       stat_add(sm.stat, ST_ABORT_READ_WRITE, stat_rw);
       stat_add(sm.stat, ST_ABORT_RECORD_AGE, stat_ra);
-      stat_add(sm.stat, ST_SECTIONS, 1);
     }
   }
 }
@@ -691,10 +886,14 @@ __global__ void __launch_bounds__(1024, 1) bank_kernel(BankParams p) {
     sm.mail[i].rep = 0;
   }
   __syncthreads();
-  if (warp == 0)
-    server_warp<DEPTH, MAXR, MAXW>(p, sm);
-  else
+  if (warp == 0) {
+    if (p.validate == CSMV_VALIDATE_STAMP)
+      server_warp_stamp<MAXR, MAXW>(p, sm);
+    else
+      server_warp_ring<DEPTH, MAXR, MAXW>(p, sm);
+  } else {
     client_warp<DEPTH, MAXR, MAXW>(p, sm, warp - 1);
+  }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < ST_COUNT; i += blockDim.x)
     if (sm.stat[i]) atomicAdd(&p.stats[i], sm.stat[i]);

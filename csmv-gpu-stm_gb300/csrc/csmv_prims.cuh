@@ -94,7 +94,8 @@ __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t code) {
 }
 
 // Bounded poll: returns true when pred() holds, false when the budget ran out or another warp
-// raised an error (which is then left in *err). Backs off with nanosleep.
+// raised an error (which is then left in *err). The first polls spin (the commit-order hand-offs
+// are latency-critical), later ones back off with nanosleep up to 256 ns.
 template <class Pred>
 __device__ __forceinline__ bool bounded_wait(Pred pred, uint32_t* err, uint32_t code,
                                              uint32_t limit_log2) {
@@ -103,11 +104,24 @@ __device__ __forceinline__ bool bounded_wait(Pred pred, uint32_t* err, uint32_t 
   for (uint64_t it = 0; it < limit; ++it) {
     if (pred()) return true;
     if ((it & 15u) == 15u && ld_relaxed_gpu(err) != 0) return false;
-    __nanosleep(ns);
-    if (ns < 1024) ns <<= 1;
+    if (it >= 64) {
+      __nanosleep(ns);
+      if (ns < 256) ns <<= 1;
+    }
   }
   raise_error(err, code);
   return false;
+}
+
+// 4-byte asynchronous global->shared copy (lands in shared memory; wait with cp_async_wait_all).
+__device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(smem_dst)),
+               "l"(gmem_src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
 }  // namespace csmv

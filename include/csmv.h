@@ -159,9 +159,10 @@ typedef struct csmv_stats {
   uint64_t aborts_record_age;  /* commit ring no longer covers the snapshot (API.cu:93-100)    */
   uint64_t aborts_read_write;  /* read item written by a later committed transaction          */
   uint64_t aborts_prevalid;    /* lost to a lower lane / earlier batch member (API.cu:94-191)  */
+  uint64_t aborts_write_write; /* write lock held by another warp (stamp protocol)             */
   uint64_t sections;           /* commit sections entered (global order steps)                */
   uint64_t rounds;             /* warp rounds executed, retries included                      */
-  uint32_t final_ts;           /* last commit timestamp                                        */
+  uint32_t final_ts;           /* last timestamp handed out (commits and holes)                */
   uint32_t error;              /* device error word (0 = none); see csmv_last_error           */
   double kernel_ms;            /* device time of the run, CUDA events on the engine stream    */
   double total_ms;             /* host wall time of the call                                   */
@@ -195,8 +196,10 @@ csmv_status csmv_bank_read_values(csmv_bank_t* h, int32_t* host_values);
  * empty slot has ts 0xFFFFFFFF. */
 csmv_status csmv_bank_read_versions(csmv_bank_t* h, uint64_t* host_slots);
 
-/* Commit log of the last run (needs log_commits): host_log_txn[ts-1] = transaction id that
- * committed with timestamp ts, for ts = 1..final_ts. host_outcome[i] for every transaction i:
+/* Commit log of the last run (needs log_commits): host_log_txn[k] = transaction id that
+ * committed with timestamp base+k+1 (base = final ts of the previous run), for every timestamp
+ * the run used; 0xFFFFFFFF marks a timestamp whose transaction failed validation after taking
+ * it (stamp protocol). host_outcome[i] for every transaction i:
  * commit ts for a transfer with writes, else (snapshot | 0x80000000) for read-only/no-write;
  * host_result[i] = read-only sum (0 otherwise). Any pointer may be NULL. */
 csmv_status csmv_bank_read_log(csmv_bank_t* h, uint32_t* host_log_txn, uint32_t n_log,

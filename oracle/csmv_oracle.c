@@ -475,9 +475,11 @@ int orc_bank_check(uint32_t n_txn, const uint32_t* op, const uint32_t* off, cons
     rc = fail(msg, msg_len, "oracle out of memory");
     goto out;
   }
-  /* 1. the log names distinct transfers; outcomes agree with it */
+  /* 1. the log names distinct transfers; outcomes agree with it. 0xFFFFFFFF is a hole: a
+   * timestamp handed to a transaction that then failed validation (no commit). */
   for (uint32_t ts = 1; ts <= final_ts; ts++) {
     uint32_t t = log_txn[ts - 1];
+    if (t == 0xFFFFFFFFu) continue;
     if (t >= n_txn) {
       rc = fail(msg, msg_len, "ts %u: txn id %u out of range", ts, t);
       goto out;
@@ -516,7 +518,7 @@ int orc_bank_check(uint32_t n_txn, const uint32_t* op, const uint32_t* off, cons
   for (uint32_t i = 0; i < n_accounts; i++) vals[i] = init[i];
   init_slots(slots, n_accounts, depth, init);
   for (uint32_t ts = 0; ts <= final_ts; ts++) {
-    if (ts > 0) {
+    if (ts > 0 && log_txn[ts - 1] != 0xFFFFFFFFu) {
       uint32_t t = log_txn[ts - 1];
       int32_t v[64], r, wv[2];
       uint32_t wa[2];

@@ -56,16 +56,15 @@ def test_c1_plain_bank_exact(variant):
     assert st.commits_readonly > 0 and st.commits_update > 0
 
 
+@pytest.mark.parametrize("validate", [cg.VALIDATE_STAMP, cg.VALIDATE_RING])
 @pytest.mark.parametrize("depth", [2, 4, 16])
-def test_high_contention_small_ring_exact(depth):
-    """16 accounts, 32 client warps: most attempts conflict; a 64-record ring forces RecordAge,
-    depth 2 forces DataAge on read-only scans."""
+def test_high_contention_exact(depth, validate):
+    """16 accounts, 32 client warps: most attempts conflict; the ring form runs with a 64-record
+    ring (RecordAge), depth 2 keeps only two versions (DataAge on read-only scans)."""
     w = c1_workload(n_txn=32 * 600, n_accounts=16, pr_read_pct=30, ro_reads=8, up_reads=3, seed=3)
     st, _, _ = run_checked(w, ctas=4, client_warps=8, version_depth=depth, ring_size=64,
-                           validate=cg.VALIDATE_RING)
-    assert st.aborts_read_write + st.aborts_prevalid > 0
-    if depth == 2:
-        assert st.aborts_data_age > 0
+                           validate=validate)
+    assert st.aborts > 0
 
 
 def test_two_accounts_extreme():
@@ -122,6 +121,8 @@ def _replay_values(s, init, log):
     L = orc.lib()
     wa, wv, r = np.zeros(2, np.uint32), np.zeros(2, np.int32), C.c_int32()
     for t in log:
+        if t == 0xFFFFFFFF:  # timestamp of a transaction that failed validation
+            continue
         nr = (int(s.op[t]) >> 2) & 63
         a = s.addr[s.off[t]:s.off[t] + nr].copy()
         v = vals[a].astype(np.int32)
