@@ -36,6 +36,7 @@ namespace csmv {
 
 constexpr uint32_t kSnapFlag = 0x80000000u;
 constexpr uint32_t kHole = 0xFFFFFFFFu;  // log entry of a timestamp whose transaction aborted
+constexpr uint32_t kPendingFlag = 0x80000000u;  // lock word: holder's commit timestamp is known
 constexpr int kMaxClientWarps = 31;
 constexpr int kHashSize = 4096;  // shared-memory hash entries (power of two)
 constexpr int kBatchDescs = 32;
@@ -71,7 +72,8 @@ struct BankParams {
   uint32_t n_rounds;
   uint32_t n_items;
   unsigned long long* slots;
-  unsigned long long* cw;  // per item: stamp | owner << 32
+  unsigned long long* cw;  // per item: stamp | lock << 32; lock = 0 free, warp id + 1 while the
+                           // holder's timestamp is unknown, kPendingFlag | ts once it is known
   uint4* ring;             // {ts, n_writes, w0, w1}
   uint32_t ring_mask;
   uint32_t* done;          // completion bitmap, one bit per timestamp (ring of done_mask+1 words)
@@ -158,7 +160,9 @@ __device__ void complete_range(const BankParams& p, uint32_t lo, uint32_t hi) {
     atomicOr(&p.done[(t >> 5) & p.done_mask], m);
     t += span;
   }
-  __threadfence();
+  // store-buffering pattern with the warp completing the range below ours: with SC fences on
+  // both sides at least one of us sees the other's bits, so the clock never stalls
+  fence_sc_gpu();
   for (uint32_t attempt = 0; attempt < 4096; attempt++) {
     const uint32_t c = ld_acquire_gpu(&p.gs->clock);
     uint32_t n = c;
@@ -236,16 +240,28 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
     }
 
     uint32_t pending = 0xFFFFFFFFu;
+    uint32_t need = 0;  // stamp protocol: a newer commit this lane must see before retrying
     while (pending) {
       if (lane == 0) atomicAdd(&sm.stat[ST_ROUNDS], 1ull);
       const bool mine = (pending >> lane) & 1u;
       ReadSet<MAXR> rs;
       WriteSet<MAXW> ws;
+      // a retry after reading a stamp newer than its snapshot first lets the clock catch up
+      // with that commit (bounded; the reference's TXBegin waits for prevTs the same way,
+      // bank/csmv_sh/API.cu:283), instead of re-failing the same check
+      const uint32_t want = __reduce_max_sync(0xFFFFFFFFu, mine ? need : 0u);
       uint32_t snap = 0;
-      if (lane == 0) snap = TXBegin(&p.gs->clock, rs, ws);
+      if (lane == 0) {
+        snap = TXBegin(&p.gs->clock, rs, ws);
+        for (uint32_t it = 0; snap < want && it < 4096; it++) {
+          __nanosleep(64);
+          snap = ld_acquire_gpu(&p.gs->clock);
+        }
+      }
       rs.n = 0;
       ws.n = 0;
       snap = __shfl_sync(0xFFFFFFFFu, snap, 0);
+      need = 0;
       bool aborted = false;
 
       if (ro) {  // read-only: consistent snapshot read, commits without validation
@@ -290,7 +306,10 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
       }
       bool stale = false;
 #pragma unroll
-      for (int k = 0; k < MAXR; k++) stale |= stv[k] > snap;
+      for (int k = 0; k < MAXR; k++) {
+        stale |= stv[k] > snap;
+        need = max(need, stv[k]);
+      }
       stale = stale && !aborted;
       bool has_w = false;
       if (mine && !aborted && !stale) {
@@ -321,49 +340,59 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
       }
       pending &= ~nwm;
       if (cand == 0) continue;
-      // intra-warp resolution; the stamp protocol always needs it (a lane must not commit after
-      // a lower lane of its own warp wrote what it read: both hold locks of the same owner)
-      if (p.prevalidate || stamp) {
-        const uint32_t pass = TXPreValidation(rs, ws, (cand >> lane) & 1u);
-        if (lane == 0)
-          stat_add(sm.stat, p.prevalidate ? ST_ABORT_PREVALID : ST_ABORT_READ_WRITE,
-                   __popc(cand & ~pass));
-        cand = pass;
-        if (cand == 0) continue;
-      }
       bool cand_me = (cand >> lane) & 1u;
 
-      if (stamp) {  // lock the write items before asking for timestamps
+      if (stamp) {
+        // lock the write items first (before the timestamps are drawn; only the lowest lane
+        // writing an address tries), then resolve lane order among the lanes that hold their
+        // locks, so no lane is dropped for a lower lane that could not lock
+        const bool attempt = cand_me && (TXWriteOverlap(ws, cand_me) & cand) == 0;
         bool got[MAXW];
-        bool all = true;
+        bool all = attempt;
 #pragma unroll
         for (int k = 0; k < MAXW; k++) {
           got[k] = false;
-          if (cand_me && k < (int)ws.n) {
+          if (attempt && k < (int)ws.n) {
             got[k] = atomicCAS(owner_word(p.cw, ws.addr[k]), 0u, me) == 0u;
             all &= got[k];
           }
         }
-        if (cand_me && !all) {
+        const uint32_t locked = __ballot_sync(0xFFFFFFFFu, attempt && all);
+        // intra-warp resolution: always needed here, since a lane must not commit after a lower
+        // lane of its own warp wrote what it read (their locks have the same owner)
+        const uint32_t pass = TXPreValidation(rs, ws, (locked >> lane) & 1u);
+        if (cand_me && !((pass >> lane) & 1u)) {
 #pragma unroll
           for (int k = 0; k < MAXW; k++)
             if (got[k]) st_relaxed_gpu(owner_word(p.cw, ws.addr[k]), 0u);
         }
-        const uint32_t locked = __ballot_sync(0xFFFFFFFFu, cand_me && all);
-        if (lane == 0) stat_add(sm.stat, ST_ABORT_WRITE_WRITE, __popc(cand & ~locked));
-        cand = locked;
+        if (lane == 0) {
+          stat_add(sm.stat, ST_ABORT_WRITE_WRITE, __popc(cand & ~locked));
+          stat_add(sm.stat, p.prevalidate ? ST_ABORT_PREVALID : ST_ABORT_READ_WRITE,
+                   __popc(locked & ~pass));
+        }
+        cand = pass;
         cand_me = (cand >> lane) & 1u;
         if (cand == 0) continue;
-      } else if (cand_me) {  // ring protocol: the server validates from the mailbox
-#pragma unroll
-        for (int k = 0; k < MAXR; k++) ms.rs[k][lane] = rs.addr[k];
-#pragma unroll
-        for (int k = 0; k < MAXW; k++) {
-          ms.ws[k][lane] = ws.addr[k];
-          ms.wv[k][lane] = ws.val[k];
+      } else {
+        if (p.prevalidate) {
+          const uint32_t pass = TXPreValidation(rs, ws, cand_me);
+          if (lane == 0) stat_add(sm.stat, ST_ABORT_PREVALID, __popc(cand & ~pass));
+          cand = pass;
+          cand_me = (cand >> lane) & 1u;
+          if (cand == 0) continue;
         }
-        ms.n[lane] = rs.n | (ws.n << 8);
-        ms.txn[lane] = t;
+        if (cand_me) {  // ring protocol: the server validates from the mailbox
+#pragma unroll
+          for (int k = 0; k < MAXR; k++) ms.rs[k][lane] = rs.addr[k];
+#pragma unroll
+          for (int k = 0; k < MAXW; k++) {
+            ms.ws[k][lane] = ws.addr[k];
+            ms.wv[k][lane] = ws.val[k];
+          }
+          ms.n[lane] = rs.n | (ws.n << 8);
+          ms.txn[lane] = t;
+        }
       }
       // post the request into the shared-memory mailbox, wait for the reply
       seq++;
@@ -386,10 +415,18 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
 
       uint32_t okm = 0, my_ts = 0;
       if (stamp) {
-        // timestamps base+1.. in lane order over the locked lanes; validate the reads now
+        // timestamps base+1.. in lane order over the locked lanes
         const uint32_t base = ms.base;
         my_ts = base + 1 + __popc(cand & lanemask_lt());
         fence_acq_rel_gpu();
+        // advertise the pending timestamp in the lock words: a validator later in the order
+        // may then ignore our lock, one earlier waits for our outcome instead of aborting
+#pragma unroll
+        for (int k = 0; k < MAXW; k++)
+          if (cand_me && k < (int)ws.n) st_relaxed_gpu(owner_word(p.cw, ws.addr[k]), kPendingFlag | my_ts);
+        // validate the reads: the stamp must not be newer than the snapshot, and a lock held by
+        // a transaction earlier in the order (or one whose timestamp is not known yet) must be
+        // resolved first. Waits only ever point to smaller timestamps: no cycles.
         bool valid = cand_me;
         if (cand_me) {
           unsigned long long word[MAXR];
@@ -398,8 +435,21 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
             word[k] = k < (int)rs.n ? ld_relaxed_gpu(&p.cw[rs.addr[k]]) : 0ull;
 #pragma unroll
           for (int k = 0; k < MAXR; k++) {
-            const uint32_t own = (uint32_t)(word[k] >> 32), st = (uint32_t)word[k];
-            if (k < (int)rs.n) valid &= (own == 0u || own == me) && st <= snap;
+            if (k >= (int)rs.n || !valid) continue;
+            unsigned long long wd = word[k];
+            bool settled = false;
+            for (uint32_t it = 0; it < 2048; it++) {
+              const uint32_t own = (uint32_t)(wd >> 32);
+              if (own == 0u || own == me || ((own & kPendingFlag) && (own & ~kPendingFlag) >= my_ts)) {
+                settled = true;
+                break;
+              }
+              __nanosleep(32);
+              wd = ld_relaxed_gpu(&p.cw[rs.addr[k]]);
+            }
+            const uint32_t st = (uint32_t)wd;
+            valid = settled && st <= snap;
+            need = max(need, st);
           }
         }
         okm = __ballot_sync(0xFFFFFFFFu, valid);
@@ -525,7 +575,7 @@ __device__ void server_warp_stamp(const BankParams& p, CtaShared<MAXR, MAXW>& sm
     }
     const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
     uint32_t t0 = 0;
-    if (lane == 0) t0 = atomicAdd(&p.gs->ts_next, total);
+    if (lane == 0) t0 = atom_add_acq_rel_gpu(&p.gs->ts_next, total);
     t0 = __shfl_sync(0xFFFFFFFFu, t0, 0);
     if (mine) {
       sm.mail[lane].base = t0 + incl - cnt;

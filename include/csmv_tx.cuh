@@ -166,6 +166,28 @@ __device__ __forceinline__ uint32_t TXPreValidation(const ReadSet<MAXR>& rs,
   return commit;
 }
 
+// Lanes below this one (among the active lanes) whose write sets share an address with this
+// lane's write set, warp-collective. The stamp protocol lets only the lowest writer of an
+// address in a warp try for its lock, so the warp's outcome never depends on which lane's atomic
+// the memory system serves first.
+template <int MAXW>
+__device__ __forceinline__ uint32_t TXWriteOverlap(const WriteSet<MAXW>& ws, bool active) {
+  const uint32_t me = lane_id();
+  uint32_t overlap = 0;
+  for (uint32_t i = 0; i < 31; i++) {
+    const uint32_t nw = __shfl_sync(0xFFFFFFFFu, active ? ws.n : 0u, i);
+#pragma unroll
+    for (int j = 0; j < MAXW; j++) {
+      const uint32_t a = __shfl_sync(0xFFFFFFFFu, ws.addr[j], i);
+      bool hit = false;
+#pragma unroll
+      for (int k = 0; k < MAXW; k++) hit |= (k < (int)ws.n) && (ws.addr[k] == a);
+      if (active && i < me && (uint32_t)j < nw && hit) overlap |= 1u << i;
+    }
+  }
+  return overlap;
+}
+
 // Slot to overwrite with a new version: an empty slot first, else the oldest - the slot the
 // reference frees by advancing tail (bank/csmv_sh/API.cu:157-161). Lowest index on ties.
 template <int DEPTH>

@@ -576,7 +576,7 @@ out:
  * lanes with consecutive timestamps in lane order. Failed lanes retry the same transaction. */
 int orc_bank_sim_1warp(uint32_t n_txn, const uint32_t* op, const uint32_t* off,
                        const uint32_t* addr, uint32_t n_accounts, const int32_t* init,
-                       int depth, int prevalidate, uint64_t* slots, uint32_t* log_txn,
+                       int depth, int prevalidate, int locks, uint64_t* slots, uint32_t* log_txn,
                        uint32_t* outcome, int32_t* result, orc_sim_stats* st) {
   memset(st, 0, sizeof(*st));
   init_slots(slots, n_accounts, depth, init);
@@ -614,11 +614,24 @@ int orc_bank_sim_1warp(uint32_t n_txn, const uint32_t* op, const uint32_t* off,
         cand |= 1u << l;
       }
       if (!cand) continue;
-      uint32_t pass = orc_prevalidate(&rs[0][0], nrs, 32, &ws[0][0], nws, 2, cand, NULL);
+      uint32_t locked = cand;
+      if (locks) { /* only the lowest candidate writing an address takes its lock */
+        for (int l = 0; l < 32; l++) {
+          if (!((cand >> l) & 1)) continue;
+          for (int i = 0; i < l; i++) {
+            if (!((cand >> i) & 1)) continue;
+            for (uint32_t x = 0; x < nws[l]; x++)
+              for (uint32_t y = 0; y < nws[i]; y++)
+                if (ws[l][x] == ws[i][y]) locked &= ~(1u << l);
+          }
+        }
+        st->aborts_write_write += (uint64_t)__builtin_popcount(cand & ~locked);
+      }
+      uint32_t pass = orc_prevalidate(&rs[0][0], nrs, 32, &ws[0][0], nws, 2, locked, NULL);
       if (prevalidate)
-        st->aborts_prevalid += (uint64_t)__builtin_popcount(cand & ~pass);
+        st->aborts_prevalid += (uint64_t)__builtin_popcount(locked & ~pass);
       else
-        st->aborts_read_write += (uint64_t)__builtin_popcount(cand & ~pass);
+        st->aborts_read_write += (uint64_t)__builtin_popcount(locked & ~pass);
       for (int l = 0; l < 32; l++) {
         if (!((pass >> l) & 1)) continue;
         uint32_t t = g * 32 + l, ts = ++clock;

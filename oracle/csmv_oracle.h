@@ -113,13 +113,16 @@ int orc_bank_check(uint32_t n_txn, const uint32_t* op, const uint32_t* off, cons
 /* Deterministic model of the GB300 engine with one client warp and one server. */
 typedef struct orc_sim_stats {
   uint64_t commits_update, commits_readonly, commits_nowrite, aborts_prevalid,
-      aborts_read_write, rounds;
+      aborts_read_write, rounds, aborts_write_write;
   uint32_t final_ts;
 } orc_sim_stats;
+/* locks = 1 models the stamp protocol's intra-warp rule (a lane whose write set overlaps a lower
+ * candidate's does not lock; lane order is then resolved among the locked lanes), locks = 0 the
+ * ring protocol (lane order among all candidates). */
 int orc_bank_sim_1warp(uint32_t n_txn, const uint32_t* op, const uint32_t* off,
                        const uint32_t* addr, uint32_t n_accounts, const int32_t* init,
-                       int depth, int prevalidate, uint64_t* slots_out, uint32_t* log_txn,
-                       uint32_t* outcome, int32_t* result, orc_sim_stats* st);
+                       int depth, int prevalidate, int locks, uint64_t* slots_out,
+                       uint32_t* log_txn, uint32_t* outcome, int32_t* result, orc_sim_stats* st);
 
 /* CPU baselines: executes the stream, returns elapsed nanoseconds in *ns. */
 int orc_bank_serial(uint32_t n_txn, const uint32_t* op, const uint32_t* off,

@@ -44,7 +44,8 @@ class Record(C.Structure):
 class SimStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("commits_update", "commits_readonly",
                                           "commits_nowrite", "aborts_prevalid",
-                                          "aborts_read_write", "rounds")] + [
+                                          "aborts_read_write", "rounds",
+                                          "aborts_write_write")] + [
         ("final_ts", C.c_uint32)]
 
 
@@ -78,7 +79,7 @@ def lib() -> C.CDLL:
             "orc_memcd_set_slot": (I, [P, P, P, I, C.c_int32]),
             "orc_bank_exec": (I, [U, P, P, P, P, P]),
             "orc_bank_check": (I, [U, P, P, P, U, P, I, U, P, P, P, P, C.c_char_p, I]),
-            "orc_bank_sim_1warp": (I, [U, P, P, P, U, P, I, I, P, P, P, P, P]),
+            "orc_bank_sim_1warp": (I, [U, P, P, P, U, P, I, I, I, P, P, P, P, P]),
             "orc_bank_serial": (I, [U, P, P, P, U, P, P]),
             "orc_bank_locked": (I, [U, P, P, P, U, P, I, P]),
         })
@@ -143,7 +144,7 @@ def check(op, off, addr, n_accounts, init, depth, final_ts, log_txn, outcome, re
     return None if rc == 0 else msg.value.decode()
 
 
-def sim_1warp(op, off, addr, n_accounts, init, depth, prevalidate=True):
+def sim_1warp(op, off, addr, n_accounts, init, depth, prevalidate=True, locks=True):
     n = len(op)
     slots = np.empty(n_accounts * depth, np.uint64)
     log_txn = np.zeros(n, np.uint32)
@@ -152,7 +153,8 @@ def sim_1warp(op, off, addr, n_accounts, init, depth, prevalidate=True):
     st = SimStats()
     init = np.ascontiguousarray(init, np.int32)
     rc = lib().orc_bank_sim_1warp(C.c_uint32(n), p(op), p(off), p(addr), C.c_uint32(n_accounts),
-                                  p(init), C.c_int(depth), C.c_int(int(prevalidate)), p(slots),
+                                  p(init), C.c_int(depth), C.c_int(int(prevalidate)),
+                                  C.c_int(int(locks)), p(slots),
                                   p(log_txn), p(outcome), p(result), C.byref(st))
     assert rc == 0
     return slots, log_txn[:st.final_ts], outcome, result, st

@@ -25,15 +25,16 @@ def test_one_client_warp_equals_oracle_model(prevalidate, validate):
         w, ctas=1, client_warps=1, prevalidate=prevalidate, validate=validate, batch=cg.BATCH_WARP,
         init_value=100)
     init = np.full(40, 100, np.int32)
-    mslots, mlog, mout, mres, ms = orc.sim_1warp(s.op, s.off, s.addr, 40, init, 4, bool(prevalidate))
+    mslots, mlog, mout, mres, ms = orc.sim_1warp(s.op, s.off, s.addr, 40, init, 4, bool(prevalidate),
+                                                 locks=validate == cg.VALIDATE_STAMP)
     np.testing.assert_array_equal(log_txn, mlog)
     np.testing.assert_array_equal(outcome, mout)
     np.testing.assert_array_equal(result, mres)
     np.testing.assert_array_equal(slots, mslots)
     assert (st.commits_update, st.commits_readonly, st.commits_nowrite) == (
         ms.commits_update, ms.commits_readonly, ms.commits_nowrite)
-    assert (st.aborts_prevalid, st.aborts_read_write, st.rounds) == (
-        ms.aborts_prevalid, ms.aborts_read_write, ms.rounds)
+    assert (st.aborts_prevalid, st.aborts_read_write, st.aborts_write_write, st.rounds) == (
+        ms.aborts_prevalid, ms.aborts_read_write, ms.aborts_write_write, ms.rounds)
     assert st.aborts_data_age == 0 and st.aborts_record_age == 0
 
 

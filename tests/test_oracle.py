@@ -235,12 +235,13 @@ def test_check_rejects_planted_mistakes():
     assert orc.check(*args, dup, outcome, result, slots) is not None
 
 
+@pytest.mark.parametrize("locks", [True, False])
 @pytest.mark.parametrize("prevalidate", [True, False])
-def test_one_warp_model_is_exact(prevalidate):
+def test_one_warp_model_is_exact(prevalidate, locks):
     w = small_workload(n_txn=32 * 64, n_accounts=40)
     op, off, addr = orc.generate(w)
     init = np.full(40, 100, np.int32)
-    slots, log, outcome, result, st = orc.sim_1warp(op, off, addr, 40, init, 4, prevalidate)
+    slots, log, outcome, result, st = orc.sim_1warp(op, off, addr, 40, init, 4, prevalidate, locks)
     assert st.commits_update + st.commits_readonly + st.commits_nowrite == len(op)
     assert orc.check(op, off, addr, 40, init, 4, st.final_ts, log, outcome, result, slots) is None
     assert (st.aborts_prevalid if prevalidate else st.aborts_read_write) > 0
