@@ -162,7 +162,7 @@ __device__ void complete_range(const BankParams& p, uint32_t lo, uint32_t hi) {
   }
   // store-buffering pattern with the warp completing the range below ours: with SC fences on
   // both sides at least one of us sees the other's bits, so the clock never stalls
-  fence_sc_gpu();
+  __threadfence();
   for (uint32_t attempt = 0; attempt < 4096; attempt++) {
     const uint32_t c = ld_acquire_gpu(&p.gs->clock);
     uint32_t n = c;
@@ -223,8 +223,10 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
     const uint32_t op = p.op[t];
     const uint32_t kind = CSMV_OP_KIND(op), nr = CSMV_OP_NREADS(op);
     const uint32_t off = p.off[t];
-    const bool ro = (kind == CSMV_KIND_READONLY);
-    bool bad = !ro && (nr < 2 || nr > (uint32_t)MAXR);
+    // the round's kind must be warp-uniform (the stream format guarantees it, the reference
+    // decides it per warp, bank/csmv_sh/exe.cu:134-139): every branch on it holds collectives
+    const bool ro = __all_sync(0xFFFFFFFFu, kind == CSMV_KIND_READONLY);
+    bool bad = (ro != (kind == CSMV_KIND_READONLY)) || (!ro && (nr < 2 || nr > (uint32_t)MAXR));
     uint32_t a[MAXR];
 #pragma unroll
     for (int k = 0; k < MAXR; k++) {
@@ -346,7 +348,9 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
         // lock the write items first (before the timestamps are drawn; only the lowest lane
         // writing an address tries), then resolve lane order among the lanes that hold their
         // locks, so no lane is dropped for a lower lane that could not lock
-        const bool attempt = cand_me && (TXWriteOverlap(ws, cand_me) & cand) == 0;
+        // (warp-collective: every lane calls it, candidate or not)
+        const uint32_t overlap = TXWriteOverlap(ws, cand_me);
+        const bool attempt = cand_me && (overlap & cand) == 0;
         bool got[MAXW];
         bool all = attempt;
 #pragma unroll
@@ -498,7 +502,9 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
       __syncwarp();
       if (lane == 0) stat_add(sm.stat, ST_COMMIT_UPDATE, __popc(okm));
       pending &= ~okm;
-      if (ld_relaxed_gpu(&p.gs->error) != 0) {
+      uint32_t err = 0;  // read once and broadcast: the warp leaves the loop together
+      if (lane == 0) err = ld_relaxed_gpu(&p.gs->error);
+      if (__shfl_sync(0xFFFFFFFFu, err, 0) != 0) {
         failed = true;
         break;
       }
@@ -575,7 +581,11 @@ __device__ void server_warp_stamp(const BankParams& p, CtaShared<MAXR, MAXW>& sm
     }
     const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
     uint32_t t0 = 0;
-    if (lane == 0) t0 = atom_add_acq_rel_gpu(&p.gs->ts_next, total);
+    if (lane == 0) {  // fences on both sides order the draw after the observed locks and
+      __threadfence();  // before the validations that follow it
+      t0 = atomicAdd(&p.gs->ts_next, total);
+      __threadfence();
+    }
     t0 = __shfl_sync(0xFFFFFFFFu, t0, 0);
     if (mine) {
       sm.mail[lane].base = t0 + incl - cnt;

@@ -62,14 +62,7 @@ __device__ __forceinline__ void ld_relaxed_gpu_v2(const unsigned long long* p,
 __device__ __forceinline__ void fence_acq_rel_gpu() {
   asm volatile("fence.acq_rel.gpu;" ::: "memory");
 }
-__device__ __forceinline__ void fence_sc_gpu() { asm volatile("fence.sc.gpu;" ::: "memory"); }
-// fetch-and-add with acquire-release semantics at gpu scope (orders the commit-timestamp draw
-// after the locks the caller observed and before the validation reads that follow it)
-__device__ __forceinline__ uint32_t atom_add_acq_rel_gpu(uint32_t* p, uint32_t v) {
-  uint32_t old;
-  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
-  return old;
-}
+
 
 // ---- shared (cta scope) -------------------------------------------------------------------
 __device__ __forceinline__ uint32_t ld_acquire_cta(const uint32_t* p) {

@@ -30,15 +30,15 @@ struct VersionStore {
 
 template <int MAXR>
 struct ReadSet {
-  uint32_t n;
-  uint32_t addr[MAXR];
+  uint32_t n = 0;
+  uint32_t addr[MAXR] = {};
 };
 
 template <int MAXW>
 struct WriteSet {
-  uint32_t n;
-  uint32_t addr[MAXW];
-  int32_t val[MAXW];
+  uint32_t n = 0;
+  uint32_t addr[MAXW] = {};
+  int32_t val[MAXW] = {};
 };
 
 __device__ __forceinline__ unsigned long long pack_version(uint32_t ts, int32_t v) {
