@@ -145,6 +145,51 @@ __device__ __forceinline__ uint32_t* owner_word(unsigned long long* cw, uint32_t
   return reinterpret_cast<uint32_t*>(cw + x) + 1;  // high half of the little-endian word
 }
 
+// Writes of a transfer given the values it read (include/csmv.h): amount from amt0 and the extra
+// reads, debit a0 / credit a1 when funds suffice (always for CSMV_KIND_TRANSFER_ALWAYS).
+template <int MAXR>
+__device__ __forceinline__ bool transfer_writes(uint32_t op, uint32_t nr, const int32_t (&v)[MAXR],
+                                                int32_t& w0, int32_t& w1) {
+  uint32_t acc = CSMV_OP_AMT0(op) - 1u;
+#pragma unroll
+  for (int k = 2; k < MAXR; k++)
+    if (k < (int)nr) acc += (uint32_t)v[k];
+  const uint32_t amt = 1u + acc % CSMV_OP_AMOD(op);
+  w0 = (int32_t)((uint32_t)v[0] - amt);
+  w1 = (int32_t)((uint32_t)v[1] + amt);
+  return CSMV_OP_KIND(op) == CSMV_KIND_TRANSFER_ALWAYS || v[0] >= (int32_t)amt;
+}
+
+// Install versions (ts, value) into an item whose lock the caller holds: `n` insertions applied
+// to the item's slots in registers (victim = empty, else oldest), then stored back.
+template <int DEPTH>
+struct SlotEditor {
+  unsigned long long s[DEPTH];
+  __device__ __forceinline__ void load(const unsigned long long* item) {
+#pragma unroll
+    for (int d = 0; d < DEPTH; d += 2) ld_relaxed_gpu_v2(item + d, s[d], s[d + 1]);
+  }
+  __device__ __forceinline__ void insert(uint32_t ts, int32_t v) {
+    int vic = 0;
+    uint32_t key = version_ts(s[0]) + 1u;
+#pragma unroll
+    for (int d = 1; d < DEPTH; d++) {
+      const uint32_t k = version_ts(s[d]) + 1u;
+      if (k < key) {
+        key = k;
+        vic = d;
+      }
+    }
+#pragma unroll
+    for (int d = 0; d < DEPTH; d++)
+      if (d == vic) s[d] = pack_version(ts, v);
+  }
+  __device__ __forceinline__ void store(unsigned long long* item) const {
+#pragma unroll
+    for (int d = 0; d < DEPTH; d++) st_relaxed_gpu(item + d, s[d]);
+  }
+};
+
 // ---------------------------------------------------------------------------------------------
 // clock: completion bitmap
 // ---------------------------------------------------------------------------------------------
@@ -313,6 +358,219 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
         need = max(need, stv[k]);
       }
       stale = stale && !aborted;
+
+      // ---- stamp protocol with intra-warp chaining (prevalidate == 2): instead of aborting a
+      // lane that read what a lower lane writes (TXPreValidation), the warp runs its transfers as
+      // one serial chain in lane order, forwarding each lower lane's written values to the lanes
+      // that read them; only reads taken from the snapshot are validated, each written account
+      // is locked once (by its lowest writer), and every link of the chain gets the next commit
+      // timestamp. A link whose lock or validation fails takes down the links that consumed it.
+      if (stamp && p.prevalidate == 2) {
+        const bool okr = mine && !aborted && !stale;
+        uint32_t dep = 0;  // lower lanes whose possible writes {a0, a1} hit my reads
+        for (uint32_t i = 0; i < 31; i++) {
+          const bool oki = __shfl_sync(0xFFFFFFFFu, okr, i);
+          const uint32_t x0 = __shfl_sync(0xFFFFFFFFu, a[0], i), x1 = __shfl_sync(0xFFFFFFFFu, a[1], i);
+          bool hit = false;
+#pragma unroll
+          for (int k = 0; k < MAXR; k++) hit |= (k < (int)nr) && (a[k] == x0 || a[k] == x1);
+          if (okr && oki && i < lane && hit) dep |= 1u << i;
+        }
+        const uint32_t srcs = __reduce_or_sync(0xFFFFFFFFu, dep);
+        uint32_t fwd = 0, fwdk = 0;  // lanes whose values I consumed / my reads that were forwarded
+        for (uint32_t m = srcs; m; m &= m - 1) {
+          const uint32_t i = __ffs(m) - 1;
+          int32_t w0, w1;
+          const bool hw = okr && transfer_writes<MAXR>(op, nr, v, w0, w1);
+          const bool hwi = __shfl_sync(0xFFFFFFFFu, hw, i);
+          const uint32_t x0 = __shfl_sync(0xFFFFFFFFu, a[0], i), x1 = __shfl_sync(0xFFFFFFFFu, a[1], i);
+          const int32_t y0 = __shfl_sync(0xFFFFFFFFu, w0, i), y1 = __shfl_sync(0xFFFFFFFFu, w1, i);
+          if (okr && lane > i && hwi) {
+#pragma unroll
+            for (int k = 0; k < MAXR; k++) {
+              if (k >= (int)nr) continue;
+              if (a[k] == x0) {
+                v[k] = y0;
+                fwd |= 1u << i;
+                fwdk |= 1u << k;
+              } else if (a[k] == x1) {
+                v[k] = y1;
+                fwd |= 1u << i;
+                fwdk |= 1u << k;
+              }
+            }
+          }
+        }
+        int32_t w0, w1;
+        const bool has_w = okr && transfer_writes<MAXR>(op, nr, v, w0, w1);
+        const bool part = okr && (has_w || fwd != 0);      // a link of the chain: needs a timestamp
+        const bool snap_ok = okr && !has_w && fwd == 0;    // read-only outcome at the snapshot
+        // lock leaders: the lowest lane writing each address takes its lock
+        uint32_t lead_lane[2] = {lane, lane}, lead_slot[2] = {0u, 1u};
+        bool found[2] = {false, false};
+        for (uint32_t i = 0; i < 32; i++) {
+          const bool h = __shfl_sync(0xFFFFFFFFu, has_w, i);
+          const uint32_t x0 = __shfl_sync(0xFFFFFFFFu, a[0], i), x1 = __shfl_sync(0xFFFFFFFFu, a[1], i);
+#pragma unroll
+          for (int k = 0; k < 2; k++) {
+            if (has_w && !found[k] && h && (x0 == a[k] || x1 == a[k])) {
+              lead_lane[k] = i;
+              lead_slot[k] = x0 == a[k] ? 0u : 1u;
+              found[k] = true;
+            }
+          }
+        }
+        bool got[2] = {false, false};
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+          if (has_w && lead_lane[k] == lane) got[k] = atomicCAS(owner_word(p.cw, a[k]), 0u, me) == 0u;
+        bool lock_ok = true;
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+          const bool g0 = __shfl_sync(0xFFFFFFFFu, got[0], lead_lane[k]);
+          const bool g1 = __shfl_sync(0xFFFFFFFFu, got[1], lead_lane[k]);
+          if (has_w) lock_ok &= lead_slot[k] == 0 ? g0 : g1;
+        }
+        uint32_t F = 0;  // failed links, cascading to the links that consumed them
+        for (uint32_t i = 0; i < 32; i++)
+          F |= __ballot_sync(0xFFFFFFFFu, lane == i && part && (!lock_ok || (fwd & F) != 0));
+        const uint32_t partm = __ballot_sync(0xFFFFFFFFu, part);
+        const uint32_t lockf = __ballot_sync(0xFFFFFFFFu, part && !lock_ok);
+        const uint32_t snapm = __ballot_sync(0xFFFFFFFFu, snap_ok);
+        const uint32_t agm = __ballot_sync(0xFFFFFFFFu, mine && aborted);
+        const uint32_t stm = __ballot_sync(0xFFFFFFFFu, mine && stale);
+        if (snap_ok && p.log) {
+          p.outcome[t] = snap | kSnapFlag;
+          p.result[t] = 0;
+        }
+        if (lane == 0) {
+          stat_add(sm.stat, ST_COMMIT_NOWRITE, __popc(snapm));
+          stat_add(sm.stat, ST_ABORT_DATA_AGE, __popc(agm));
+          stat_add(sm.stat, ST_ABORT_READ_WRITE, __popc(stm));
+          stat_add(sm.stat, ST_ABORT_WRITE_WRITE, __popc(lockf));
+          stat_add(sm.stat, ST_ABORT_PREVALID, __popc(F & ~lockf));
+        }
+        const uint32_t cand = partm & ~F;
+        const bool cand_me = (cand >> lane) & 1u;
+        uint32_t C = 0, base = 0, my_ts = 0;
+        if (cand) {
+          seq++;
+          __syncwarp();
+          if (lane == 0) {
+            ms.snap = snap;
+            ms.cand = cand;
+            st_release_cta(&ms.req, seq);
+          }
+          bool ok_wait = true;
+          if (lane == 0)
+            ok_wait = bounded_wait([&] { return ld_acquire_cta(&ms.rep) == seq; }, &p.gs->error,
+                                   ERR_WAIT_REPLY, p.spin_log2);
+          ok_wait = __shfl_sync(0xFFFFFFFFu, ok_wait, 0);
+          if (!ok_wait) {
+            failed = true;
+            break;
+          }
+          (void)ld_acquire_cta(&ms.rep);
+          base = ms.base;
+          my_ts = base + 1 + __popc(cand & lanemask_lt());
+          fence_acq_rel_gpu();
+#pragma unroll
+          for (int k = 0; k < 2; k++)
+            if (got[k] && cand_me) st_relaxed_gpu(owner_word(p.cw, a[k]), kPendingFlag | my_ts);
+          // validate the reads that came from the snapshot (forwarded ones are the chain's own)
+          bool valid = cand_me;
+          if (cand_me) {
+            unsigned long long word[MAXR];
+#pragma unroll
+            for (int k = 0; k < MAXR; k++)
+              word[k] = (k < (int)nr && !((fwdk >> k) & 1u)) ? ld_relaxed_gpu(&p.cw[a[k]]) : 0ull;
+#pragma unroll
+            for (int k = 0; k < MAXR; k++) {
+              if (k >= (int)nr || ((fwdk >> k) & 1u) || !valid) continue;
+              unsigned long long wd = word[k];
+              bool settled = false;
+              for (uint32_t it = 0; it < 2048; it++) {
+                const uint32_t own = (uint32_t)(wd >> 32);
+                if (own == 0u || own == me || ((own & kPendingFlag) && (own & ~kPendingFlag) >= my_ts)) {
+                  settled = true;
+                  break;
+                }
+                __nanosleep(32);
+                wd = ld_relaxed_gpu(&p.cw[a[k]]);
+              }
+              const uint32_t st = (uint32_t)wd;
+              valid = settled && st <= snap;
+              need = max(need, st);
+            }
+          }
+          uint32_t F2 = 0;
+          for (uint32_t i = 0; i < 32; i++)
+            F2 |= __ballot_sync(0xFFFFFFFFu, lane == i && cand_me && (!valid || (fwd & F2) != 0));
+          C = cand & ~F2;
+          const bool commit = (C >> lane) & 1u;
+          if (lane == 0) stat_add(sm.stat, ST_ABORT_READ_WRITE, __popc(F2));
+          if (p.log && cand_me) {
+            const uint32_t li = my_ts - 1 - p.log_base;
+            if (li < p.log_cap)
+              p.log_txn[li] = commit ? t : kHole;
+            else
+              raise_error(&p.gs->error, ERR_CAPACITY);
+          }
+          if (commit && p.log) {
+            p.outcome[t] = my_ts;
+            p.result[t] = 0;
+          }
+          // write-back by the lock leaders: every committed link's version of the item, in
+          // timestamp order, then the stamp of the last one and the unlock
+          const uint32_t hwm = __ballot_sync(0xFFFFFFFFu, has_w && commit);
+#pragma unroll
+          for (int k = 0; k < 2; k++) {
+            const bool lead = got[k];
+            unsigned long long* item = p.slots + (size_t)a[k] * DEPTH;
+            SlotEditor<DEPTH> ed;
+            if (lead) ed.load(item);
+            uint32_t last = 0;
+            for (uint32_t m = hwm; m; m &= m - 1) {
+              const uint32_t i = __ffs(m) - 1;
+              const uint32_t x0 = __shfl_sync(0xFFFFFFFFu, a[0], i), x1 = __shfl_sync(0xFFFFFFFFu, a[1], i);
+              const int32_t y0 = __shfl_sync(0xFFFFFFFFu, w0, i), y1 = __shfl_sync(0xFFFFFFFFu, w1, i);
+              const uint32_t ti = __shfl_sync(0xFFFFFFFFu, my_ts, i);
+              if (lead && (x0 == a[k] || x1 == a[k])) {
+                ed.insert(ti, x0 == a[k] ? y0 : y1);
+                last = ti;
+              }
+            }
+            if (lead && last) ed.store(item);
+            __threadfence();
+            if (lead) {
+              if (last)
+                st_release_gpu(&p.cw[a[k]], (unsigned long long)last);  // stamp, unlock
+              else
+                st_relaxed_gpu(owner_word(p.cw, a[k]), 0u);
+            }
+          }
+          __syncwarp();
+          if (lane == 0) complete_range(p, base + 1, base + __popc(cand));
+        } else {
+          // no links: leaders release whatever they locked
+#pragma unroll
+          for (int k = 0; k < 2; k++)
+            if (got[k]) st_relaxed_gpu(owner_word(p.cw, a[k]), 0u);
+        }
+        const uint32_t hw_c = __ballot_sync(0xFFFFFFFFu, has_w && ((C >> lane) & 1u));
+        if (lane == 0) {
+          stat_add(sm.stat, ST_COMMIT_UPDATE, __popc(hw_c));
+          stat_add(sm.stat, ST_COMMIT_NOWRITE, __popc(C & ~hw_c));
+        }
+        pending &= ~(C | snapm);
+        uint32_t err = 0;
+        if (lane == 0) err = ld_relaxed_gpu(&p.gs->error);
+        if (__shfl_sync(0xFFFFFFFFu, err, 0) != 0) {
+          failed = true;
+          break;
+        }
+        continue;
+      }
       bool has_w = false;
       if (mine && !aborted && !stale) {
         uint32_t acc = CSMV_OP_AMT0(op) - 1u;

@@ -17,15 +17,17 @@ from gpu_util import c1_workload, run_checked
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("prevalidate", [1, 0])
+@pytest.mark.parametrize("prevalidate", [1, 0, 2])
 @pytest.mark.parametrize("validate", [cg.VALIDATE_STAMP, cg.VALIDATE_RING, cg.VALIDATE_RING_LANE])
 def test_one_client_warp_equals_oracle_model(prevalidate, validate):
+    if prevalidate == 2 and validate != cg.VALIDATE_STAMP:
+        pytest.skip("intra-warp chaining is a stamp-protocol mode")
     w = c1_workload(n_txn=32 * 96, n_accounts=40, pr_read_pct=20, up_reads=3, seed=11)
     st, s, (log_txn, outcome, result, slots) = run_checked(
         w, ctas=1, client_warps=1, prevalidate=prevalidate, validate=validate, batch=cg.BATCH_WARP,
         init_value=100)
     init = np.full(40, 100, np.int32)
-    mslots, mlog, mout, mres, ms = orc.sim_1warp(s.op, s.off, s.addr, 40, init, 4, bool(prevalidate),
+    mslots, mlog, mout, mres, ms = orc.sim_1warp(s.op, s.off, s.addr, 40, init, 4, prevalidate,
                                                  locks=validate == cg.VALIDATE_STAMP)
     np.testing.assert_array_equal(log_txn, mlog)
     np.testing.assert_array_equal(outcome, mout)
@@ -47,6 +49,7 @@ VARIANTS = {
     "ring-warp-server": dict(validate=cg.VALIDATE_RING, batch=cg.BATCH_WARP, writeback=cg.WRITEBACK_SERVER),
     "ringlane-warp-client": dict(validate=cg.VALIDATE_RING_LANE, batch=cg.BATCH_WARP),
     "stamp-cta-noprevalid": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CTA, prevalidate=0),
+    "stamp-cta-chain": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CTA, prevalidate=2),
 }
 
 
@@ -57,14 +60,15 @@ def test_c1_plain_bank_exact(variant):
     assert st.commits_readonly > 0 and st.commits_update > 0
 
 
-@pytest.mark.parametrize("validate", [cg.VALIDATE_STAMP, cg.VALIDATE_RING])
+@pytest.mark.parametrize("validate,prevalidate", [(cg.VALIDATE_STAMP, 1), (cg.VALIDATE_STAMP, 2),
+                                                  (cg.VALIDATE_RING, 1)])
 @pytest.mark.parametrize("depth", [2, 4, 16])
-def test_high_contention_exact(depth, validate):
+def test_high_contention_exact(depth, validate, prevalidate):
     """16 accounts, 32 client warps: most attempts conflict; the ring form runs with a 64-record
     ring (RecordAge), depth 2 keeps only two versions (DataAge on read-only scans)."""
     w = c1_workload(n_txn=32 * 600, n_accounts=16, pr_read_pct=30, ro_reads=8, up_reads=3, seed=3)
     st, _, _ = run_checked(w, ctas=4, client_warps=8, version_depth=depth, ring_size=64,
-                           validate=validate)
+                           validate=validate, prevalidate=prevalidate)
     assert st.aborts > 0
 
 
@@ -77,19 +81,20 @@ def test_single_round():
     run_checked(c1_workload(n_txn=32, n_accounts=100), ctas=1, client_warps=1)
 
 
-def test_zipf_contended_full_gpu_exact():
-    """1M accounts, Zipf 0.99, read 4 / write 2, 20% read-only scans of 32, persistent grid."""
-    w = cg.bank_workload(1 << 20, 1 << 18, seed=9, pr_read_pct=20, ro_reads=32, up_reads=4,
+@pytest.mark.parametrize("prevalidate", [2, 1])
+def test_zipf_contended_exact(prevalidate):
+    """1M accounts, Zipf 0.99, read 4 / write 2, 20% read-only scans of 32, one CTA per SM."""
+    w = cg.bank_workload(1 << 20, 1 << 16, seed=9, pr_read_pct=20, ro_reads=32, up_reads=4,
                          kind=cg.KIND_TRANSFER, amt_lo=1, amt_hi=10, dist=cg.DIST_ZIPF,
                          zipf_theta=0.99)
-    st, _, _ = run_checked(w, ctas=0, client_warps=15)
+    st, _, _ = run_checked(w, ctas=152, client_warps=2, version_depth=8, prevalidate=prevalidate)
     assert st.aborts > 0
 
 
 def test_hotspot_full_gpu_exact():
     w = cg.bank_workload(1 << 20, 1 << 18, seed=4, pr_read_pct=10, ro_reads=8, up_reads=4,
                          dist=cg.DIST_HOTSPOT, hot_frac=0.01, hot_prob=0.9, shift_every=1 << 16)
-    run_checked(w, ctas=0, client_warps=15)
+    run_checked(w, ctas=0, client_warps=15, prevalidate=2)
 
 
 def test_runs_continue_the_commit_order():

@@ -236,7 +236,7 @@ def test_check_rejects_planted_mistakes():
 
 
 @pytest.mark.parametrize("locks", [True, False])
-@pytest.mark.parametrize("prevalidate", [True, False])
+@pytest.mark.parametrize("prevalidate", [1, 0, 2])
 def test_one_warp_model_is_exact(prevalidate, locks):
     w = small_workload(n_txn=32 * 64, n_accounts=40)
     op, off, addr = orc.generate(w)
@@ -244,7 +244,11 @@ def test_one_warp_model_is_exact(prevalidate, locks):
     slots, log, outcome, result, st = orc.sim_1warp(op, off, addr, 40, init, 4, prevalidate, locks)
     assert st.commits_update + st.commits_readonly + st.commits_nowrite == len(op)
     assert orc.check(op, off, addr, 40, init, 4, st.final_ts, log, outcome, result, slots) is None
-    assert (st.aborts_prevalid if prevalidate else st.aborts_read_write) > 0
+    if prevalidate == 2:  # the chain commits every transaction on its first attempt
+        assert st.aborts_prevalid + st.aborts_read_write + st.aborts_write_write == 0
+        assert st.rounds == len(op) // 32
+    else:
+        assert (st.aborts_prevalid if prevalidate else st.aborts_read_write) > 0
 
 
 def test_cpu_baselines_agree_on_commutative_stream():
