@@ -284,7 +284,7 @@ static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* of
     out->kernel_ms = ms;
   }
   if (gs.error) {
-    set_error("device error %u (1 turn, 2 clock, 3 reply, 4 request, 5 capacity, 6 data)",
+    set_error("device error %u (1 turn, 2 clock, 3 reply, 4 request, 5 capacity, 6 data, 7 livelock)",
               gs.error);
     return gs.error == ERR_DATA ? CSMV_ERR_INVALID_ARG : CSMV_ERR_TIMEOUT;
   }

@@ -287,28 +287,26 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
     }
 
     uint32_t pending = 0xFFFFFFFFu;
-    uint32_t need = 0;  // stamp protocol: a newer commit this lane must see before retrying
+    uint32_t attempts = 0, lock_fails = 0;
     while (pending) {
       if (lane == 0) atomicAdd(&sm.stat[ST_ROUNDS], 1ull);
+      if (lock_fails) {  // randomized, growing back-off after a lost lock: breaks lock-step retries
+        const uint32_t h = (me * 0x9E3779B1u) ^ (attempts * 0x85EBCA6Bu);
+        __nanosleep((h >> 16) & ((64u << lock_fails) - 1u));
+      }
+      if (++attempts > (1u << 20)) {  // no round may retry forever: report and leave
+        if (lane == 0) raise_error(&p.gs->error, ERR_LIVELOCK);
+        failed = true;
+        break;
+      }
       const bool mine = (pending >> lane) & 1u;
       ReadSet<MAXR> rs;
       WriteSet<MAXW> ws;
-      // a retry after reading a stamp newer than its snapshot first lets the clock catch up
-      // with that commit (bounded; the reference's TXBegin waits for prevTs the same way,
-      // bank/csmv_sh/API.cu:283), instead of re-failing the same check
-      const uint32_t want = __reduce_max_sync(0xFFFFFFFFu, mine ? need : 0u);
       uint32_t snap = 0;
-      if (lane == 0) {
-        snap = TXBegin(&p.gs->clock, rs, ws);
-        for (uint32_t it = 0; snap < want && it < 4096; it++) {
-          __nanosleep(64);
-          snap = ld_acquire_gpu(&p.gs->clock);
-        }
-      }
+      if (lane == 0) snap = TXBegin(&p.gs->clock, rs, ws);
       rs.n = 0;
       ws.n = 0;
       snap = __shfl_sync(0xFFFFFFFFu, snap, 0);
-      need = 0;
       bool aborted = false;
 
       if (ro) {  // read-only: consistent snapshot read, commits without validation
@@ -337,9 +335,9 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
         continue;
       }
 
-      // transfer: read everything at the snapshot; in the stamp protocol each item's commit
-      // word is loaded alongside its versions, so a read already overwritten by a later commit
-      // aborts here instead of reaching the commit step
+      // transfer reads. Ring protocol: the reference's rule, everything at the snapshot. Stamp
+      // protocol: each item's latest committed version, with its stamp kept for validation (a
+      // snapshot read would go stale whenever the clock trails a hot item's commits)
       int32_t v[MAXR];
       uint32_t stv[MAXR];
 #pragma unroll
@@ -347,17 +345,30 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
         v[k] = 0;
         stv[k] = 0;
         if (mine && k < (int)nr) {
-          v[k] = TXRead<DEPTH>(vs, a[k], snap, rs, ws, &aborted);
-          if (stamp) stv[k] = (uint32_t)ld_relaxed_gpu(&p.cw[a[k]]);
+          if (stamp)
+            v[k] = TXReadLatest<DEPTH>(vs, p.cw, a[k], rs, stv[k], &aborted);
+          else
+            v[k] = TXRead<DEPTH>(vs, a[k], snap, rs, ws, &aborted);
         }
       }
-      bool stale = false;
+      const bool stale = false;
+      // a transfer that commits no writes is read-only: in the stamp protocol it serialises at
+      // the largest stamp it read, once a second collect finds every stamp unchanged and no
+      // lock on them (a writer of one of them with a smaller timestamp would hold its lock)
+      uint32_t ro_snap = snap;
+      auto recheck = [&](bool active) {
+        bool ok = active;
+        uint32_t mx = 0;
 #pragma unroll
-      for (int k = 0; k < MAXR; k++) {
-        stale |= stv[k] > snap;
-        need = max(need, stv[k]);
-      }
-      stale = stale && !aborted;
+        for (int k = 0; k < MAXR; k++) {
+          if (!active || k >= (int)nr) continue;
+          const unsigned long long wd = ld_relaxed_gpu(&p.cw[a[k]]);
+          ok &= (uint32_t)wd == stv[k] && (uint32_t)(wd >> 32) == 0u;
+          mx = max(mx, stv[k]);
+        }
+        ro_snap = mx;
+        return ok;
+      };
 
       // ---- stamp protocol with intra-warp chaining (prevalidate == 2): instead of aborting a
       // lane that read what a lower lane writes (TXPreValidation), the warp runs its transfers as
@@ -404,7 +415,9 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
         int32_t w0, w1;
         const bool has_w = okr && transfer_writes<MAXR>(op, nr, v, w0, w1);
         const bool part = okr && (has_w || fwd != 0);      // a link of the chain: needs a timestamp
-        const bool snap_ok = okr && !has_w && fwd == 0;    // read-only outcome at the snapshot
+        const bool ro_cand = okr && !has_w && fwd == 0;    // read-only outcome
+        const bool snap_ok = recheck(ro_cand);
+        const bool ro_fail = ro_cand && !snap_ok;
         // lock leaders: the lowest lane writing each address takes its lock
         uint32_t lead_lane[2] = {lane, lane}, lead_slot[2] = {0u, 1u};
         bool found[2] = {false, false};
@@ -438,9 +451,9 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
         const uint32_t lockf = __ballot_sync(0xFFFFFFFFu, part && !lock_ok);
         const uint32_t snapm = __ballot_sync(0xFFFFFFFFu, snap_ok);
         const uint32_t agm = __ballot_sync(0xFFFFFFFFu, mine && aborted);
-        const uint32_t stm = __ballot_sync(0xFFFFFFFFu, mine && stale);
+        const uint32_t stm = __ballot_sync(0xFFFFFFFFu, ro_fail);
         if (snap_ok && p.log) {
-          p.outcome[t] = snap | kSnapFlag;
+          p.outcome[t] = ro_snap | kSnapFlag;
           p.result[t] = 0;
         }
         if (lane == 0) {
@@ -450,6 +463,7 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
           stat_add(sm.stat, ST_ABORT_WRITE_WRITE, __popc(lockf));
           stat_add(sm.stat, ST_ABORT_PREVALID, __popc(F & ~lockf));
         }
+        lock_fails = lockf ? min(lock_fails + 1, 6u) : 0u;
         const uint32_t cand = partm & ~F;
         const bool cand_me = (cand >> lane) & 1u;
         uint32_t C = 0, base = 0, my_ts = 0;
@@ -498,9 +512,7 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
                 __nanosleep(32);
                 wd = ld_relaxed_gpu(&p.cw[a[k]]);
               }
-              const uint32_t st = (uint32_t)wd;
-              valid = settled && st <= snap;
-              need = max(need, st);
+              valid = settled && (uint32_t)wd == stv[k];
             }
           }
           uint32_t F2 = 0;
@@ -584,14 +596,20 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
           has_w = true;
         }
       }
-      const bool nowrite = mine && !aborted && !stale && !has_w;
+      bool nowrite = mine && !aborted && !stale && !has_w;
+      bool ro_fail = false;
+      if (stamp) {
+        const bool ok = recheck(nowrite);
+        ro_fail = nowrite && !ok;
+        nowrite = nowrite && ok;
+      }
       if (nowrite && p.log) {
-        p.outcome[t] = snap | kSnapFlag;
+        p.outcome[t] = ro_snap | kSnapFlag;
         p.result[t] = 0;
       }
       const uint32_t nwm = __ballot_sync(0xFFFFFFFFu, nowrite);
       const uint32_t agm = __ballot_sync(0xFFFFFFFFu, mine && aborted);
-      const uint32_t stm = __ballot_sync(0xFFFFFFFFu, mine && stale);
+      const uint32_t stm = __ballot_sync(0xFFFFFFFFu, ro_fail);
       uint32_t cand = __ballot_sync(0xFFFFFFFFu, has_w);
       if (lane == 0) {
         stat_add(sm.stat, ST_COMMIT_NOWRITE, __popc(nwm));
@@ -609,17 +627,23 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
         // (warp-collective: every lane calls it, candidate or not)
         const uint32_t overlap = TXWriteOverlap(ws, cand_me);
         const bool attempt = cand_me && (overlap & cand) == 0;
-        bool got[MAXW];
-        bool all = attempt;
-#pragma unroll
-        for (int k = 0; k < MAXW; k++) {
-          got[k] = false;
-          if (attempt && k < (int)ws.n) {
-            got[k] = atomicCAS(owner_word(p.cw, ws.addr[k]), 0u, me) == 0u;
-            all &= got[k];
-          }
+        // locks in address order, no waiting: the higher one is tried only once the lower one is
+        // held, so two warps never each hold one of the other's pair (that lock-step was a
+        // livelock); a lost lock releases what was taken and backs off
+        static_assert(MAXW == 2, "ordered acquisition below is written for two write items");
+        const uint32_t lo_a = ws.n > 1 ? min(ws.addr[0], ws.addr[1]) : ws.addr[0];
+        const uint32_t hi_a = ws.n > 1 ? max(ws.addr[0], ws.addr[1]) : ws.addr[0];
+        bool got_lo = false, got_hi = ws.n < 2;
+        if (attempt) {
+          got_lo = atomicCAS(owner_word(p.cw, lo_a), 0u, me) == 0u;
+          if (got_lo && !got_hi) got_hi = atomicCAS(owner_word(p.cw, hi_a), 0u, me) == 0u;
+          if (got_lo && !got_hi) st_relaxed_gpu(owner_word(p.cw, lo_a), 0u);
         }
-        const uint32_t locked = __ballot_sync(0xFFFFFFFFu, attempt && all);
+        const bool all = attempt && got_lo && got_hi;
+        bool got[MAXW];
+#pragma unroll
+        for (int k = 0; k < MAXW; k++) got[k] = all && k < (int)ws.n;
+        const uint32_t locked = __ballot_sync(0xFFFFFFFFu, all);
         // intra-warp resolution: always needed here, since a lane must not commit after a lower
         // lane of its own warp wrote what it read (their locks have the same owner)
         const uint32_t pass = TXPreValidation(rs, ws, (locked >> lane) & 1u);
@@ -633,6 +657,8 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
           stat_add(sm.stat, p.prevalidate ? ST_ABORT_PREVALID : ST_ABORT_READ_WRITE,
                    __popc(locked & ~pass));
         }
+        // back off only when a lock was lost to another warp (not for own-warp overlaps)
+        lock_fails = __ballot_sync(0xFFFFFFFFu, attempt && !all) ? min(lock_fails + 1, 6u) : 0u;
         cand = pass;
         cand_me = (cand >> lane) & 1u;
         if (cand == 0) continue;
@@ -709,9 +735,7 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
               __nanosleep(32);
               wd = ld_relaxed_gpu(&p.cw[rs.addr[k]]);
             }
-            const uint32_t st = (uint32_t)wd;
-            valid = settled && st <= snap;
-            need = max(need, st);
+            valid = settled && (uint32_t)wd == stv[k];
           }
         }
         okm = __ballot_sync(0xFFFFFFFFu, valid);
@@ -807,22 +831,15 @@ template <int MAXR, int MAXW>
 __device__ void server_warp_stamp(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
   const uint32_t lane = lane_id();
   uint32_t seen = 0;
-  uint64_t idle = 0;
-  const uint64_t idle_limit = 1ull << (p.spin_log2 + 2);
   for (;;) {
     uint32_t req;
     bool stop;
     uint32_t ready = poll_mailboxes(p, sm, seen, &req, &stop);
     if (ready == 0) {
       if (stop) break;
-      if (++idle > idle_limit) {
-        if (lane == 0) raise_error(&p.gs->error, ERR_WAIT_REQUEST);
-        break;
-      }
-      __nanosleep(32);
+      __nanosleep(64);
       continue;
     }
-    idle = 0;
     if (p.batch != CSMV_BATCH_CTA) ready &= (0u - ready);  // one warp per assignment
     const bool mine = lane < p.nc && ((ready >> lane) & 1u);
     uint32_t cnt = 0;
@@ -967,8 +984,6 @@ __device__ void server_warp_ring(const BankParams& p, CtaShared<MAXR, MAXW>& sm)
   const uint32_t nc = p.nc;
   uint32_t seen = 0;
   uint32_t* snaps = sm.snaps;
-  uint64_t idle = 0;
-  const uint64_t idle_limit = 1ull << (p.spin_log2 + 2);
   const VersionStore vs{p.slots, p.n_items};
 
   for (;;) {
@@ -977,14 +992,9 @@ __device__ void server_warp_ring(const BankParams& p, CtaShared<MAXR, MAXW>& sm)
     uint32_t ready = poll_mailboxes(p, sm, seen, &req, &stop);
     if (ready == 0) {
       if (stop) break;
-      if (++idle > idle_limit) {
-        if (lane == 0) raise_error(&p.gs->error, ERR_WAIT_REQUEST);
-        break;
-      }
       __nanosleep(64);
       continue;
     }
-    idle = 0;
     if (p.batch != CSMV_BATCH_CTA) ready &= (0u - ready);  // lowest ready warp only
     {  // the batch read hash must fit: cap the batch
       uint32_t capped = 0, entries = 0;

@@ -87,7 +87,8 @@ enum : uint32_t {
   ERR_WAIT_REPLY = 3,    // a client warp's request got no reply
   ERR_WAIT_REQUEST = 4,  // the server saw no progress from its clients
   ERR_CAPACITY = 5,      // read/write set or batch capacity exceeded
-  ERR_DATA = 6           // malformed transaction (bad size / address)
+  ERR_DATA = 6,          // malformed transaction (bad size / address)
+  ERR_LIVELOCK = 7       // a round exhausted its attempt budget without committing
 };
 
 __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t code) {

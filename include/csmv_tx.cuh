@@ -128,6 +128,47 @@ __device__ __forceinline__ int32_t TXRead(const VersionStore& vs, uint32_t addr,
   return v;
 }
 
+// Read of the latest committed version in the stamp protocol: an item's commit word holds the
+// timestamp of its last committed writer (published only after that writer's version is in
+// the list), and the read returns that version. The stamp joins the read set; commit-time
+// validation then only checks that it has not moved. When the version of the stamp is not yet
+// visible (the word and the slots were fetched concurrently), the word is fetched again with
+// acquire semantics and the slots after it.
+template <int DEPTH>
+__device__ __forceinline__ bool read_stamped(const unsigned long long* item, uint32_t stamp,
+                                             int32_t& out) {
+  unsigned long long s[DEPTH];
+#pragma unroll
+  for (int d = 0; d < DEPTH; d += 2) ld_relaxed_gpu_v2(item + d, s[d], s[d + 1]);
+  bool found = false;
+#pragma unroll
+  for (int d = 0; d < DEPTH; d++)
+    if (version_ts(s[d]) == stamp) {
+      out = version_val(s[d]);
+      found = true;
+    }
+  return found;
+}
+
+template <int DEPTH, int MAXR>
+__device__ __forceinline__ int32_t TXReadLatest(const VersionStore& vs,
+                                                const unsigned long long* commit_words,
+                                                uint32_t addr, ReadSet<MAXR>& rs,
+                                                uint32_t& stamp, bool* isAborted) {
+  const unsigned long long* item = vs.slots + (size_t)addr * DEPTH;
+  int32_t v = 0;
+  stamp = (uint32_t)ld_relaxed_gpu(commit_words + addr);
+  if (!read_stamped<DEPTH>(item, stamp, v)) {
+    stamp = (uint32_t)ld_acquire_gpu(commit_words + addr);
+    if (!read_stamped<DEPTH>(item, stamp, v)) *isAborted = true;
+  }
+#pragma unroll
+  for (int i = 0; i < MAXR; i++)
+    if (i == (int)rs.n) rs.addr[i] = addr;
+  if (rs.n < (uint32_t)MAXR) rs.n++;
+  return v;
+}
+
 // TXReadOnly (bank/csmv_sh/API.cu:43-67): the version rule without read-set logging.
 template <int DEPTH>
 __device__ __forceinline__ int32_t TXReadOnly(const VersionStore& vs, uint32_t addr, uint32_t ts,

@@ -568,6 +568,29 @@ out:
   return rc;
 }
 
+static uint32_t newest_ts(const uint64_t* slots, int depth) {
+  uint32_t m = 0;
+  for (int d = 0; d < depth; d++) {
+    uint32_t t = (uint32_t)(slots[d] >> 32);
+    if (t != 0xFFFFFFFFu && t > m) m = t;
+  }
+  return m;
+}
+
+/* Read-only outcome of a transfer that wrote nothing: the ring protocol serialises it at its
+ * snapshot, the stamp protocol (it reads latest versions) at the newest stamp it read. */
+static uint32_t nowrite_snap(uint32_t t, const uint32_t* op, const uint32_t* off,
+                             const uint32_t* addr, const uint64_t* slots, int depth, int locks,
+                             uint32_t snap) {
+  if (!locks || (op[t] & 3u) == 0) return snap;
+  uint32_t m = 0, nr = (op[t] >> 2) & 63u;
+  for (uint32_t k = 0; k < nr; k++) {
+    uint32_t x = newest_ts(slots + (uint64_t)addr[off[t] + k] * depth, depth);
+    if (x > m) m = x;
+  }
+  return m;
+}
+
 /* Deterministic model of the engine with one client warp: rounds run in order; every
  * attempt snapshots the current clock, executes, drops no-write transfers as snapshot
  * commits, pre-validates (or lets the server resolve lane order), and commits the surviving
@@ -626,7 +649,7 @@ int orc_bank_sim_1warp(uint32_t n_txn, const uint32_t* op, const uint32_t* off,
           if (nw > 0 || fwd) {
             links |= 1u << l;
           } else {
-            outcome[t] = snap | SNAP_FLAG;
+            outcome[t] = nowrite_snap(t, op, off, addr, slots, depth, locks, snap) | SNAP_FLAG;
             result[t] = r;
             if ((op[t] & 3u) == 0)
               st->commits_readonly++;
@@ -665,7 +688,7 @@ int orc_bank_sim_1warp(uint32_t n_txn, const uint32_t* op, const uint32_t* off,
         nrs[l] = nr;
         int nw = orc_bank_exec(op[t], addr + off[t], v, ws[l], wv[l], &r);
         if (nw == 0) {
-          outcome[t] = snap | SNAP_FLAG;
+          outcome[t] = nowrite_snap(t, op, off, addr, slots, depth, locks, snap) | SNAP_FLAG;
           result[t] = r;
           if ((op[t] & 3u) == 0)
             st->commits_readonly++;

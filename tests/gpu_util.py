@@ -30,7 +30,8 @@ def run_checked(w, *, init_value=1000, check=True, **cfg):
     if cfg.get("validate", cg.VALIDATE_STAMP) == cg.VALIDATE_STAMP:
         # timestamps of transactions that failed validation after taking one are holes
         assert st.commits_update <= st.final_ts
-        assert np.count_nonzero(log_txn != 0xFFFFFFFF) == st.commits_update
+        logged = np.count_nonzero(log_txn != 0xFFFFFFFF)  # chained links may commit no writes
+        assert st.commits_update <= logged <= st.commits_update + st.commits_nowrite
     else:
         assert st.commits_update == st.final_ts  # the reference's dense commit order
     if check:
