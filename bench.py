@@ -51,8 +51,9 @@ def parse():
     ap.add_argument("--impl", default="csmv", choices=["csmv", "reference"])
     ap.add_argument("--n-txn", type=int, default=N_TXN)
     ap.add_argument("--dist", default="zipf", choices=["zipf", "uniform", "hotspot"])
-    ap.add_argument("--client-warps", type=int, default=int(os.environ.get("CSMV_CLIENT_WARPS", 15)))
-    ap.add_argument("--ctas", type=int, default=int(os.environ.get("CSMV_CTAS", 0)))
+    ap.add_argument("--client-warps", type=int, default=int(os.environ.get("CSMV_CLIENT_WARPS", 2)))
+    ap.add_argument("--ctas", type=int, default=int(os.environ.get("CSMV_CTAS", 152)))
+    ap.add_argument("--depth", type=int, default=int(os.environ.get("CSMV_DEPTH", 8)))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -209,7 +210,7 @@ def main():
     h2d = (s.op.nbytes + s.off.nbytes + s.addr.nbytes)
     dev = [torch.from_numpy(np.asarray(a).view(np.int32).copy()).cuda() for a in (s.op, s.off, s.addr)]
     ds = cg.BankStream(n, dev[0].data_ptr(), dev[1].data_ptr(), dev[2].data_ptr(), s.addr.shape[0])
-    bank = cg.Bank(n_accounts=N_ACCOUNTS, version_depth=4, client_warps=args.client_warps,
+    bank = cg.Bank(n_accounts=N_ACCOUNTS, version_depth=args.depth, client_warps=args.client_warps,
                    ctas=args.ctas, max_txn=n, log_commits=0, device=local)
     bank.load()
     for _ in range(args.warmup):
@@ -258,7 +259,7 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic",
         "config": {"workload": f"bank {args.dist}(0.99), 2^20 int32 accounts, transfers r4/w2, "
-                               f"20% read-only scans of 32, {n} txn/step, depth 4",
+                               f"20% read-only scans of 32, {n} txn/step, depth {args.depth}",
                    "l2": "inputs larger than L2 (stream ~%d MB)" % (h2d >> 20),
                    "ctas": info["ctas"], "threads_per_cta": info["threads_per_cta"],
                    "parallelism": f"replicas x{world}"},

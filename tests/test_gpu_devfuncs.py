@@ -35,7 +35,7 @@ def random_histories(rng, n, depth):
     ts_all, val_all = [], []
     slots = np.tile(np.full(depth, np.uint64(0xFFFFFFFF) << np.uint64(32), np.uint64), n)
     for i in range(n):
-        slots[i * depth] = np.uint64(np.uint32(int(rng.integers(-1000, 1000))))
+        slots[i * depth] = np.uint64(int(rng.integers(-1000, 1000)) & 0xFFFFFFFF)
         ts = 0
         for _ in range(int(rng.integers(0, 3 * depth))):
             ts += int(rng.integers(1, 4))
