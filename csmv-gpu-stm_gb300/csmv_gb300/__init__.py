@@ -2,8 +2,8 @@
 
 Mirrors the reference's host interface for the commit path: ``Bank`` stands in for the
 TXInit / parent_kernel / TXEnd sequence of bank/csmv_sh/exe.cu:340-529 (create + load, run,
-read back), with statistics named after the reference's Statistics struct
-(bank/csmv_sh/API.cuh:112-119). There is no CPU fallback: every call goes through
+read back), ``Memcd`` for the cache set-up and batch loop of memcachedGPU/memcdSH.cu:557-651,
+with statistics named after the reference's Statistics struct (bank/csmv_sh/API.cuh:112-119). There is no CPU fallback: every call goes through
 ``lib/libcsmv.so`` and raises when the library is missing or a call fails.
 """
 from __future__ import annotations
@@ -27,6 +27,9 @@ VALIDATE_STAMP, VALIDATE_RING, VALIDATE_RING_LANE = 0, 1, 2
 WRITEBACK_CLIENT, WRITEBACK_SERVER = 0, 1
 BATCH_LANE, BATCH_WARP, BATCH_CTA, BATCH_CLUSTER = 0, 1, 2, 3
 SNAP_FLAG = 0x80000000
+MEMCD_GET, MEMCD_SET = 0, 1
+MEMCD_WAYS, MEMCD_DEPTH, KEY_WORDS, VAL_WORDS = 8, 2, 4, 8
+HOLE = 0xFFFFFFFF
 
 
 class CsmvError(RuntimeError):
@@ -83,6 +86,23 @@ class Stats(C.Structure):
         return self.aborts / tot if tot else 0.0
 
 
+class MemcdWorkload(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("n_keys", C.c_uint32), ("n_req", C.c_uint32),
+                ("get_pct", C.c_uint32), ("dist", C.c_uint32), ("zipf_theta", C.c_double)]
+
+
+class MemcdBatch(C.Structure):
+    _fields_ = [("n_req", C.c_uint32), ("tick", C.c_uint32), ("kind", C.c_void_p),
+                ("key", C.c_void_p), ("val", C.c_void_p), ("found", C.c_void_p),
+                ("val_out", C.c_void_p)]
+
+
+class MemcdConfig(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in (
+        "n_sets", "n_ways", "version_depth", "client_warps", "ctas", "batch", "log_commits",
+        "max_req", "spin_limit_log2")] + [("device", C.c_int32)]
+
+
 _lib = None
 
 
@@ -110,6 +130,17 @@ def lib() -> C.CDLL:
         "csmv_bank_device_info": (I32, [P, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                         C.POINTER(C.c_int), C.POINTER(C.c_size_t)]),
         "csmv_bank_destroy": (None, [P]),
+        "csmv_memcd_generate": (I32, [C.POINTER(MemcdWorkload), P, P, P]),
+        "csmv_memcd_config_default": (None, [C.POINTER(MemcdConfig)]),
+        "csmv_memcd_create": (I32, [C.POINTER(MemcdConfig), C.POINTER(P)]),
+        "csmv_memcd_clear": (I32, [P]),
+        "csmv_memcd_run": (I32, [P, C.POINTER(MemcdBatch), C.POINTER(Stats)]),
+        "csmv_memcd_run_device": (I32, [P, C.POINTER(MemcdBatch), C.POINTER(Stats)]),
+        "csmv_memcd_read_table": (I32, [P, P, P]),
+        "csmv_memcd_read_log": (I32, [P, P, U32, P, U32, C.POINTER(C.c_uint32)]),
+        "csmv_memcd_device_info": (I32, [P, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                         C.POINTER(C.c_int), C.POINTER(C.c_size_t)]),
+        "csmv_memcd_destroy": (None, [P]),
         "csmv_pinned_alloc": (I32, [C.c_size_t, C.POINTER(P)]),
         "csmv_pinned_free": (None, [P]),
         "csmv_last_error": (C.c_char_p, []),
@@ -285,6 +316,141 @@ class Bank:
         a, b, c_, d = C.c_int(), C.c_int(), C.c_int(), C.c_size_t()
         _check(lib().csmv_bank_device_info(self._h, C.byref(a), C.byref(b), C.byref(c_),
                                            C.byref(d)), "csmv_bank_device_info")
+        return {"n_sms": a.value, "ctas": b.value, "threads_per_cta": c_.value,
+                "device_bytes": d.value}
+
+
+# ---------------------------------------------------------------------------------------------
+# transactional cache
+# ---------------------------------------------------------------------------------------------
+
+def memcd_workload(n_keys: int, n_req: int, *, seed: int = 1, get_pct: int = 99,
+                   dist: int = DIST_ZIPF, zipf_theta: float = 0.99) -> MemcdWorkload:
+    return MemcdWorkload(seed, n_keys, n_req, get_pct, dist, zipf_theta)
+
+
+@dataclass
+class Requests:
+    kind: np.ndarray   # [n] uint32
+    key: np.ndarray    # [n, 4] uint32
+    val: np.ndarray    # [n, 8] uint32
+
+    @property
+    def n_req(self) -> int:
+        return int(self.kind.shape[0])
+
+
+def memcd_generate(w: MemcdWorkload, pinned: bool = False) -> Requests:
+    """Host generator of the library (csmv_memcd_generate)."""
+    n = w.n_req
+    if pinned:
+        holders = [PinnedArray(n), PinnedArray(4 * n), PinnedArray(8 * n)]
+        kind, key, val = (h.array for h in holders)
+    else:
+        holders = []
+        kind, key, val = (np.empty(n, np.uint32), np.empty(4 * n, np.uint32),
+                          np.empty(8 * n, np.uint32))
+    _check(lib().csmv_memcd_generate(C.byref(w), _ptr(kind), _ptr(key), _ptr(val)),
+           "csmv_memcd_generate")
+    r = Requests(kind, key.reshape(n, 4), val.reshape(n, 8))
+    r._holders = holders
+    return r
+
+
+def memcd_config(**kw) -> MemcdConfig:
+    cfg = MemcdConfig()
+    lib().csmv_memcd_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        if not hasattr(cfg, k):
+            raise KeyError(f"unknown memcd config field {k}")
+        setattr(cfg, k, v)
+    return cfg
+
+
+class Memcd:
+    """One transactional cache on one GPU. ``run`` is one iteration of the reference's batch
+    loop; the LRU tick starts at 1 and advances after every batch (memcdSH.cu:573,648)."""
+
+    def __init__(self, cfg: MemcdConfig | None = None, **kw):
+        self.cfg = cfg if cfg is not None else memcd_config(**kw)
+        h = C.c_void_p()
+        _check(lib().csmv_memcd_create(C.byref(self.cfg), C.byref(h)), "csmv_memcd_create")
+        self._h = h
+        self.tick = 1
+        self.last_stats: Stats | None = None
+        self.clear()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            lib().csmv_memcd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def clear(self) -> None:
+        _check(lib().csmv_memcd_clear(self._h), "csmv_memcd_clear")
+        self.tick = 1
+
+    def run(self, req: Requests, found: np.ndarray | None = None,
+            val_out: np.ndarray | None = None, tick: int | None = None):
+        """Host buffers in and out; returns (found, val_out, stats)."""
+        n = req.n_req
+        found = np.empty(n, np.uint32) if found is None else found
+        val_out = np.empty((n, 8), np.uint32) if val_out is None else val_out
+        t = self.tick if tick is None else tick
+        b = MemcdBatch(n, t, _ptr(req.kind), _ptr(req.key), _ptr(req.val), _ptr(found),
+                       _ptr(val_out))
+        st = Stats()
+        rc = lib().csmv_memcd_run(self._h, C.byref(b), C.byref(st))
+        self.last_stats = st
+        _check(rc, "csmv_memcd_run")
+        if tick is None:
+            self.tick += 1
+        return found, val_out, st
+
+    def run_device(self, batch: MemcdBatch) -> Stats:
+        st = Stats()
+        rc = lib().csmv_memcd_run_device(self._h, C.byref(batch), C.byref(st))
+        self.last_stats = st
+        _check(rc, "csmv_memcd_run_device")
+        return st
+
+    def table(self):
+        """(tags [n_sets*16] uint64, recs [n_sets*16, 16] uint32)."""
+        nv = self.cfg.n_sets * MEMCD_WAYS * MEMCD_DEPTH
+        tags = np.empty(nv, np.uint64)
+        recs = np.empty((nv, 16), np.uint32)
+        _check(lib().csmv_memcd_read_table(self._h, _ptr(tags), _ptr(recs)),
+               "csmv_memcd_read_table")
+        return tags, recs
+
+    def log(self, n_req: int):
+        """(log_txn, outcome[n_req], base_ts) of the last run: log_txn[k] is the request that
+        committed with timestamp base_ts + k + 1 (HOLE for a failed validation)."""
+        base = C.c_uint32()
+        _check(lib().csmv_memcd_read_log(self._h, None, 0, None, 0, C.byref(base)),
+               "csmv_memcd_read_log")
+        n_log = self.last_stats.final_ts - base.value
+        log_txn = np.empty(max(1, n_log), np.uint32)
+        outcome = np.empty(max(1, n_req), np.uint32)
+        _check(lib().csmv_memcd_read_log(self._h, _ptr(log_txn), max(1, n_log), _ptr(outcome),
+                                         n_req, C.byref(base)), "csmv_memcd_read_log")
+        return log_txn[:n_log], outcome[:n_req], base.value
+
+    def device_info(self) -> dict:
+        a, b, c_, d = C.c_int(), C.c_int(), C.c_int(), C.c_size_t()
+        _check(lib().csmv_memcd_device_info(self._h, C.byref(a), C.byref(b), C.byref(c_),
+                                            C.byref(d)), "csmv_memcd_device_info")
         return {"n_sms": a.value, "ctas": b.value, "threads_per_cta": c_.value,
                 "device_bytes": d.value}
 

@@ -37,7 +37,7 @@ namespace csmv {
 constexpr uint32_t kSnapFlag = 0x80000000u;
 constexpr uint32_t kHole = 0xFFFFFFFFu;  // log entry of a timestamp whose transaction aborted
 constexpr uint32_t kPendingFlag = 0x80000000u;  // lock word: holder's commit timestamp is known
-constexpr int kMaxClientWarps = 31;
+constexpr int kMaxClientWarps = 15;
 constexpr int kHashSize = 4096;  // shared-memory hash entries (power of two)
 constexpr int kBatchDescs = 32;
 
@@ -197,23 +197,24 @@ struct SlotEditor {
 // Mark timestamps [lo, hi] complete (their write-back is visible), then move the clock over the
 // longest complete prefix. Any warp may advance: a CAS keeps the clock monotonic, and the warp
 // that passes the end of a bitmap word clears it for the next lap. Called by one lane.
-__device__ void complete_range(const BankParams& p, uint32_t lo, uint32_t hi) {
+static __device__ void complete_range(uint32_t* done, uint32_t done_mask, GlobalSync* gs, uint32_t lo,
+                               uint32_t hi) {
   __threadfence();
   for (uint32_t t = lo; t <= hi;) {
     const uint32_t bit = t & 31u, span = min(32u - bit, hi - t + 1);
     const uint32_t m = (span == 32u ? 0xFFFFFFFFu : ((1u << span) - 1u)) << bit;
-    atomicOr(&p.done[(t >> 5) & p.done_mask], m);
+    atomicOr(&done[(t >> 5) & done_mask], m);
     t += span;
   }
   // store-buffering pattern with the warp completing the range below ours: with SC fences on
   // both sides at least one of us sees the other's bits, so the clock never stalls
   __threadfence();
   for (uint32_t attempt = 0; attempt < 4096; attempt++) {
-    const uint32_t c = ld_acquire_gpu(&p.gs->clock);
+    const uint32_t c = ld_acquire_gpu(&gs->clock);
     uint32_t n = c;
     for (uint32_t words = 0; words < 64; words++) {  // bounded scan per attempt
       const uint32_t t = n + 1, bit = t & 31u;
-      const uint32_t w = ld_relaxed_gpu(&p.done[(t >> 5) & p.done_mask]) >> bit;
+      const uint32_t w = ld_relaxed_gpu(&done[(t >> 5) & done_mask]) >> bit;
       const uint32_t ones = (w == 0xFFFFFFFFu) ? 32u : (uint32_t)(__ffs(~w) - 1);
       const uint32_t run = min(ones, 32u - bit);
       n += run;
@@ -221,10 +222,10 @@ __device__ void complete_range(const BankParams& p, uint32_t lo, uint32_t hi) {
     }
     if (n == c) return;  // c+1 not complete yet: its owner will advance past us
     __threadfence();
-    if (atomicCAS(&p.gs->clock, c, n) == c) {
+    if (atomicCAS(&gs->clock, c, n) == c) {
       // clear every word whose last timestamp this advance passed
       for (uint32_t wd = (c + 1) >> 5; wd <= (n >> 5); wd++)
-        if (wd * 32u + 31u <= n) st_relaxed_gpu(&p.done[wd & p.done_mask], 0u);
+        if (wd * 32u + 31u <= n) st_relaxed_gpu(&done[wd & done_mask], 0u);
     }
   }
 }
@@ -562,7 +563,7 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
             }
           }
           __syncwarp();
-          if (lane == 0) complete_range(p, base + 1, base + __popc(cand));
+          if (lane == 0) complete_range(p.done, p.done_mask, p.gs, base + 1, base + __popc(cand));
         } else {
           // no links: leaders release whatever they locked
 #pragma unroll
@@ -765,7 +766,7 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
           }
         }
         __syncwarp();
-        if (lane == 0) complete_range(p, base + 1, base + __popc(cand));
+        if (lane == 0) complete_range(p.done, p.done_mask, p.gs, base + 1, base + __popc(cand));
       } else {
         okm = ms.ok;
         const uint32_t bid = ms.bid;
@@ -802,24 +803,25 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
 // ---------------------------------------------------------------------------------------------
 
 // Polls the mailboxes of the CTA's client warps; returns the ready mask (0 = none), sets
-// *stop when every client finished or an error was raised.
-template <int MAXR, int MAXW>
-__device__ __forceinline__ uint32_t poll_mailboxes(const BankParams& p, CtaShared<MAXR, MAXW>& sm,
+// *stop when every client finished or an error was raised. SM is any CTA layout with
+// mail[w].{req,rep,cand,base} slots and done_warps/stat fields.
+template <class SM>
+__device__ __forceinline__ uint32_t poll_mailboxes(uint32_t nc, GlobalSync* gs, SM& sm,
                                                    uint32_t seen, uint32_t* req, bool* stop) {
   const uint32_t lane = lane_id();
   *req = 0;
-  if (lane < p.nc) *req = ld_acquire_cta(&sm.mail[lane].req);
-  const uint32_t ready = __ballot_sync(0xFFFFFFFFu, lane < p.nc && *req != seen);
+  if (lane < nc) *req = ld_acquire_cta(&sm.mail[lane].req);
+  const uint32_t ready = __ballot_sync(0xFFFFFFFFu, lane < nc && *req != seen);
   *stop = false;
   if (ready == 0) {
     uint32_t done = 0, err = 0;
     if (lane == 0) {
       done = *(volatile uint32_t*)&sm.done_warps;
-      err = ld_relaxed_gpu(&p.gs->error);
+      err = ld_relaxed_gpu(&gs->error);
     }
     done = __shfl_sync(0xFFFFFFFFu, done, 0);
     err = __shfl_sync(0xFFFFFFFFu, err, 0);
-    *stop = (done == p.nc) || err;
+    *stop = (done == nc) || err;
   }
   return ready;
 }
@@ -827,21 +829,21 @@ __device__ __forceinline__ uint32_t poll_mailboxes(const BankParams& p, CtaShare
 // Stamp protocol server: one atomicAdd draws consecutive timestamps for every ready warp
 // (batched commit-timestamp assignment, batchedAtrInsert/csmv_sh/API.cu:331-361, here per CTA
 // batch instead of per warp); warp w gets (base_w, base_w + count_w].
-template <int MAXR, int MAXW>
-__device__ void server_warp_stamp(const BankParams& p, CtaShared<MAXR, MAXW>& sm) {
+template <class SM>
+__device__ void server_warp_stamp(uint32_t nc, uint32_t batch, GlobalSync* gs, SM& sm) {
   const uint32_t lane = lane_id();
   uint32_t seen = 0;
   for (;;) {
     uint32_t req;
     bool stop;
-    uint32_t ready = poll_mailboxes(p, sm, seen, &req, &stop);
+    uint32_t ready = poll_mailboxes(nc, gs, sm, seen, &req, &stop);
     if (ready == 0) {
       if (stop) break;
       __nanosleep(64);
       continue;
     }
-    if (p.batch != CSMV_BATCH_CTA) ready &= (0u - ready);  // one warp per assignment
-    const bool mine = lane < p.nc && ((ready >> lane) & 1u);
+    if (batch != CSMV_BATCH_CTA) ready &= (0u - ready);  // one warp per assignment
+    const bool mine = lane < nc && ((ready >> lane) & 1u);
     uint32_t cnt = 0;
     if (mine) {
       seen = req;
@@ -858,7 +860,7 @@ __device__ void server_warp_stamp(const BankParams& p, CtaShared<MAXR, MAXW>& sm
     uint32_t t0 = 0;
     if (lane == 0) {  // fences on both sides order the draw after the observed locks and
       __threadfence();  // before the validations that follow it
-      t0 = atomicAdd(&p.gs->ts_next, total);
+      t0 = atomicAdd(&gs->ts_next, total);
       __threadfence();
     }
     t0 = __shfl_sync(0xFFFFFFFFu, t0, 0);
@@ -989,7 +991,7 @@ __device__ void server_warp_ring(const BankParams& p, CtaShared<MAXR, MAXW>& sm)
   for (;;) {
     uint32_t req;
     bool stop;
-    uint32_t ready = poll_mailboxes(p, sm, seen, &req, &stop);
+    uint32_t ready = poll_mailboxes(p.nc, p.gs, sm, seen, &req, &stop);
     if (ready == 0) {
       if (stop) break;
       __nanosleep(64);
@@ -1200,7 +1202,7 @@ __device__ void server_warp_ring(const BankParams& p, CtaShared<MAXR, MAXW>& sm)
 }
 
 template <int DEPTH, int MAXR, int MAXW>
-__global__ void __launch_bounds__(1024, 1) bank_kernel(BankParams p) {
+__global__ void __launch_bounds__(512, 1) bank_kernel(BankParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   CtaShared<MAXR, MAXW>& sm = *reinterpret_cast<CtaShared<MAXR, MAXW>*>(smem_raw);
   const uint32_t warp = threadIdx.x >> 5;
@@ -1216,7 +1218,7 @@ __global__ void __launch_bounds__(1024, 1) bank_kernel(BankParams p) {
   __syncthreads();
   if (warp == 0) {
     if (p.validate == CSMV_VALIDATE_STAMP)
-      server_warp_stamp<MAXR, MAXW>(p, sm);
+      server_warp_stamp(p.nc, p.batch, p.gs, sm);
     else
       server_warp_ring<DEPTH, MAXR, MAXW>(p, sm);
   } else {

@@ -1,0 +1,363 @@
+// memcd_engine.cu - C-ABI host side of the transactional cache (include/csmv.h, memcached part).
+//
+// Data layout in HBM (entry = set * 8 + way, allocated once per handle):
+//   tag   entries * 2 * 8 B    version tags: ts << 32 | valid << 31 | 31-bit key hash; the 16
+//                              tags of a set are one 128-byte line
+//   rec   entries * 2 * 64 B   version records {lru, 0, 0, 0 | key[4] | value[8]}
+//   cw    entries * 8 B        commit word: stamp (ts of the last committed SET) and lock owner
+//   done  256 KB               completion bitmap, one bit per commit timestamp
+//   logs  8*max_req*4 + max_req*4 B   log_txn[ts-1] (holes included), outcome[req]
+//   io    max_req * (4 + 16 + 32 + 4 + 32) B   request / response staging for host-buffer runs
+#include <chrono>
+#include <cstring>
+#include <vector>
+
+#include "common.h"
+#include "memcd_kernel.cuh"
+
+using namespace csmv;
+
+namespace {
+constexpr uint32_t kDoneWords = 1u << 16;
+}
+
+struct csmv_memcd_t {
+  csmv_memcd_config cfg{};
+  int n_sms = 0, ctas = 0, threads = 0;
+  size_t device_bytes = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  unsigned long long* tag = nullptr;
+  uint4* rec = nullptr;
+  unsigned long long* cw = nullptr;
+  uint32_t* done = nullptr;
+  GlobalSync* gs = nullptr;
+  uint32_t log_cap = 0;
+  uint32_t* log_txn = nullptr;
+  uint32_t* outcome = nullptr;
+  unsigned long long* stats = nullptr;
+  uint32_t* d_kind = nullptr;
+  uint4* d_key = nullptr;
+  uint4* d_val = nullptr;
+  uint32_t* d_found = nullptr;
+  uint4* d_out = nullptr;
+  bool loaded = false;
+  uint32_t last_final_ts = 0, last_n_req = 0, run_base_ts = 0;
+};
+
+extern "C" void csmv_memcd_config_default(csmv_memcd_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->n_sets = 1u << 20;
+  c->n_ways = kWays;
+  c->version_depth = kMemcdDepth;
+  c->client_warps = 4;
+  c->ctas = 0;
+  c->batch = CSMV_BATCH_CTA;
+  c->log_commits = 1;
+  c->max_req = 1u << 16;
+  c->spin_limit_log2 = 24;
+  c->device = 0;
+}
+
+static csmv_status validate_config(const csmv_memcd_config* c) {
+  auto bad = [](const char* why) {
+    set_error("invalid memcd config: %s", why);
+    return CSMV_ERR_INVALID_ARG;
+  };
+  if (!c) return bad("null");
+  if (c->n_sets < 1 || c->n_sets > (1u << 26)) return bad("n_sets must be 1..2^26");
+  if (c->n_ways != (uint32_t)kWays) return bad("n_ways must be 8");
+  if (c->version_depth != (uint32_t)kMemcdDepth) return bad("version_depth must be 2");
+  if (c->client_warps < 1 || c->client_warps > (uint32_t)kMaxClientWarps) return bad("client_warps");
+  if (c->batch != CSMV_BATCH_WARP && c->batch != CSMV_BATCH_CTA) return bad("batch (warp or cta)");
+  if (c->max_req == 0 || c->max_req % 32) return bad("max_req must be a positive multiple of 32");
+  if (c->spin_limit_log2 < 10 || c->spin_limit_log2 > 30) return bad("spin_limit_log2");
+  return CSMV_OK;
+}
+
+static void free_all(csmv_memcd_t* h) {
+  cudaFree(h->tag);
+  cudaFree(h->rec);
+  cudaFree(h->cw);
+  cudaFree(h->done);
+  cudaFree(h->gs);
+  cudaFree(h->log_txn);
+  cudaFree(h->outcome);
+  cudaFree(h->stats);
+  cudaFree(h->d_kind);
+  cudaFree(h->d_key);
+  cudaFree(h->d_val);
+  cudaFree(h->d_found);
+  cudaFree(h->d_out);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+extern "C" csmv_status csmv_memcd_create(const csmv_memcd_config* cfg, csmv_memcd_t** out) {
+  if (!out) return CSMV_ERR_INVALID_ARG;
+  *out = nullptr;
+  csmv_status st = validate_config(cfg);
+  if (st != CSMV_OK) return st;
+  int n_sms = 0;
+  if ((st = check_device(cfg->device, &n_sms)) != CSMV_OK) return st;
+  CSMV_CUDA(cudaSetDevice(cfg->device));
+  int coop = 0;
+  CSMV_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, cfg->device));
+  if (!coop) {
+    set_error("device does not support cooperative launch");
+    return CSMV_ERR_NO_DEVICE;
+  }
+  csmv_memcd_t* h = new csmv_memcd_t;
+  h->cfg = *cfg;
+  h->n_sms = n_sms;
+  h->threads = (int)(cfg->client_warps + 1) * 32;
+  auto fail = [&](csmv_status s) {
+    free_all(h);
+    delete h;
+    return s;
+  };
+  int per_sm = 0;
+  if ((st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, memcd_kernel,
+                                                                       h->threads, 0),
+                        "occupancy")) != CSMV_OK)
+    return fail(st);
+  const int max_ctas = per_sm * n_sms;
+  if (max_ctas <= 0) {
+    set_error("kernel does not fit on an SM (threads %d)", h->threads);
+    return fail(CSMV_ERR_INVALID_ARG);
+  }
+  h->ctas = cfg->ctas ? (int)cfg->ctas : max_ctas;
+  if (h->ctas > max_ctas) {
+    set_error("%d CTAs requested, only %d can be co-resident", h->ctas, max_ctas);
+    return fail(CSMV_ERR_INVALID_ARG);
+  }
+  const size_t ent = (size_t)cfg->n_sets * kWays, D = kMemcdDepth, R = cfg->max_req;
+  h->log_cap = cfg->log_commits ? (cfg->max_req > 0x1FFFFFFFu ? 0xFFFFFFFFu : cfg->max_req * 8u) : 1u;
+  struct {
+    void** p;
+    size_t bytes;
+  } allocs[] = {
+      {(void**)&h->tag, ent * D * 8},        {(void**)&h->rec, ent * D * 64},
+      {(void**)&h->cw, ent * 8},             {(void**)&h->gs, sizeof(GlobalSync)},
+      {(void**)&h->done, (size_t)kDoneWords * 4},
+      {(void**)&h->log_txn, (size_t)h->log_cap * 4}, {(void**)&h->outcome, R * 4},
+      {(void**)&h->stats, ST_COUNT * 8},     {(void**)&h->d_kind, R * 4},
+      {(void**)&h->d_key, R * 16},           {(void**)&h->d_val, R * 32},
+      {(void**)&h->d_found, R * 4},          {(void**)&h->d_out, R * 32},
+  };
+  for (auto& a : allocs) {
+    if ((st = cuda_status(cudaMalloc(a.p, a.bytes), "cudaMalloc")) != CSMV_OK) return fail(st);
+    h->device_bytes += a.bytes;
+  }
+  if ((st = cuda_status(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream")) != CSMV_OK ||
+      (st = cuda_status(cudaEventCreate(&h->ev0), "event")) != CSMV_OK ||
+      (st = cuda_status(cudaEventCreate(&h->ev1), "event")) != CSMV_OK)
+    return fail(st);
+  *out = h;
+  return CSMV_OK;
+}
+
+// Initial table: every entry holds one invalid version with ts 0 (the reference's state array
+// zeroed with head_ptr 1, memcdSH.cu:562-574); the other version slots are empty.
+__global__ void memcd_clear_kernel(unsigned long long* tag, size_t n_tags) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_tags; i += stride)
+    tag[i] = (i % kMemcdDepth == 0) ? 0ull : ((unsigned long long)kEmptyTs << 32);
+}
+
+extern "C" csmv_status csmv_memcd_clear(csmv_memcd_t* h) {
+  if (!h) return CSMV_ERR_INVALID_ARG;
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  const size_t ent = (size_t)h->cfg.n_sets * kWays;
+  memcd_clear_kernel<<<h->n_sms * 4, 256, 0, h->stream>>>(h->tag, ent * kMemcdDepth);
+  CSMV_CUDA(cudaGetLastError());
+  CSMV_CUDA(cudaMemsetAsync(h->rec, 0, ent * kMemcdDepth * 64, h->stream));
+  CSMV_CUDA(cudaMemsetAsync(h->cw, 0, ent * 8, h->stream));
+  CSMV_CUDA(cudaMemsetAsync(h->done, 0, (size_t)kDoneWords * 4, h->stream));
+  CSMV_CUDA(cudaMemsetAsync(h->gs, 0, sizeof(GlobalSync), h->stream));
+  CSMV_CUDA(cudaStreamSynchronize(h->stream));
+  h->loaded = true;
+  h->last_final_ts = h->run_base_ts = h->last_n_req = 0;
+  return CSMV_OK;
+}
+
+static csmv_status check_batch(const csmv_memcd_t* h, const csmv_memcd_batch* b) {
+  if (!b || !b->kind || !b->key || !b->val || !b->found || !b->val_out || b->n_req == 0 ||
+      b->n_req % 32) {
+    set_error("batch: n_req must be a positive multiple of 32 with every pointer set");
+    return CSMV_ERR_INVALID_ARG;
+  }
+  if (b->n_req > h->cfg.max_req) {
+    set_error("batch of %u requests exceeds max_req %u", b->n_req, h->cfg.max_req);
+    return CSMV_ERR_CAPACITY;
+  }
+  return CSMV_OK;
+}
+
+static csmv_status launch(csmv_memcd_t* h, const uint32_t* kind, const uint4* key, const uint4* val,
+                          uint32_t* found, uint4* val_out, uint32_t n_req, uint32_t tick,
+                          csmv_stats* out) {
+  const csmv_memcd_config& c = h->cfg;
+  MemcdParams p{};
+  p.kind = kind;
+  p.key = key;
+  p.val = val;
+  p.n_rounds = n_req / 32;
+  p.tick = tick;
+  p.n_sets = c.n_sets;
+  p.tag = h->tag;
+  p.rec = h->rec;
+  p.cw = h->cw;
+  p.done = h->done;
+  p.done_mask = kDoneWords - 1;
+  p.gs = h->gs;
+  p.found = found;
+  p.val_out = val_out;
+  p.log_txn = h->log_txn;
+  p.outcome = h->outcome;
+  p.log = c.log_commits;
+  p.log_base = h->last_final_ts;
+  p.log_cap = h->log_cap;
+  p.stats = h->stats;
+  p.nc = c.client_warps;
+  p.batch = c.batch;
+  p.spin_log2 = c.spin_limit_log2;
+  CSMV_CUDA(cudaMemsetAsync(&h->gs->round_next, 0, 4, h->stream));
+  CSMV_CUDA(cudaMemsetAsync(&h->gs->error, 0, 4, h->stream));
+  CSMV_CUDA(cudaMemsetAsync(h->stats, 0, ST_COUNT * 8, h->stream));
+  void* args[] = {&p};
+  CSMV_CUDA(cudaEventRecord(h->ev0, h->stream));
+  CSMV_CUDA(cudaLaunchCooperativeKernel((const void*)memcd_kernel, dim3(h->ctas), dim3(h->threads),
+                                        args, 0, h->stream));
+  CSMV_CUDA(cudaEventRecord(h->ev1, h->stream));
+  unsigned long long st[ST_COUNT];
+  GlobalSync gs;
+  CSMV_CUDA(cudaMemcpyAsync(st, h->stats, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  CSMV_CUDA(cudaMemcpyAsync(&gs, h->gs, sizeof(gs), cudaMemcpyDeviceToHost, h->stream));
+  CSMV_CUDA(cudaStreamSynchronize(h->stream));
+  float ms = 0;
+  CSMV_CUDA(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+  h->last_n_req = n_req;
+  h->run_base_ts = h->last_final_ts;
+  h->last_final_ts = gs.ts_next;
+  if (out) {
+    std::memset(out, 0, sizeof(*out));
+    out->commits_update = st[ST_COMMIT_UPDATE];
+    out->commits_readonly = st[ST_COMMIT_RO];
+    out->aborts_data_age = st[ST_ABORT_DATA_AGE];
+    out->aborts_read_write = st[ST_ABORT_READ_WRITE];
+    out->aborts_prevalid = st[ST_ABORT_PREVALID];
+    out->aborts_write_write = st[ST_ABORT_WRITE_WRITE];
+    out->sections = st[ST_SECTIONS];
+    out->rounds = st[ST_ROUNDS];
+    out->final_ts = gs.ts_next;
+    out->error = gs.error;
+    out->kernel_ms = ms;
+  }
+  if (gs.error) {
+    set_error("device error %u (3 reply, 5 capacity, 6 mixed GET/SET round, 7 livelock)", gs.error);
+    return gs.error == ERR_DATA ? CSMV_ERR_INVALID_ARG : CSMV_ERR_TIMEOUT;
+  }
+  return CSMV_OK;
+}
+
+static csmv_status ready(csmv_memcd_t* h) {
+  if (!h) return CSMV_ERR_INVALID_ARG;
+  if (!h->loaded) {
+    set_error("csmv_memcd_clear must come first");
+    return CSMV_ERR_STATE;
+  }
+  return CSMV_OK;
+}
+
+extern "C" csmv_status csmv_memcd_run_device(csmv_memcd_t* h, const csmv_memcd_batch* b,
+                                             csmv_stats* out) {
+  csmv_status st = ready(h);
+  if (st != CSMV_OK || (st = check_batch(h, b)) != CSMV_OK) return st;
+  if (((uintptr_t)b->key | (uintptr_t)b->val | (uintptr_t)b->val_out) & 15u) {
+    set_error("device batch: key, val and val_out must be 16-byte aligned");
+    return CSMV_ERR_INVALID_ARG;
+  }
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  auto t0 = std::chrono::steady_clock::now();
+  st = launch(h, b->kind, (const uint4*)b->key, (const uint4*)b->val, b->found, (uint4*)b->val_out,
+              b->n_req, b->tick, out);
+  if (out)
+    out->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return st;
+}
+
+extern "C" csmv_status csmv_memcd_run(csmv_memcd_t* h, const csmv_memcd_batch* b, csmv_stats* out) {
+  csmv_status st = ready(h);
+  if (st != CSMV_OK || (st = check_batch(h, b)) != CSMV_OK) return st;
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  auto t0 = std::chrono::steady_clock::now();
+  const size_t n = b->n_req;
+  CSMV_CUDA(cudaMemcpyAsync(h->d_kind, b->kind, n * 4, cudaMemcpyHostToDevice, h->stream));
+  CSMV_CUDA(cudaMemcpyAsync(h->d_key, b->key, n * 16, cudaMemcpyHostToDevice, h->stream));
+  CSMV_CUDA(cudaMemcpyAsync(h->d_val, b->val, n * 32, cudaMemcpyHostToDevice, h->stream));
+  st = launch(h, h->d_kind, h->d_key, h->d_val, h->d_found, h->d_out, b->n_req, b->tick, out);
+  if (st == CSMV_OK) {
+    CSMV_CUDA(cudaMemcpyAsync(b->found, h->d_found, n * 4, cudaMemcpyDeviceToHost, h->stream));
+    CSMV_CUDA(cudaMemcpyAsync(b->val_out, h->d_out, n * 32, cudaMemcpyDeviceToHost, h->stream));
+    CSMV_CUDA(cudaStreamSynchronize(h->stream));
+  }
+  if (out)
+    out->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return st;
+}
+
+extern "C" csmv_status csmv_memcd_read_table(csmv_memcd_t* h, uint64_t* host_tags,
+                                             uint32_t* host_recs) {
+  csmv_status st = ready(h);
+  if (st != CSMV_OK) return st;
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  const size_t nv = (size_t)h->cfg.n_sets * kWays * kMemcdDepth;
+  if (host_tags) CSMV_CUDA(cudaMemcpy(host_tags, h->tag, nv * 8, cudaMemcpyDeviceToHost));
+  if (host_recs) CSMV_CUDA(cudaMemcpy(host_recs, h->rec, nv * 64, cudaMemcpyDeviceToHost));
+  return CSMV_OK;
+}
+
+extern "C" csmv_status csmv_memcd_read_log(csmv_memcd_t* h, uint32_t* host_log_txn, uint32_t n_log,
+                                           uint32_t* host_outcome, uint32_t n_req,
+                                           uint32_t* base_ts) {
+  csmv_status st = ready(h);
+  if (st != CSMV_OK) return st;
+  if (!h->cfg.log_commits) {
+    set_error("handle was created with log_commits = 0");
+    return CSMV_ERR_STATE;
+  }
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  const uint32_t used = h->last_final_ts - h->run_base_ts;
+  if (base_ts) *base_ts = h->run_base_ts;
+  if (host_log_txn) {
+    if (n_log < used) {
+      set_error("log buffer holds %u entries, run used %u timestamps", n_log, used);
+      return CSMV_ERR_CAPACITY;
+    }
+    CSMV_CUDA(cudaMemcpy(host_log_txn, h->log_txn, (size_t)used * 4, cudaMemcpyDeviceToHost));
+  }
+  if (n_req > h->last_n_req) n_req = h->last_n_req;
+  if (host_outcome)
+    CSMV_CUDA(cudaMemcpy(host_outcome, h->outcome, (size_t)n_req * 4, cudaMemcpyDeviceToHost));
+  return CSMV_OK;
+}
+
+extern "C" csmv_status csmv_memcd_device_info(csmv_memcd_t* h, int* n_sms, int* ctas,
+                                              int* threads_per_cta, size_t* device_bytes) {
+  if (!h) return CSMV_ERR_INVALID_ARG;
+  if (n_sms) *n_sms = h->n_sms;
+  if (ctas) *ctas = h->ctas;
+  if (threads_per_cta) *threads_per_cta = h->threads;
+  if (device_bytes) *device_bytes = h->device_bytes;
+  return CSMV_OK;
+}
+
+extern "C" void csmv_memcd_destroy(csmv_memcd_t* h) {
+  if (!h) return;
+  cudaSetDevice(h->cfg.device);
+  free_all(h);
+  delete h;
+}

@@ -1,0 +1,439 @@
+// memcd_kernel.cuh - transactional set-associative cache (the reference's memcachedGPU driver,
+// memcachedGPU/memcdSH.cu:237-448) on the stamp commit protocol (sm_103a).
+//
+// Reference: four versioned arrays (key, val, ts, state) of one word each per way; a SET reads
+// key/state/ts of every way with TXRead, picks the way holding the key (valid) or else the one
+// with the smallest LRU timestamp, and writes all four items; a GET reads key/state of each way
+// read-only and the value of the first match. Every transaction goes through the single
+// commit-server block.
+//
+// Here an entry (set, way) holds kMemcdDepth versions; version j is
+//   tag  (8 bytes): ts << 32 | valid << 31 | 31-bit key hash   - one single-copy-atomic word
+//   rec  (64 bytes): {lru, 0, 0, 0}, 16-byte key, 32-byte value
+// A writer (holding the entry's lock) empties the victim's tag, fences, writes the record,
+// fences and publishes the new tag; a reader re-reads the tag after the record, so a record is
+// used only if its tag did not move (a sequence-lock). The tags of a set's 8 ways sit in one
+// 128-byte line: a GET at snapshot S loads them in one access, picks per way the newest version
+// <= S, and reads only the records whose valid hash matches, in way order (first full key match
+// wins, as the reference breaks at the first match). A SET reads each way's latest committed
+// version (by its commit word), chooses the slot by the reference's rule, locks only that entry,
+// takes a commit timestamp from the CTA's server, validates the eight stamps and installs the
+// new version. Rounds of 32 requests are warp-uniform GETs or SETs (memcdSH.cu:333-339).
+#pragma once
+#include <cstdint>
+
+#include "bank_kernel.cuh"
+
+namespace csmv {
+
+constexpr int kWays = 8;
+constexpr int kMemcdDepth = 2;
+constexpr uint32_t kValidBit = 0x80000000u;
+
+struct MemcdParams {
+  const uint32_t* kind;  // [n] 0 = GET, 1 = SET
+  const uint4* key;      // [n]
+  const uint4* val;      // [2n]
+  uint32_t n_rounds;
+  uint32_t tick;         // LRU timestamp a SET writes (the reference's curr_clock)
+  uint32_t n_sets;
+  unsigned long long* tag;  // [entry][kMemcdDepth]
+  uint4* rec;               // [entry][kMemcdDepth][4]
+  unsigned long long* cw;   // [entry] commit words
+  uint32_t* done;
+  uint32_t done_mask;
+  GlobalSync* gs;
+  uint32_t* found;       // [n]
+  uint4* val_out;        // [2n]
+  uint32_t* log_txn;
+  uint32_t* outcome;
+  uint32_t log, log_base, log_cap;
+  unsigned long long* stats;
+  uint32_t nc, batch, spin_log2;
+};
+
+struct MemcdMail {
+  uint32_t req, rep, snap, cand, base, pad[3];
+};
+
+struct MemcdShared {
+  uint32_t done_warps, pad[3];
+  unsigned long long stat[ST_COUNT];
+  MemcdMail mail[kMaxClientWarps];
+};
+
+// Set of a 16-byte key (the reference takes its one-word key modulo nbSets,
+// memcdSH.cu:79-82; the four words are mixed first) and the 31-bit hash kept in the tag.
+__host__ __device__ __forceinline__ uint32_t memcd_mix(uint32_t k0, uint32_t k1, uint32_t k2,
+                                                       uint32_t k3) {
+  uint32_t h = k0 * 0x9E3779B1u ^ k1 * 0x85EBCA6Bu ^ k2 * 0xC2B2AE35u ^ k3 * 0x27D4EB2Fu;
+  return h ^ (h >> 16);
+}
+__host__ __device__ __forceinline__ uint32_t memcd_set_of(uint32_t h, uint32_t n_sets) {
+  return h % n_sets;
+}
+__host__ __device__ __forceinline__ uint32_t memcd_tag_hash(uint32_t h) {
+  return (h * 0x2C1B3C6Du) & 0x7FFFFFFFu;
+}
+
+__device__ __forceinline__ bool key_eq(uint4 a, uint4 b) {
+  return a.x == b.x && a.y == b.y && a.z == b.z && a.w == b.w;
+}
+__device__ __forceinline__ uint4 ld_relaxed_gpu_v4(const uint4* p) {
+  uint4 v;
+  asm volatile("ld.relaxed.gpu.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p)
+               : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_gpu_v4(uint4* p, uint4 v) {
+  asm volatile("st.relaxed.gpu.global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(p), "r"(v.x),
+               "r"(v.y), "r"(v.z), "r"(v.w)
+               : "memory");
+}
+__device__ __forceinline__ uint32_t tag_ts(unsigned long long t) { return (uint32_t)(t >> 32); }
+
+__device__ void memcd_client(const MemcdParams& p, MemcdShared& sm, uint32_t w) {
+  constexpr int D = kMemcdDepth;
+  MemcdMail& ms = sm.mail[w];
+  const uint32_t lane = lane_id();
+  const uint32_t me = blockIdx.x * p.nc + w + 1;
+  uint32_t seq = 0;
+  bool failed = false;
+  for (;;) {
+    uint32_t g = 0;
+    if (lane == 0) g = atomicAdd(&p.gs->round_next, 1u);
+    g = __shfl_sync(0xFFFFFFFFu, g, 0);
+    if (g >= p.n_rounds) break;
+    const uint32_t r = g * 32u + lane;
+    const uint32_t kind = p.kind[r];
+    const bool is_set = __all_sync(0xFFFFFFFFu, kind == 1u);
+    if (__any_sync(0xFFFFFFFFu, (kind == 1u) != is_set || kind > 1u)) {  // mixed round
+      if (lane == 0) raise_error(&p.gs->error, ERR_DATA);
+      failed = true;
+      break;
+    }
+    const uint4 key = p.key[r];
+    const uint32_t hmix = memcd_mix(key.x, key.y, key.z, key.w);
+    const uint32_t e0 = memcd_set_of(hmix, p.n_sets) * kWays;
+    const uint32_t th = memcd_tag_hash(hmix) | kValidBit;
+    uint4 nv0 = make_uint4(0, 0, 0, 0), nv1 = nv0;
+    if (is_set) {
+      nv0 = p.val[2 * r];
+      nv1 = p.val[2 * r + 1];
+    }
+    uint32_t pending = 0xFFFFFFFFu, attempts = 0, lock_fails = 0;
+    while (pending) {
+      if (lane == 0) atomicAdd(&sm.stat[ST_ROUNDS], 1ull);
+      if (++attempts > (1u << 20)) {
+        if (lane == 0) raise_error(&p.gs->error, ERR_LIVELOCK);
+        failed = true;
+        break;
+      }
+      if (lock_fails) {
+        const uint32_t h = (me * 0x9E3779B1u) ^ (attempts * 0x85EBCA6Bu);
+        __nanosleep((h >> 16) & ((64u << lock_fails) - 1u));
+      }
+      const bool mine = (pending >> lane) & 1u;
+      uint32_t snap = 0;
+      if (lane == 0) snap = ld_acquire_gpu(&p.gs->clock);
+      snap = __shfl_sync(0xFFFFFFFFu, snap, 0);
+      // the set's tag words: 8 ways x kMemcdDepth versions, one 128-byte line
+      unsigned long long tg[kWays * D];
+      if (mine) {
+#pragma unroll
+        for (int i = 0; i < kWays * D; i += 2)
+          ld_relaxed_gpu_v2(p.tag + (size_t)e0 * D + i, tg[i], tg[i + 1]);
+      }
+
+      if (!is_set) {
+        // GET: read-only at the snapshot
+        bool found = false, aged = false;
+        uint4 o0 = make_uint4(0, 0, 0, 0), o1 = o0;
+        if (mine) {
+          int pick[kWays];
+          unsigned long long ptag[kWays];
+#pragma unroll
+          for (int wy = 0; wy < kWays; wy++) {
+            int best = -1;
+            uint32_t bts = 0;
+            unsigned long long bt = 0;
+#pragma unroll
+            for (int j = 0; j < D; j++) {
+              const uint32_t t = tag_ts(tg[wy * D + j]);
+              if (t != kEmptyTs && t <= snap && (best < 0 || t > bts)) {
+                best = j;
+                bts = t;
+                bt = tg[wy * D + j];
+              }
+            }
+            pick[wy] = best;
+            ptag[wy] = bt;
+            aged |= best < 0;
+          }
+          bool fenced = false;
+#pragma unroll
+          for (int wy = 0; wy < kWays; wy++) {
+            const unsigned long long t0 = ptag[wy];
+            // skip: decided, or not valid, or another key's hash
+            if (aged || found || (uint32_t)t0 != th) continue;
+            if (!fenced) {  // the record loads stay behind the tag loads (sequence lock)
+              fence_acq_rel_gpu();
+              fenced = true;
+            }
+            const size_t v = (size_t)(e0 + wy) * D + pick[wy];
+            const uint4 kk = ld_relaxed_gpu_v4(p.rec + v * 4 + 1);
+            const uint4 a0 = ld_relaxed_gpu_v4(p.rec + v * 4 + 2);
+            const uint4 a1 = ld_relaxed_gpu_v4(p.rec + v * 4 + 3);
+            fence_acq_rel_gpu();
+            if (ld_relaxed_gpu(p.tag + v) != t0) {  // overwritten meanwhile: retry
+              aged = true;
+              continue;
+            }
+            if (key_eq(kk, key)) {
+              found = true;
+              o0 = a0;
+              o1 = a1;
+            }
+          }
+        }
+        const bool done = mine && !aged;
+        if (done) {
+          p.found[r] = found ? 1u : 0u;
+          p.val_out[2 * r] = o0;
+          p.val_out[2 * r + 1] = o1;
+          if (p.log) p.outcome[r] = snap | kSnapFlag;
+        }
+        const uint32_t dm = __ballot_sync(0xFFFFFFFFu, done);
+        const uint32_t am = __ballot_sync(0xFFFFFFFFu, mine && aged);
+        if (lane == 0) {
+          stat_add(sm.stat, ST_COMMIT_RO, __popc(dm));
+          stat_add(sm.stat, ST_ABORT_DATA_AGE, __popc(am));
+        }
+        pending &= ~dm;
+        continue;
+      }
+
+      // SET: each way's latest committed version (the one whose ts is the way's stamp); the
+      // slot by the reference's rule: the way holding the key (valid), else the smallest LRU
+      // timestamp, first on ties (memcdSH.cu:365-387)
+      uint32_t stw[kWays];
+      bool aborted = false;
+      int slot = -1;
+      uint32_t slot_lru = 0;
+      bool matched = false;
+#pragma unroll
+      for (int wy = 0; wy < kWays; wy++) stw[wy] = 0;
+      if (mine) {
+        unsigned long long wordv[kWays];
+#pragma unroll
+        for (int wy = 0; wy < kWays; wy++) wordv[wy] = ld_relaxed_gpu(&p.cw[e0 + wy]);
+        fence_acq_rel_gpu();  // the record loads stay behind the tag loads (sequence lock)
+        int sj[kWays];
+        unsigned long long s0[kWays];
+        uint32_t lru[kWays];
+        bool km[kWays];
+#pragma unroll
+        for (int wy = 0; wy < kWays; wy++) {
+          const uint32_t st = (uint32_t)wordv[wy];
+          stw[wy] = st;
+          int j = -1;
+          unsigned long long t0 = 0;
+#pragma unroll
+          for (int q = 0; q < D; q++)
+            if (tag_ts(tg[wy * D + q]) == st) {
+              j = q;
+              t0 = tg[wy * D + q];
+            }
+          sj[wy] = j;
+          s0[wy] = t0;
+          lru[wy] = 0;
+          km[wy] = false;
+          if (j < 0) {  // the stamp's version not seen yet (fetched concurrently): retry
+            aborted = true;
+            continue;
+          }
+          const size_t v = (size_t)(e0 + wy) * D + j;
+          const uint4 hd = ld_relaxed_gpu_v4(p.rec + v * 4);
+          const uint4 kk = ld_relaxed_gpu_v4(p.rec + v * 4 + 1);
+          lru[wy] = hd.x;
+          km[wy] = ((uint32_t)t0 & kValidBit) && key_eq(kk, key);
+        }
+        fence_acq_rel_gpu();
+        unsigned long long tg2[kWays * D];
+#pragma unroll
+        for (int i = 0; i < kWays * D; i += 2)
+          ld_relaxed_gpu_v2(p.tag + (size_t)e0 * D + i, tg2[i], tg2[i + 1]);
+#pragma unroll
+        for (int wy = 0; wy < kWays; wy++) {
+#pragma unroll
+          for (int q = 0; q < D; q++)
+            if (q == sj[wy] && tg2[wy * D + q] != s0[wy]) aborted = true;  // record moved
+          if (!matched) {
+            if (km[wy]) {
+              slot = wy;
+              matched = true;
+            } else if (slot < 0 || lru[wy] < slot_lru) {
+              slot = wy;
+              slot_lru = lru[wy];
+            }
+          }
+        }
+      }
+      const uint32_t target = e0 + (uint32_t)(slot < 0 ? 0 : slot);
+      // intra-warp: lane order over (reads: the 8 entries of the set, write: the slot)
+      ReadSet<kWays> rs;
+      WriteSet<1> ws;
+      bool cand_me = mine && !aborted;
+      if (cand_me) {
+        rs.n = kWays;
+#pragma unroll
+        for (int wy = 0; wy < kWays; wy++) rs.addr[wy] = e0 + wy;
+        ws.n = 1;
+        ws.addr[0] = target;
+      }
+      uint32_t cand = __ballot_sync(0xFFFFFFFFu, cand_me);
+      const uint32_t overlap = TXWriteOverlap(ws, cand_me);
+      const bool attempt = cand_me && (overlap & cand) == 0;
+      const bool got = attempt && atomicCAS(owner_word(p.cw, target), 0u, me) == 0u;
+      const uint32_t locked = __ballot_sync(0xFFFFFFFFu, got);
+      const uint32_t pass = TXPreValidation(rs, ws, got);
+      if (got && !((pass >> lane) & 1u)) st_relaxed_gpu(owner_word(p.cw, target), 0u);
+      const uint32_t agm = __ballot_sync(0xFFFFFFFFu, mine && aborted);
+      if (lane == 0) {
+        stat_add(sm.stat, ST_ABORT_DATA_AGE, __popc(agm));
+        stat_add(sm.stat, ST_ABORT_WRITE_WRITE, __popc(cand & ~locked));
+        stat_add(sm.stat, ST_ABORT_PREVALID, __popc(locked & ~pass));
+      }
+      lock_fails = __ballot_sync(0xFFFFFFFFu, attempt && !got) ? min(lock_fails + 1, 6u) : 0u;
+      cand = pass;
+      cand_me = (cand >> lane) & 1u;
+      if (cand == 0) continue;
+      // commit timestamps from the CTA's server
+      seq++;
+      __syncwarp();
+      if (lane == 0) {
+        ms.snap = snap;
+        ms.cand = cand;
+        st_release_cta(&ms.req, seq);
+      }
+      bool ok_wait = true;
+      if (lane == 0)
+        ok_wait = bounded_wait([&] { return ld_acquire_cta(&ms.rep) == seq; }, &p.gs->error,
+                               ERR_WAIT_REPLY, p.spin_log2);
+      ok_wait = __shfl_sync(0xFFFFFFFFu, ok_wait, 0);
+      if (!ok_wait) {
+        failed = true;
+        break;
+      }
+      (void)ld_acquire_cta(&ms.rep);
+      const uint32_t base = ms.base;
+      const uint32_t my_ts = base + 1 + __popc(cand & lanemask_lt());
+      fence_acq_rel_gpu();
+      if (cand_me) st_relaxed_gpu(owner_word(p.cw, target), kPendingFlag | my_ts);
+      bool valid = cand_me;
+      if (cand_me) {
+        unsigned long long wd[kWays];
+#pragma unroll
+        for (int wy = 0; wy < kWays; wy++) wd[wy] = ld_relaxed_gpu(&p.cw[e0 + wy]);
+#pragma unroll
+        for (int wy = 0; wy < kWays; wy++) {
+          if (!valid) continue;
+          // a lock of an earlier or not yet numbered holder: wait (bounded) for its outcome;
+          // a later holder is ordered after this SET and is ignored
+          bool settled = false;
+          for (uint32_t it = 0; it < 2048; it++) {
+            const uint32_t own = (uint32_t)(wd[wy] >> 32);
+            if (own == 0u || own == me ||
+                ((own & kPendingFlag) && (own & ~kPendingFlag) >= my_ts)) {
+              settled = true;
+              break;
+            }
+            __nanosleep(32);
+            wd[wy] = ld_relaxed_gpu(&p.cw[e0 + wy]);
+          }
+          valid = settled && (uint32_t)wd[wy] == stw[wy];
+        }
+      }
+      const uint32_t okm = __ballot_sync(0xFFFFFFFFu, valid);
+      if (lane == 0) stat_add(sm.stat, ST_ABORT_READ_WRITE, __popc(cand & ~okm));
+      if (p.log && cand_me) {
+        const uint32_t li = my_ts - 1 - p.log_base;
+        if (li < p.log_cap)
+          p.log_txn[li] = valid ? r : kHole;
+        else
+          raise_error(&p.gs->error, ERR_CAPACITY);
+      }
+      if (valid) {  // install: an empty version first, else the oldest (we hold the lock)
+        const size_t v0 = (size_t)target * D;
+        int vic = 0;
+        uint32_t vkey = 0xFFFFFFFFu;
+#pragma unroll
+        for (int j = 0; j < D; j++) {
+          const uint32_t k = tag_ts(ld_relaxed_gpu(p.tag + v0 + j)) + 1u;
+          if (j == 0 || k < vkey) {
+            vkey = k;
+            vic = j;
+          }
+        }
+        const size_t v = v0 + vic;
+        st_relaxed_gpu(p.tag + v, (unsigned long long)kEmptyTs << 32);  // readers: moving
+        __threadfence();
+        st_relaxed_gpu_v4(p.rec + v * 4, make_uint4(p.tick, 0u, 0u, 0u));
+        st_relaxed_gpu_v4(p.rec + v * 4 + 1, key);
+        st_relaxed_gpu_v4(p.rec + v * 4 + 2, nv0);
+        st_relaxed_gpu_v4(p.rec + v * 4 + 3, nv1);
+        __threadfence();
+        st_relaxed_gpu(p.tag + v, ((unsigned long long)my_ts << 32) | th);
+        if (p.log) p.outcome[r] = my_ts;
+        p.found[r] = 0u;
+        p.val_out[2 * r] = make_uint4(0, 0, 0, 0);
+        p.val_out[2 * r + 1] = make_uint4(0, 0, 0, 0);
+      }
+      __threadfence();
+      if (cand_me) {
+        if (valid)
+          st_release_gpu(&p.cw[target], (unsigned long long)my_ts);
+        else
+          st_relaxed_gpu(owner_word(p.cw, target), 0u);
+      }
+      __syncwarp();
+      if (lane == 0) {
+        complete_range(p.done, p.done_mask, p.gs, base + 1, base + __popc(cand));
+        stat_add(sm.stat, ST_COMMIT_UPDATE, __popc(okm));
+      }
+      pending &= ~okm;
+      uint32_t err = 0;
+      if (lane == 0) err = ld_relaxed_gpu(&p.gs->error);
+      if (__shfl_sync(0xFFFFFFFFu, err, 0) != 0) {
+        failed = true;
+        break;
+      }
+    }
+    if (failed) break;
+  }
+  __syncwarp();
+  if (lane == 0) atomicAdd(&sm.done_warps, 1u);
+}
+
+__global__ void __launch_bounds__(512, 1) memcd_kernel(MemcdParams p) {
+  __shared__ MemcdShared sm;
+  const uint32_t warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) sm.done_warps = 0;
+  for (uint32_t i = threadIdx.x; i < ST_COUNT; i += blockDim.x) sm.stat[i] = 0;
+  for (uint32_t i = threadIdx.x; i < p.nc; i += blockDim.x) {
+    sm.mail[i].req = 0;
+    sm.mail[i].rep = 0;
+  }
+  __syncthreads();
+  if (warp == 0)
+    server_warp_stamp(p.nc, p.batch, p.gs, sm);
+  else
+    memcd_client(p, sm, warp - 1);
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < ST_COUNT; i += blockDim.x)
+    if (sm.stat[i]) atomicAdd(&p.stats[i], sm.stat[i]);
+}
+
+}  // namespace csmv

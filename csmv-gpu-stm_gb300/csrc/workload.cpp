@@ -175,3 +175,39 @@ extern "C" csmv_status csmv_bank_generate(const csmv_bank_workload* w, uint32_t*
   }
   return CSMV_OK;
 }
+
+// ---------------------------------------------------------------------------------------------
+// cache requests
+// ---------------------------------------------------------------------------------------------
+namespace {
+csmv_status check_memcd_workload(const csmv_memcd_workload* w) {
+  if (!w || w->n_req == 0 || w->n_req % 32 || w->n_keys < 1 || w->get_pct > 100 ||
+      (w->dist != CSMV_DIST_UNIFORM && w->dist != CSMV_DIST_ZIPF) ||
+      (w->dist == CSMV_DIST_ZIPF && !(w->zipf_theta > 0.0))) {
+    csmv::set_error("invalid memcd workload");
+    return CSMV_ERR_INVALID_ARG;
+  }
+  return CSMV_OK;
+}
+}  // namespace
+
+extern "C" csmv_status csmv_memcd_generate(const csmv_memcd_workload* w, uint32_t* kind,
+                                           uint32_t* key, uint32_t* val) {
+  csmv_status st = check_memcd_workload(w);
+  if (st != CSMV_OK) return st;
+  if (!kind || !key || !val) return CSMV_ERR_INVALID_ARG;
+  const Zipf zipf(w->dist == CSMV_DIST_ZIPF ? w->zipf_theta : 1.0, w->n_keys);
+  for (uint32_t r = 0; r < w->n_req / 32; ++r) {
+    const bool get = scale(draw32(w->seed, (3ull << 40) + r, 0), 100) < w->get_pct;
+    for (uint32_t lane = 0; lane < 32; ++lane) {
+      const uint64_t i = static_cast<uint64_t>(r) * 32 + lane;
+      kind[i] = get ? CSMV_MEMCD_GET : CSMV_MEMCD_SET;
+      const uint32_t id = w->dist == CSMV_DIST_ZIPF ? zipf.rank(w->seed, i, 0) - 1u
+                                                    : scale(draw32(w->seed, i, 0x100ull), w->n_keys);
+      key[4 * i] = id;
+      for (uint32_t j = 1; j < 4; ++j) key[4 * i + j] = static_cast<uint32_t>(mix64(id * 4ull + j) >> 32);
+      for (uint32_t j = 0; j < 8; ++j) val[8 * i + j] = get ? 0u : draw32(w->seed, i, 0x200ull + j);
+    }
+  }
+  return CSMV_OK;
+}

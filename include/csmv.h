@@ -136,7 +136,7 @@ typedef struct csmv_bank_config {
   int32_t init_value;          /* every account starts at this balance                        */
   uint32_t version_depth;      /* versions kept per account, 2..16                            */
   uint32_t ring_size;          /* commit-record ring entries, power of two, >= 64             */
-  uint32_t client_warps;       /* client warps per CTA (1..31)                                */
+  uint32_t client_warps;       /* client warps per CTA (1..15)                                */
   uint32_t ctas;               /* CTAs; 0 = as many as fit co-resident on the GPU             */
   uint32_t cluster_size;       /* CTAs per cluster for CSMV_BATCH_CLUSTER (2..8)               */
   uint32_t validate;           /* CSMV_VALIDATE_*                                             */
@@ -205,12 +205,112 @@ csmv_status csmv_bank_read_versions(csmv_bank_t* h, uint64_t* host_slots);
 csmv_status csmv_bank_read_log(csmv_bank_t* h, uint32_t* host_log_txn, uint32_t n_log,
                                uint32_t* host_outcome, int32_t* host_result, uint32_t n_txn);
 
-/* Device pointers of the engine's stream-input buffers (capacity max_txn / n_addr_cap) so a
- * caller can stage input itself and call csmv_bank_run_device. */
+/* SM count, CTAs and threads per CTA of the commit kernel, and device bytes the handle holds. */
 csmv_status csmv_bank_device_info(csmv_bank_t* h, int* n_sms, int* ctas, int* threads_per_cta,
                                   size_t* device_bytes);
 
 void csmv_bank_destroy(csmv_bank_t* h);
+
+/* ------------------------------------------------------------------------------------------
+ * Transactional cache (memcachedGPU/memcdSH.cu)
+ *
+ * An 8-way set-associative table of n_sets sets. An entry holds a 16-byte key (4 uint32
+ * words), a 32-byte value (8 words), a valid flag and an LRU timestamp, each SET a
+ * transaction over its set as in the reference (memcdSH.cu:343-398): it reads the 8 ways, takes
+ * the way that holds the key (valid), else the way with the smallest LRU timestamp (first on
+ * ties), and writes key, value, LRU = the batch's tick and valid. A GET reads the set at a
+ * snapshot and returns the value of the valid way holding the key (memcdSH.cu:400-440).
+ * Two versions of each entry are kept.
+ *
+ * Request batch: n_req requests, a multiple of 32; requests [32r, 32r+32) are all GETs or all
+ * SETs (the reference decides GET vs SET per warp, memcdSH.cu:333-339).
+ *   kind[i]            CSMV_MEMCD_GET or CSMV_MEMCD_SET
+ *   key[4i .. 4i+3]    key words
+ *   val[8i .. 8i+7]    value words (SET; ignored for GET)
+ *   found[i]           out: GET 1 = hit, 0 = miss; SET 0
+ *   val_out[8i ..]     out: GET hit value, else zeros
+ *   tick               LRU timestamp the batch's SETs write: the reference's curr_clock, which
+ *                      its host loop sets to 1 and increments after every batch (memcdSH.cu:573,648)
+ * The key's set is h % n_sets (the reference's one-word key % nbSets, memcdSH.cu:80-83, over
+ * four words) with h = k0*0x9E3779B1 ^ k1*0x85EBCA6B ^ k2*0xC2B2AE35 ^ k3*0x27D4EB2F (uint32),
+ * h ^= h >> 16. Device batches need 16-byte aligned key, val and val_out.
+ * ------------------------------------------------------------------------------------------ */
+enum { CSMV_MEMCD_GET = 0, CSMV_MEMCD_SET = 1 };
+#define CSMV_MEMCD_WAYS 8
+#define CSMV_MEMCD_KEY_WORDS 4
+#define CSMV_MEMCD_VAL_WORDS 8
+
+typedef struct csmv_memcd_batch {
+  uint32_t n_req;
+  uint32_t tick;
+  const uint32_t* kind;   /* [n_req]     */
+  const uint32_t* key;    /* [n_req * 4] */
+  const uint32_t* val;    /* [n_req * 8] */
+  uint32_t* found;        /* [n_req]     */
+  uint32_t* val_out;      /* [n_req * 8] */
+} csmv_memcd_batch;
+
+typedef struct csmv_memcd_workload {
+  uint64_t seed;
+  uint32_t n_keys;     /* key population; request keys are drawn from ids 0..n_keys-1        */
+  uint32_t n_req;      /* multiple of 32                                                     */
+  uint32_t get_pct;    /* % of rounds that are GETs (0..100)                                  */
+  uint32_t dist;       /* CSMV_DIST_UNIFORM or CSMV_DIST_ZIPF (over key ids)                  */
+  double zipf_theta;
+} csmv_memcd_workload;
+
+/* Requests of a seeded workload into caller buffers (kind [n_req], key [4 n_req],
+ * val [8 n_req]). Key id k has words {k, h(k,1), h(k,2), h(k,3)}; replaces the reference's
+ * host key generation (memcdSH.cu:590-600, 624-634). */
+csmv_status csmv_memcd_generate(const csmv_memcd_workload* w, uint32_t* host_kind,
+                                uint32_t* host_key, uint32_t* host_val);
+
+typedef struct csmv_memcd_config {
+  uint32_t n_sets;           /* sets (2^20 for the 8 M-entry cache)                            */
+  uint32_t n_ways;           /* must be 8                                                       */
+  uint32_t version_depth;    /* versions per entry, must be 2                                   */
+  uint32_t client_warps;     /* client warps per CTA (1..15)                                    */
+  uint32_t ctas;             /* CTAs; 0 = as many as fit co-resident                            */
+  uint32_t batch;            /* CSMV_BATCH_WARP or CSMV_BATCH_CTA                               */
+  uint32_t log_commits;      /* 1 = keep the per-ts commit log and per-request outcomes        */
+  uint32_t max_req;          /* largest batch a run may carry                                  */
+  uint32_t spin_limit_log2;  /* bounded waits give up after 2^this polls                        */
+  int32_t device;
+} csmv_memcd_config;
+
+typedef struct csmv_memcd_t csmv_memcd_t;
+
+void csmv_memcd_config_default(csmv_memcd_config* cfg);
+
+/* Replaces the cache allocation of memcdSH's main (memcdSH.cu:557-566), create_gbc and TXInit. */
+csmv_status csmv_memcd_create(const csmv_memcd_config* cfg, csmv_memcd_t** out);
+
+/* Empties the table (every entry invalid, LRU 0, memcdSH.cu:567-574) and restarts the commit
+ * order at timestamp 0. */
+csmv_status csmv_memcd_clear(csmv_memcd_t* h);
+
+/* Runs one batch from HOST buffers (copies in, runs the commit kernel, copies results out):
+ * one iteration of the reference's batch loop (memcdSH.cu:622-651). */
+csmv_status csmv_memcd_run(csmv_memcd_t* h, const csmv_memcd_batch* host_batch, csmv_stats* out);
+
+/* Same with every batch pointer in device memory. */
+csmv_status csmv_memcd_run_device(csmv_memcd_t* h, const csmv_memcd_batch* dev_batch,
+                                  csmv_stats* out);
+
+/* Raw version store: host_tags[v] = ts << 32 | valid << 31 | key hash (empty: ts 0xFFFFFFFF),
+ * host_recs[16 v ..] = {lru, 0, 0, 0, key[4], value[8]}, v = (set*8 + way)*2 + version.
+ * Either pointer may be NULL. */
+csmv_status csmv_memcd_read_table(csmv_memcd_t* h, uint64_t* host_tags, uint32_t* host_recs);
+
+/* Commit log of the last run: host_log_txn[k] = request that committed a SET with timestamp
+ * *base_ts + k + 1 (0xFFFFFFFF: a timestamp whose SET failed validation);
+ * host_outcome[i] = commit ts of a SET, (snapshot | 0x80000000) of a GET. */
+csmv_status csmv_memcd_read_log(csmv_memcd_t* h, uint32_t* host_log_txn, uint32_t n_log,
+                                uint32_t* host_outcome, uint32_t n_req, uint32_t* base_ts);
+
+csmv_status csmv_memcd_device_info(csmv_memcd_t* h, int* n_sms, int* ctas, int* threads_per_cta,
+                                   size_t* device_bytes);
+void csmv_memcd_destroy(csmv_memcd_t* h);
 
 /* Page-locked host buffers for staging streams (the e2e path copies from pinned memory).
  * Replaces CUDA_DUAL_ALLOC's cudaMallocHost half (memcachedGPU/cuda_util.h:50-60). */

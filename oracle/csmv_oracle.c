@@ -824,3 +824,231 @@ int orc_bank_locked(uint32_t n_txn, const uint32_t* op, const uint32_t* off,
   free(locks);
   return 0;
 }
+
+/* ======================================================================================
+ * Transactional cache: serial semantics, replay checker, CPU baseline
+ *
+ * Entry e = set*8 + way holds 2 versions; version v = e*2 + j has a tag
+ * (ts << 32 | valid << 31 | 31-bit key hash, empty = ts 0xFFFFFFFF) and a 16-word record
+ * {lru, 0, 0, 0, key[4], value[8]}. The state of an entry is its newest version (largest ts).
+ * SET slot rule: orc_memcd_set_slot (memcdSH.cu:365-387) over the ways' newest versions.
+ * ==================================================================================== */
+#define MC_WAYS 8
+#define MC_D 2
+
+uint32_t orc_memcd_mix(const uint32_t* k) {
+  uint32_t h = k[0] * 0x9E3779B1u ^ k[1] * 0x85EBCA6Bu ^ k[2] * 0xC2B2AE35u ^ k[3] * 0x27D4EB2Fu;
+  return h ^ (h >> 16);
+}
+static uint32_t mc_tag_hash(uint32_t h) { return (h * 0x2C1B3C6Du) & 0x7FFFFFFFu; }
+
+void orc_memcd_init_table(uint32_t n_sets, uint64_t* tags, uint32_t* recs) {
+  size_t nv = (size_t)n_sets * MC_WAYS * MC_D;
+  for (size_t v = 0; v < nv; v++) tags[v] = (v % MC_D == 0) ? 0ull : (0xFFFFFFFFull << 32);
+  memset(recs, 0, nv * 16 * sizeof(uint32_t));
+}
+
+static int mc_newest(const uint64_t* tags, size_t e) {
+  int best = -1;
+  uint32_t bts = 0;
+  for (int j = 0; j < MC_D; j++) {
+    uint32_t t = (uint32_t)(tags[e * MC_D + j] >> 32);
+    if (t == 0xFFFFFFFFu) continue;
+    if (best < 0 || t > bts) {
+      best = j;
+      bts = t;
+    }
+  }
+  return best;
+}
+
+/* GET at the table's current state: 1 on a hit (value copied to out[8]). */
+static int mc_get(uint32_t n_sets, const uint64_t* tags, const uint32_t* recs, const uint32_t* key,
+                  uint32_t* out) {
+  size_t e0 = (size_t)(orc_memcd_mix(key) % n_sets) * MC_WAYS;
+  for (int w = 0; w < MC_WAYS; w++) {
+    int j = mc_newest(tags, e0 + w);
+    if (j < 0) continue;
+    size_t v = (e0 + w) * MC_D + j;
+    const uint32_t* r = recs + v * 16;
+    if ((tags[v] & 0x80000000ull) && !memcmp(r + 4, key, 16)) {
+      memcpy(out, r + 8, 32);
+      return 1;
+    }
+  }
+  memset(out, 0, 32);
+  return 0;
+}
+
+/* SET with commit timestamp ts: slot by the reference rule, new version into the victim. */
+static void mc_set(uint32_t n_sets, uint64_t* tags, uint32_t* recs, const uint32_t* key,
+                   const uint32_t* val, uint32_t tick, uint32_t ts) {
+  uint32_t h = orc_memcd_mix(key);
+  size_t e0 = (size_t)(h % n_sets) * MC_WAYS;
+  int32_t match[MC_WAYS], state[MC_WAYS], age[MC_WAYS];
+  for (int w = 0; w < MC_WAYS; w++) {
+    int j = mc_newest(tags, e0 + w);
+    size_t v = (e0 + w) * MC_D + (j < 0 ? 0 : j);
+    const uint32_t* r = recs + v * 16;
+    state[w] = (j >= 0 && (tags[v] & 0x80000000ull)) ? 1 : 0;
+    match[w] = (j >= 0 && !memcmp(r + 4, key, 16)) ? 1 : 0;
+    age[w] = (int32_t)r[0];
+  }
+  int slot = orc_memcd_set_slot(match, state, age, MC_WAYS, 1);
+  size_t e = e0 + slot;
+  int vic = 0;
+  uint32_t vkey = (uint32_t)(tags[e * MC_D] >> 32) + 1u;
+  for (int j = 1; j < MC_D; j++) {
+    uint32_t k = (uint32_t)(tags[e * MC_D + j] >> 32) + 1u;
+    if (k < vkey) {
+      vkey = k;
+      vic = j;
+    }
+  }
+  size_t v = e * MC_D + vic;
+  tags[v] = ((uint64_t)ts << 32) | 0x80000000ull | mc_tag_hash(h);
+  uint32_t* r = recs + v * 16;
+  r[0] = tick;
+  r[1] = r[2] = r[3] = 0;
+  memcpy(r + 4, key, 16);
+  memcpy(r + 8, val, 32);
+}
+
+void orc_memcd_serial(uint32_t n_req, const uint32_t* kind, const uint32_t* key,
+                      const uint32_t* val, uint32_t tick, uint32_t n_sets, uint32_t base_ts,
+                      uint64_t* tags, uint32_t* recs, uint32_t* found, uint32_t* val_out,
+                      uint32_t* log_txn, uint32_t* outcome, uint32_t* n_log) {
+  uint32_t ts = base_ts;
+  for (uint32_t i = 0; i < n_req; i++) {
+    if (kind[i] == 1u) {
+      ts++;
+      mc_set(n_sets, tags, recs, key + 4 * (size_t)i, val + 8 * (size_t)i, tick, ts);
+      if (found) found[i] = 0;
+      if (val_out) memset(val_out + 8 * (size_t)i, 0, 32);
+      if (log_txn) log_txn[ts - base_ts - 1] = i;
+      if (outcome) outcome[i] = ts;
+    } else {
+      uint32_t tmp[8];
+      uint32_t f = (uint32_t)mc_get(n_sets, tags, recs, key + 4 * (size_t)i, tmp);
+      if (found) found[i] = f;
+      if (val_out) memcpy(val_out + 8 * (size_t)i, tmp, 32);
+      if (outcome) outcome[i] = ts | SNAP_FLAG;
+    }
+  }
+  if (n_log) *n_log = ts - base_ts;
+}
+
+int orc_memcd_check(uint32_t n_req, const uint32_t* kind, const uint32_t* key,
+                    const uint32_t* val, uint32_t tick, uint32_t n_sets, const uint64_t* tags0,
+                    const uint32_t* recs0, uint32_t base_ts, uint32_t n_log,
+                    const uint32_t* log_txn, const uint32_t* outcome, const uint32_t* found,
+                    const uint32_t* val_out, const uint64_t* tags, const uint32_t* recs,
+                    char* msg, int msg_len) {
+  int rc = 0;
+  size_t nv = (size_t)n_sets * MC_WAYS * MC_D;
+  uint64_t* mt = malloc(nv * 8);
+  uint32_t* mr = malloc(nv * 64);
+  uint8_t* seen = calloc(n_req ? n_req : 1, 1);
+  uint32_t* head = malloc(sizeof(uint32_t) * ((size_t)n_log + 1));
+  uint32_t* next = malloc(sizeof(uint32_t) * (n_req ? n_req : 1));
+  if (!mt || !mr || !seen || !head || !next) {
+    rc = fail(msg, msg_len, "oracle out of memory");
+    goto out;
+  }
+  if (tags0) {
+    memcpy(mt, tags0, nv * 8);
+    memcpy(mr, recs0, nv * 64);
+  } else {
+    orc_memcd_init_table(n_sets, mt, mr);
+  }
+  /* 1. the log names distinct SETs with matching outcomes; every SET committed once */
+  for (uint32_t k = 0; k < n_log; k++) {
+    uint32_t r = log_txn[k], ts = base_ts + k + 1;
+    if (r == 0xFFFFFFFFu) continue;
+    if (r >= n_req || kind[r] != 1u) {
+      rc = fail(msg, msg_len, "ts %u: request %u is not a SET of this batch", ts, r);
+      goto out;
+    }
+    if (seen[r]) {
+      rc = fail(msg, msg_len, "ts %u: request %u committed twice", ts, r);
+      goto out;
+    }
+    if (outcome[r] != ts) {
+      rc = fail(msg, msg_len, "ts %u: request %u outcome says %u", ts, r, outcome[r]);
+      goto out;
+    }
+    seen[r] = 1;
+  }
+  /* 2. GETs bucketed by snapshot */
+  for (uint32_t b = 0; b <= n_log; b++) head[b] = 0xFFFFFFFFu;
+  for (uint32_t r = 0; r < n_req; r++) {
+    if (kind[r] == 1u) {
+      if (!seen[r]) {
+        rc = fail(msg, msg_len, "SET %u never committed", r);
+        goto out;
+      }
+      continue;
+    }
+    if (!(outcome[r] & SNAP_FLAG)) {
+      rc = fail(msg, msg_len, "GET %u has no snapshot (outcome %u)", r, outcome[r]);
+      goto out;
+    }
+    uint32_t snap = outcome[r] & ~SNAP_FLAG;
+    if (snap < base_ts || snap > base_ts + n_log) {
+      rc = fail(msg, msg_len, "GET %u: snapshot %u outside [%u, %u]", r, snap, base_ts,
+                base_ts + n_log);
+      goto out;
+    }
+    next[r] = head[snap - base_ts];
+    head[snap - base_ts] = r;
+  }
+  /* 3. replay in ts order; GETs at snapshot s see every SET with ts <= s */
+  for (uint32_t k = 0; k <= n_log; k++) {
+    for (uint32_t r = head[k]; r != 0xFFFFFFFFu; r = next[r]) {
+      uint32_t want[8];
+      uint32_t f = (uint32_t)mc_get(n_sets, mt, mr, key + 4 * (size_t)r, want);
+      if (found[r] != f || memcmp(val_out + 8 * (size_t)r, want, 32)) {
+        rc = fail(msg, msg_len, "GET %u at snapshot %u: device found=%u val0=%u, replay found=%u val0=%u",
+                  r, base_ts + k, found[r], val_out[8 * (size_t)r], f, want[0]);
+        goto out;
+      }
+    }
+    if (k == n_log) break;
+    uint32_t r = log_txn[k];
+    if (r == 0xFFFFFFFFu) continue;
+    mc_set(n_sets, mt, mr, key + 4 * (size_t)r, val + 8 * (size_t)r, tick, base_ts + k + 1);
+    if (found[r] != 0u) {
+      rc = fail(msg, msg_len, "SET %u reports found=%u", r, found[r]);
+      goto out;
+    }
+  }
+  /* 4. the version store is bit-exact */
+  for (size_t v = 0; v < nv; v++) {
+    if (tags[v] != mt[v] || memcmp(recs + 16 * v, mr + 16 * v, 64)) {
+      rc = fail(msg, msg_len, "version %zu (set %zu way %zu slot %zu): device tag %016llx lru %u "
+                "key0 %u, replay tag %016llx lru %u key0 %u", v, v / (MC_WAYS * MC_D),
+                (v / MC_D) % MC_WAYS, v % MC_D, (unsigned long long)tags[v], recs[16 * v],
+                recs[16 * v + 4], (unsigned long long)mt[v], mr[16 * v], mr[16 * v + 4]);
+      goto out;
+    }
+  }
+out:
+  free(mt);
+  free(mr);
+  free(seen);
+  free(head);
+  free(next);
+  return rc;
+}
+
+int orc_memcd_serial_time(uint32_t n_req, const uint32_t* kind, const uint32_t* key,
+                          const uint32_t* val, uint32_t tick, uint32_t n_sets, uint64_t* tags,
+                          uint32_t* recs, uint32_t* found, uint32_t* val_out, uint64_t* ns) {
+  struct timespec a, b;
+  clock_gettime(CLOCK_MONOTONIC, &a);
+  orc_memcd_serial(n_req, kind, key, val, tick, n_sets, 0, tags, recs, found, val_out, NULL, NULL,
+                   NULL);
+  clock_gettime(CLOCK_MONOTONIC, &b);
+  *ns = (uint64_t)(b.tv_sec - a.tv_sec) * 1000000000ull + (uint64_t)(b.tv_nsec - a.tv_nsec);
+  return 0;
+}

@@ -16,6 +16,8 @@
  *   - orc_collab_validate   TXValidate (collaborative), collabValidation/csmv_sh/API.cu:193-266
  *   - orc_batched_ts        commit-ts offsets, batchedAtrInsert/csmv_sh/API.cu:296-377
  *   - orc_memcd_set_slot    SET slot choice, memcachedGPU/memcdSH.cu:365-387
+ *   - orc_memcd_serial      serial GET/SET semantics of the cache, memcdSH.cu:343-440
+ *   - orc_memcd_check       replay of a cache batch's commit log (exactness oracle)
  *   - orc_bank_check        serial replay of a commit log in commit-ts order (exactness oracle)
  *   - orc_bank_sim_1warp    deterministic model of one client warp + one server
  *   - orc_bank_serial / orc_bank_locked   CPU baselines (single thread / striped locks)
@@ -97,6 +99,29 @@ int orc_window_validate(const orc_record* by_ts /* index ts-1 */, uint32_t snap,
 /* ---- memcached slot choice ---------------------------------------------------------- */
 int orc_memcd_set_slot(const int32_t* keys, const int32_t* states, const int32_t* ages,
                        int ways, int32_t key);
+
+/* ---- transactional cache (8 ways, 2 versions per entry; layout in include/csmv.h) ------ */
+uint32_t orc_memcd_mix(const uint32_t* key4);
+void orc_memcd_init_table(uint32_t n_sets, uint64_t* tags, uint32_t* recs);
+/* Executes requests in order (SET i gets the next timestamp after base_ts); any of found,
+ * val_out, log_txn, outcome, n_log may be NULL. */
+void orc_memcd_serial(uint32_t n_req, const uint32_t* kind, const uint32_t* key,
+                      const uint32_t* val, uint32_t tick, uint32_t n_sets, uint32_t base_ts,
+                      uint64_t* tags, uint32_t* recs, uint32_t* found, uint32_t* val_out,
+                      uint32_t* log_txn, uint32_t* outcome, uint32_t* n_log);
+/* Replays the batch's SETs in commit-ts order from the table before the batch (tags0/recs0,
+ * NULL = empty), checks every GET against the state at its snapshot and the final version
+ * store bit for bit. 0 = ok, else a message in msg. */
+int orc_memcd_check(uint32_t n_req, const uint32_t* kind, const uint32_t* key,
+                    const uint32_t* val, uint32_t tick, uint32_t n_sets, const uint64_t* tags0,
+                    const uint32_t* recs0, uint32_t base_ts, uint32_t n_log,
+                    const uint32_t* log_txn, const uint32_t* outcome, const uint32_t* found,
+                    const uint32_t* val_out, const uint64_t* tags, const uint32_t* recs,
+                    char* msg, int msg_len);
+/* CPU baseline: serial execution, elapsed nanoseconds in *ns. */
+int orc_memcd_serial_time(uint32_t n_req, const uint32_t* kind, const uint32_t* key,
+                          const uint32_t* val, uint32_t tick, uint32_t n_sets, uint64_t* tags,
+                          uint32_t* recs, uint32_t* found, uint32_t* val_out, uint64_t* ns);
 
 /* ---- bank execution semantics -------------------------------------------------------- */
 /* Execute one transaction against `vals`; returns number of writes (0/2) and fills

@@ -82,6 +82,12 @@ def lib() -> C.CDLL:
             "orc_bank_sim_1warp": (I, [U, P, P, P, U, P, I, I, I, P, P, P, P, P]),
             "orc_bank_serial": (I, [U, P, P, P, U, P, P]),
             "orc_bank_locked": (I, [U, P, P, P, U, P, I, P]),
+            "orc_memcd_mix": (U, [P]),
+            "orc_memcd_init_table": (None, [U, P, P]),
+            "orc_memcd_serial": (None, [U, P, P, P, U, U, U, P, P, P, P, P, P, P]),
+            "orc_memcd_check": (I, [U, P, P, P, U, U, P, P, U, U, P, P, P, P, P, P,
+                                    C.c_char_p, I]),
+            "orc_memcd_serial_time": (I, [U, P, P, P, U, U, P, P, P, P, P]),
         })
     return _lib
 
@@ -181,3 +187,69 @@ def cpu_threads() -> int:
         return len(os.sched_getaffinity(0))
     except AttributeError:
         return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------------------------
+# transactional cache
+# ---------------------------------------------------------------------------------------------
+
+MC_VERSIONS = 16  # 8 ways x 2 versions per set
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def memcd_empty_table(n_sets: int):
+    tags = np.empty(n_sets * MC_VERSIONS, np.uint64)
+    recs = np.empty((n_sets * MC_VERSIONS, 16), np.uint32)
+    lib().orc_memcd_init_table(n_sets, p(tags), p(recs))
+    return tags, recs
+
+
+def memcd_serial(kind, key, val, tick, n_sets, table=None, base_ts=0):
+    """Serial execution in request order: (found, val_out, log_txn, outcome, tags, recs)."""
+    kind, key, val = _c(kind, np.uint32), _c(key, np.uint32), _c(val, np.uint32)
+    n = kind.shape[0]
+    tags, recs = memcd_empty_table(n_sets) if table is None else (table[0].copy(), table[1].copy())
+    found = np.empty(n, np.uint32)
+    val_out = np.empty((n, 8), np.uint32)
+    log_txn = np.empty(max(1, n), np.uint32)
+    outcome = np.empty(n, np.uint32)
+    n_log = C.c_uint32()
+    lib().orc_memcd_serial(n, p(kind), p(key), p(val), tick, n_sets, base_ts, p(tags), p(recs),
+                           p(found), p(val_out), p(log_txn), p(outcome), C.byref(n_log))
+    return found, val_out, log_txn[:n_log.value], outcome, tags, recs
+
+
+def memcd_check(kind, key, val, tick, n_sets, table0, base_ts, log_txn, outcome, found, val_out,
+                tags, recs):
+    """Replay checker; raises AssertionError with the oracle's message on a mismatch."""
+    kind, key, val = _c(kind, np.uint32), _c(key, np.uint32), _c(val, np.uint32)
+    log_txn, outcome = _c(log_txn, np.uint32), _c(outcome, np.uint32)
+    found, val_out = _c(found, np.uint32), _c(val_out, np.uint32)
+    tags, recs = _c(tags, np.uint64), _c(recs, np.uint32)
+    t0 = r0 = None
+    if table0 is not None:
+        t0, r0 = _c(table0[0], np.uint64), _c(table0[1], np.uint32)
+    msg = C.create_string_buffer(512)
+    rc = lib().orc_memcd_check(kind.shape[0], p(kind), p(key), p(val), tick, n_sets,
+                               p(t0) if t0 is not None else None,
+                               p(r0) if r0 is not None else None, base_ts, log_txn.shape[0],
+                               p(log_txn), p(outcome), p(found), p(val_out), p(tags), p(recs),
+                               msg, 512)
+    if rc != 0:
+        raise AssertionError(f"cache replay: {msg.value.decode()}")
+
+
+def memcd_serial_time(kind, key, val, tick, n_sets) -> float:
+    """Seconds of one serial pass over the requests from an empty table."""
+    kind, key, val = _c(kind, np.uint32), _c(key, np.uint32), _c(val, np.uint32)
+    n = kind.shape[0]
+    tags, recs = memcd_empty_table(n_sets)
+    found = np.empty(n, np.uint32)
+    val_out = np.empty((n, 8), np.uint32)
+    ns = C.c_uint64()
+    lib().orc_memcd_serial_time(n, p(kind), p(key), p(val), tick, n_sets, p(tags), p(recs),
+                                p(found), p(val_out), C.byref(ns))
+    return ns.value * 1e-9

@@ -40,3 +40,20 @@ def run_checked(w, *, init_value=1000, check=True, **cfg):
                         outcome, result, slots)
         assert err is None, err
     return st, s, (log_txn, outcome, result, slots)
+
+
+def memcd_run_checked(cache, req, *, check=True, tick=None):
+    """One cache batch through the C ABI, checked against the oracle's serial replay from the
+    table as it was before the batch. Returns (found, val_out, stats)."""
+    table0 = cache.table() if check else None
+    found, val_out, st = cache.run(req, tick=tick)
+    t = cache.tick - 1 if tick is None else tick
+    assert st.error == 0
+    n_set = int(np.count_nonzero(req.kind == cg.MEMCD_SET))
+    assert st.commits_update == n_set and st.commits_readonly == req.n_req - n_set
+    if check:
+        log_txn, outcome, base = cache.log(req.n_req)
+        tags, recs = cache.table()
+        orc.memcd_check(req.kind, req.key, req.val, t, cache.cfg.n_sets, table0, base, log_txn,
+                        outcome, found, val_out, tags, recs)
+    return found, val_out, st

@@ -26,7 +26,8 @@ def exported(lib: Path) -> set[str]:
 
 def test_every_declared_symbol_is_exported():
     names = declared(ROOT / "include" / "csmv.h")
-    assert {"csmv_bank_create", "csmv_bank_run", "csmv_bank_read_log", "csmv_last_error"} <= names
+    assert {"csmv_bank_create", "csmv_bank_run", "csmv_bank_read_log", "csmv_last_error",
+            "csmv_memcd_create", "csmv_memcd_run", "csmv_memcd_read_table"} <= names
     missing = names - exported(b.LIB)
     assert not missing, missing
 
@@ -39,10 +40,25 @@ def test_library_loads_and_reports_version():
 
 def test_config_validation_is_a_status():
     for bad in (dict(version_depth=3), dict(ring_size=100), dict(client_warps=0),
-                dict(client_warps=32), dict(validate=1, batch=0, writeback=0), dict(max_txn=33),
+                dict(client_warps=16), dict(validate=1, batch=0, writeback=0), dict(max_txn=33),
                 dict(spin_limit_log2=2), dict(n_accounts=1), dict(batch=9)):
         with pytest.raises(cg.CsmvError) as e:
             cg.Bank(cg.bank_config(**bad))
+        assert e.value.status == 1, bad
+
+
+def test_memcd_config_validation_is_a_status():
+    for bad in (dict(n_ways=4), dict(version_depth=4), dict(client_warps=0),
+                dict(client_warps=16), dict(batch=cg.BATCH_LANE), dict(max_req=33),
+                dict(n_sets=0), dict(spin_limit_log2=40)):
+        with pytest.raises(cg.CsmvError) as e:
+            cg.Memcd(cg.memcd_config(**bad))
+        assert e.value.status == 1, bad
+    for bad in (dict(n_req=33), dict(get_pct=101), dict(dist=cg.DIST_HOTSPOT), dict(n_keys=0)):
+        kw = dict(n_keys=100, n_req=64)
+        kw.update(bad)
+        with pytest.raises(cg.CsmvError) as e:
+            cg.memcd_generate(cg.memcd_workload(**kw))
         assert e.value.status == 1, bad
 
 
@@ -62,6 +78,10 @@ def test_null_handles_are_rejected():
     assert L.csmv_bank_run(None, None, None) == 1
     assert L.csmv_bank_read_values(None, None) == 1
     L.csmv_bank_destroy(None)
+    assert L.csmv_memcd_clear(None) == 1
+    assert L.csmv_memcd_run(None, None, None) == 1
+    assert L.csmv_memcd_read_table(None, None, None) == 1
+    L.csmv_memcd_destroy(None)
 
 
 @pytest.mark.skipif(cg.cuda_device_present(), reason="a GPU is present")
@@ -75,6 +95,12 @@ def test_driver_keeps_reference_cli():
     exe = b.BIN / "csmv_bank"
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert out.returncode == 0 and "argument order" in out.stdout and "8) verbose" in out.stdout
+
+
+def test_memcd_driver_keeps_reference_cli():
+    exe = b.BIN / "csmv_memcd"
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0 and "argument order" in out.stdout and "10) verbose" in out.stdout
 
 
 def test_devtest_library_exports():
