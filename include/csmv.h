@@ -211,6 +211,28 @@ csmv_status csmv_bank_device_info(csmv_bank_t* h, int* n_sms, int* ctas, int* th
 
 void csmv_bank_destroy(csmv_bank_t* h);
 
+/* Bank run that allocates no device memory. No counterpart in the reference: it exists for
+ * callers that cannot call cudaMalloc - a host that gives the library a fixed memory budget and
+ * forbids allocation after start-up, or a process whose device memory belongs to another
+ * allocator. It runs the default engine (stamp validation, CTA batches, client write-back,
+ * pre-validation, 4 versions per account) with its scratch - version store, commit words,
+ * completion bitmap, commit log - in one fixed device array of about 4.8 MiB, which every GPU
+ * that loads the library holds until the process exits. Limits: n_accounts <= 65536 and
+ * n_txn <= 65536 per call (larger sizes return CSMV_ERR_CAPACITY). All pointers are device
+ * memory owned by the caller: dev_init_values[n_accounts] in; dev_values[n_accounts] (latest
+ * value of each account), dev_outcome[n_txn] and dev_result[n_txn] (as csmv_bank_read_log) out.
+ * cuda_stream is a cudaStream_t (NULL = the legacy default stream); the call returns after the
+ * stream has finished the run. Calls share the array and keep nothing between them, so calls
+ * that overlap on the GPU race: serialise them. The first call on a device looks up the array's
+ * device address; make that first call before any stream capture. */
+#define CSMV_NOALLOC_MAX_ACCOUNTS 65536
+#define CSMV_NOALLOC_MAX_TXN 65536
+csmv_status csmv_bank_run_noalloc(int32_t device, void* cuda_stream, uint32_t n_accounts,
+                                  const int32_t* dev_init_values,
+                                  const csmv_bank_stream* dev_stream, uint32_t client_warps,
+                                  uint32_t ctas, int32_t* dev_values, uint32_t* dev_outcome,
+                                  int32_t* dev_result, csmv_stats* out);
+
 /* ------------------------------------------------------------------------------------------
  * Transactional cache (memcachedGPU/memcdSH.cu)
  *
