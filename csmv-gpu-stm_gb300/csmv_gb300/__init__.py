@@ -48,7 +48,8 @@ class BankWorkload(C.Structure):
 
 class BankStream(C.Structure):
     _fields_ = [("n_txn", C.c_uint32), ("op", C.c_void_p), ("off", C.c_void_p),
-                ("addr", C.c_void_p), ("n_addr", C.c_uint64)]
+                ("addr", C.c_void_p), ("n_addr", C.c_uint64), ("txn_aborts", C.c_void_p),
+                ("split_round", C.c_uint32), ("deferred_warps", C.c_uint32)]
 
 
 class BankConfig(C.Structure):
@@ -278,10 +279,17 @@ class Bank:
         _check(lib().csmv_bank_load(self._h, _ptr(values) if values is not None else None),
                "csmv_bank_load")
 
-    def run(self, stream: Stream) -> Stats:
-        """Host buffers in: copies the stream to the device inside the call."""
+    def run(self, stream: Stream, txn_aborts: np.ndarray | None = None, split_round: int = 0,
+            deferred_warps: int = 0) -> Stats:
+        """Host buffers in: copies the stream to the device inside the call. txn_aborts (uint32
+        [n_txn]) receives each transaction's failed attempts; split_round/deferred_warps set
+        up the deferred queue (csmv_bank_stream)."""
         st = Stats()
         s = stream.c_struct()
+        if txn_aborts is not None:
+            assert txn_aborts.dtype == np.uint32 and txn_aborts.shape[0] >= stream.n_txn
+            s.txn_aborts = _ptr(txn_aborts)
+        s.split_round, s.deferred_warps = split_round, deferred_warps
         rc = lib().csmv_bank_run(self._h, C.byref(s), C.byref(st))
         self.last_stats = st
         _check(rc, "csmv_bank_run")

@@ -54,6 +54,7 @@ struct csmv_bank_t {
   uint32_t* d_op = nullptr;
   uint32_t* d_off = nullptr;
   uint32_t* d_addr = nullptr;
+  uint32_t* d_aborts = nullptr;
   uint64_t addr_cap = 0;
   bool loaded = false;
   uint32_t last_final_ts = 0, last_n_txn = 0, run_base_ts = 0;
@@ -113,6 +114,7 @@ static void free_all(csmv_bank_t* h) {
   cudaFree(h->d_op);
   cudaFree(h->d_off);
   cudaFree(h->d_addr);
+  cudaFree(h->d_aborts);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -175,6 +177,7 @@ extern "C" csmv_status csmv_bank_create(const csmv_bank_config* cfg, csmv_bank_t
       {(void**)&h->log_txn, (size_t)h->log_cap * 4}, {(void**)&h->outcome, (size_t)cfg->max_txn * 4},
       {(void**)&h->result, (size_t)cfg->max_txn * 4},  {(void**)&h->stats, ST_COUNT * 8},
       {(void**)&h->d_op, (size_t)cfg->max_txn * 4},    {(void**)&h->d_off, (size_t)cfg->max_txn * 4},
+      {(void**)&h->d_aborts, (size_t)cfg->max_txn * 4},
   };
   for (auto& a : allocs) {
     if ((st = cuda_status(cudaMalloc(a.p, a.bytes), "cudaMalloc")) != CSMV_OK) return fail(st);
@@ -216,11 +219,16 @@ static csmv_status check_stream(const csmv_bank_t* h, const csmv_bank_stream* s)
     set_error("stream of %u transactions exceeds max_txn %u", s->n_txn, h->cfg.max_txn);
     return CSMV_ERR_CAPACITY;
   }
+  if (s->split_round > s->n_txn / 32 || (s->split_round && s->deferred_warps == 0)) {
+    set_error("stream: split_round must be <= n_txn/32, with deferred_warps > 0");
+    return CSMV_ERR_INVALID_ARG;
+  }
   return CSMV_OK;
 }
 
 static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* off,
-                          const uint32_t* addr, uint32_t n_txn, csmv_stats* out) {
+                          const uint32_t* addr, uint32_t n_txn, uint32_t* txn_aborts,
+                          uint32_t split_round, uint32_t deferred_warps, csmv_stats* out) {
   const csmv_bank_config& c = h->cfg;
   BankParams p{};
   p.op = op;
@@ -248,8 +256,12 @@ static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* of
   p.batch = c.batch;
   p.prevalidate = c.prevalidate;
   p.spin_log2 = c.spin_limit_log2;
-  // the commit order carries on from the previous run: only the cursor and error reset
+  p.txn_aborts = txn_aborts;
+  p.split_round = split_round;
+  p.deferred_warps = deferred_warps;
+  // the commit order carries on from the previous run: only the cursors and error reset
   CSMV_CUDA(cudaMemsetAsync(&h->gs->round_next, 0, 4, h->stream));
+  CSMV_CUDA(cudaMemsetAsync(&h->gs->round_deferred, 0, 4, h->stream));
   CSMV_CUDA(cudaMemsetAsync(&h->gs->error, 0, 4, h->stream));
   CSMV_CUDA(cudaMemsetAsync(h->stats, 0, ST_COUNT * 8, h->stream));
   void* args[] = {&p};
@@ -302,7 +314,8 @@ extern "C" csmv_status csmv_bank_run_device(csmv_bank_t* h, const csmv_bank_stre
   if (st != CSMV_OK) return st;
   CSMV_CUDA(cudaSetDevice(h->cfg.device));
   auto t0 = std::chrono::steady_clock::now();
-  st = launch(h, s->op, s->off, s->addr, s->n_txn, out);
+  st = launch(h, s->op, s->off, s->addr, s->n_txn, s->txn_aborts, s->split_round,
+              s->deferred_warps, out);
   if (out)
     out->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return st;
@@ -328,7 +341,13 @@ extern "C" csmv_status csmv_bank_run(csmv_bank_t* h, const csmv_bank_stream* s, 
   CSMV_CUDA(cudaMemcpyAsync(h->d_op, s->op, (size_t)s->n_txn * 4, cudaMemcpyHostToDevice, h->stream));
   CSMV_CUDA(cudaMemcpyAsync(h->d_off, s->off, (size_t)s->n_txn * 4, cudaMemcpyHostToDevice, h->stream));
   CSMV_CUDA(cudaMemcpyAsync(h->d_addr, s->addr, s->n_addr * 4, cudaMemcpyHostToDevice, h->stream));
-  st = launch(h, h->d_op, h->d_off, h->d_addr, s->n_txn, out);
+  st = launch(h, h->d_op, h->d_off, h->d_addr, s->n_txn, s->txn_aborts ? h->d_aborts : nullptr,
+              s->split_round, s->deferred_warps, out);
+  if (st == CSMV_OK && s->txn_aborts) {
+    CSMV_CUDA(cudaMemcpyAsync(s->txn_aborts, h->d_aborts, (size_t)s->n_txn * 4,
+                              cudaMemcpyDeviceToHost, h->stream));
+    CSMV_CUDA(cudaStreamSynchronize(h->stream));
+  }
   if (out)
     out->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return st;

@@ -61,7 +61,8 @@ struct alignas(128) GlobalSync {
   alignas(128) uint32_t ticket;          // ring protocol: next ticket
   alignas(128) uint32_t clock;           // every commit with ts <= clock is written back
   alignas(128) uint32_t ts_next;         // stamp protocol: last timestamp handed out
-  alignas(128) uint32_t round_next;      // next unclaimed round of the stream
+  alignas(128) uint32_t round_next;      // next unclaimed round of the stream (main queue)
+  alignas(128) uint32_t round_deferred;  // next unclaimed round of the deferred queue
   alignas(128) uint32_t error;           // first device error (ERR_*)
 };
 
@@ -89,6 +90,9 @@ struct BankParams {
   uint32_t nc;        // client warps per CTA
   uint32_t validate, writeback, batch, prevalidate;
   uint32_t spin_log2;
+  uint32_t* txn_aborts;     // optional [n_rounds*32]: failed attempts of each transaction
+  uint32_t split_round;     // rounds [split_round, n_rounds) form the deferred queue (0 = none)
+  uint32_t deferred_warps;  // client warps (lowest global ids) that serve the deferred queue
 };
 
 template <int MAXR, int MAXW>
@@ -260,11 +264,28 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
   const uint32_t me = blockIdx.x * p.nc + w + 1;  // lock owner id of this warp
   uint32_t seq = 0;
   bool failed = false;
+  // Deferred queue (a scheduler's likely-conflicting rounds): only the first deferred_warps
+  // warps of the grid take those rounds, so at most that many run at once; they join the main
+  // queue when the deferred one is empty.
+  const uint32_t main_end = p.split_round ? p.split_round : p.n_rounds;
+  bool serve_deferred = p.split_round != 0 && blockIdx.x * p.nc + w < p.deferred_warps;
   for (;;) {
-    uint32_t g = 0;
-    if (lane == 0) g = atomicAdd(&p.gs->round_next, 1u);
+    uint32_t g = 0xFFFFFFFFu;
+    if (lane == 0) {
+      if (serve_deferred) {
+        g = p.split_round + atomicAdd(&p.gs->round_deferred, 1u);
+        if (g >= p.n_rounds) {
+          g = 0xFFFFFFFFu;
+          serve_deferred = false;
+        }
+      }
+      if (g == 0xFFFFFFFFu) {
+        g = atomicAdd(&p.gs->round_next, 1u);
+        if (g >= main_end) g = 0xFFFFFFFFu;
+      }
+    }
     g = __shfl_sync(0xFFFFFFFFu, g, 0);
-    if (g >= p.n_rounds) break;
+    if (g == 0xFFFFFFFFu) break;
     const uint32_t t = g * 32u + lane;
     const uint32_t op = p.op[t];
     const uint32_t kind = CSMV_OP_KIND(op), nr = CSMV_OP_NREADS(op);
@@ -288,9 +309,10 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
     }
 
     uint32_t pending = 0xFFFFFFFFu;
-    uint32_t attempts = 0, lock_fails = 0;
+    uint32_t attempts = 0, lock_fails = 0, tries = 0;
     while (pending) {
       if (lane == 0) atomicAdd(&sm.stat[ST_ROUNDS], 1ull);
+      tries += (pending >> lane) & 1u;
       if (lock_fails) {  // randomized, growing back-off after a lost lock: breaks lock-step retries
         const uint32_t h = (me * 0x9E3779B1u) ^ (attempts * 0x85EBCA6Bu);
         __nanosleep((h >> 16) & ((64u << lock_fails) - 1u));
@@ -793,6 +815,7 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
       }
     }
     if (failed) break;
+    if (p.txn_aborts) p.txn_aborts[t] = tries - 1u;
   }
   __syncwarp();
   if (lane == 0) atomicAdd(&sm.done_warps, 1u);

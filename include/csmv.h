@@ -75,6 +75,15 @@ typedef struct csmv_bank_stream {
   const uint32_t* off;  /* [n_txn]  */
   const uint32_t* addr; /* [n_addr] */
   uint64_t n_addr;
+  /* Optional, zero = unused. */
+  uint32_t* txn_aborts;    /* out [n_txn]: failed attempts of each transaction (same memory
+                              kind as op: host for csmv_bank_run, device for _run_device)    */
+  uint32_t split_round;    /* > 0: rounds [split_round, n_txn/32) form a deferred queue that
+                              only the first deferred_warps client warps of the grid serve, so
+                              at most that many of its rounds run at once (a scheduler's
+                              likely-conflicting transactions); they serve the main queue
+                              [0, split_round) once it is empty                              */
+  uint32_t deferred_warps;
 } csmv_bank_stream;
 
 /* Account-choice distributions for the workload generator. */

@@ -15,14 +15,17 @@ def c1_workload(n_txn=8 * 128 * 256, seed=1, **kw):
     return cg.bank_workload(n_acc, n_txn, **d)
 
 
-def run_checked(w, *, init_value=1000, check=True, **cfg):
-    """Run workload w on a fresh bank; returns (stats, stream, bank outputs); asserts exactness."""
-    s = cg.generate(w)
+def run_checked(w, *, init_value=1000, check=True, stream=None, txn_aborts=None, split_round=0,
+                deferred_warps=0, **cfg):
+    """Run workload w (or a given stream over its accounts) on a fresh bank; returns (stats,
+    stream, bank outputs); asserts exactness."""
+    s = cg.generate(w) if stream is None else stream
     cfg.setdefault("max_txn", w.n_txn)
     depth = cfg.setdefault("version_depth", 4)
     with cg.Bank(n_accounts=w.n_accounts, init_value=init_value, **cfg) as bank:
         bank.load()
-        st = bank.run(s)
+        st = bank.run(s, txn_aborts=txn_aborts, split_round=split_round,
+                      deferred_warps=deferred_warps)
         log_txn, outcome, result = bank.log(w.n_txn, st.final_ts)
         slots = bank.versions()
     assert st.error == 0
@@ -57,3 +60,19 @@ def memcd_run_checked(cache, req, *, check=True, tick=None):
         orc.memcd_check(req.kind, req.key, req.val, t, cache.cfg.n_sets, table0, base, log_txn,
                         outcome, found, val_out, tags, recs)
     return found, val_out, st
+
+
+def defer_plan(s, risky):
+    """Permutation putting the update transactions flagged risky into a deferred queue at the
+    end of the stream (rounds stay uniform in kind). Returns (permuted stream, split_round)."""
+    n = s.n_txn
+    rr = np.repeat((s.op[::32] & 3) == 0, 32)
+    idx = np.arange(n)
+    upd = idx[~rr]
+    rk = risky[upd]
+    safe_u, risky_u = upd[~rk], upd[rk]
+    pad = (-len(risky_u)) % 32
+    main = np.concatenate([idx[rr], safe_u[pad:]])
+    perm = np.concatenate([main, risky_u, safe_u[:pad]])
+    return cg.Stream(np.ascontiguousarray(s.op[perm]), np.ascontiguousarray(s.off[perm]),
+                     s.addr), len(main) // 32

@@ -12,7 +12,7 @@ import pytest
 
 import csmv_gb300 as cg
 import oracle as orc
-from gpu_util import c1_workload, run_checked
+from gpu_util import c1_workload, defer_plan, run_checked
 
 pytestmark = pytest.mark.gpu
 
@@ -169,3 +169,26 @@ def test_driver_reference_command_line():
     fields = out.stdout.strip().split("\t")
     assert len(fields) == 6 + 17 + 4
     assert float(fields[1]) > 0 and 0.0 <= float(fields[0]) < 100.0
+
+
+@pytest.mark.parametrize("deferred_warps", [1, 7, 64])
+def test_deferred_queue_and_per_transaction_aborts_exact(deferred_warps):
+    """A stream whose hot-account transfers sit in a deferred queue served by a few warps runs
+    exactly (serial replay), and the per-transaction failed-attempt counts add up to the
+    aborts the statistics report."""
+    w = c1_workload(n_txn=32 * 1024, n_accounts=8192, dist=cg.DIST_HOTSPOT, hot_frac=0.01,
+                    hot_prob=0.5, seed=4)
+    s = cg.generate(w)
+    hot = np.zeros(w.n_accounts, bool)
+    cnt = np.bincount(s.addr, minlength=w.n_accounts)
+    hot[cnt > 8 * cnt.mean()] = True
+    risky = hot[s.addr[s.off]] | hot[s.addr[s.off + 1]]
+    ps, split = defer_plan(s, risky)
+    assert 0 < split < w.n_txn // 32
+    ab = np.zeros(w.n_txn, np.uint32)
+    st, _, _ = run_checked(w, stream=ps, txn_aborts=ab, split_round=split,
+                           deferred_warps=deferred_warps, ctas=16, client_warps=4)
+    assert int(ab.sum()) == st.aborts
+    ab0 = np.zeros(w.n_txn, np.uint32)
+    st0, _, _ = run_checked(w, txn_aborts=ab0, ctas=16, client_warps=4)
+    assert int(ab0.sum()) == st0.aborts and st0.aborts > 0
