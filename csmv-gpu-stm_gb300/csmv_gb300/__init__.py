@@ -142,6 +142,14 @@ def lib() -> C.CDLL:
         "csmv_memcd_device_info": (I32, [P, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                          C.POINTER(C.c_int), C.POINTER(C.c_size_t)]),
         "csmv_memcd_destroy": (None, [P]),
+        "csmv_mlp_create": (I32, [C.c_int32, C.c_uint64, C.POINTER(P)]),
+        "csmv_mlp_set_params": (I32, [P, P]),
+        "csmv_mlp_get_params": (I32, [P, P]),
+        "csmv_mlp_forward": (I32, [P, U32, P, P]),
+        "csmv_mlp_grad": (I32, [P, U32, P, P, C.POINTER(C.c_float)]),
+        "csmv_mlp_get_grads": (I32, [P, P]),
+        "csmv_mlp_adam_step": (I32, [P, C.c_float]),
+        "csmv_mlp_destroy": (None, [P]),
         "csmv_pinned_alloc": (I32, [C.c_size_t, C.POINTER(P)]),
         "csmv_pinned_free": (None, [P]),
         "csmv_last_error": (C.c_char_p, []),
@@ -461,6 +469,66 @@ class Memcd:
                                             C.byref(d)), "csmv_memcd_device_info")
         return {"n_sms": a.value, "ctas": b.value, "threads_per_cta": c_.value,
                 "device_bytes": d.value}
+
+
+# ---------------------------------------------------------------------------------------------
+# conflict predictor network
+# ---------------------------------------------------------------------------------------------
+
+MLP_IN, MLP_HIDDEN, MLP_PARAMS = 64, 128, 24964
+
+
+class Mlp:
+    """The conflict predictor network on one GPU (csmv_mlp_*). Sample arrays are device
+    pointers (ints): features bf16 [n][64], labels and outputs fp32 [n]."""
+
+    def __init__(self, seed: int = 1, device: int = 0):
+        h = C.c_void_p()
+        _check(lib().csmv_mlp_create(device, seed, C.byref(h)), "csmv_mlp_create")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            lib().csmv_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def params(self) -> np.ndarray:
+        out = np.empty(MLP_PARAMS, np.float32)
+        _check(lib().csmv_mlp_get_params(self._h, _ptr(out)), "csmv_mlp_get_params")
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.shape == (MLP_PARAMS,)
+        _check(lib().csmv_mlp_set_params(self._h, _ptr(p)), "csmv_mlp_set_params")
+
+    def grads(self) -> np.ndarray:
+        out = np.empty(MLP_PARAMS, np.float32)
+        _check(lib().csmv_mlp_get_grads(self._h, _ptr(out)), "csmv_mlp_get_grads")
+        return out
+
+    def forward(self, n: int, dev_x: int, dev_p: int) -> None:
+        _check(lib().csmv_mlp_forward(self._h, n, dev_x, dev_p), "csmv_mlp_forward")
+
+    def grad(self, n: int, dev_x: int, dev_y: int) -> float:
+        loss = C.c_float()
+        _check(lib().csmv_mlp_grad(self._h, n, dev_x, dev_y, C.byref(loss)), "csmv_mlp_grad")
+        return loss.value
+
+    def adam_step(self, lr: float) -> None:
+        _check(lib().csmv_mlp_adam_step(self._h, lr), "csmv_mlp_adam_step")
 
 
 def cuda_device_present() -> bool:

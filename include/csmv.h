@@ -343,6 +343,33 @@ csmv_status csmv_memcd_device_info(csmv_memcd_t* h, int* n_sms, int* ctas, int* 
                                    size_t* device_bytes);
 void csmv_memcd_destroy(csmv_memcd_t* h);
 
+/* ------------------------------------------------------------------------------------------
+ * Conflict predictor network (no counterpart in the reference; the learned scheduler below
+ * uses it). 64 input features -> 128 -> 128 -> 1, ReLU, ReLU, sigmoid = probability that a
+ * transaction aborts. Weights are kept in bf16 for the kernels (rounded from fp32 master
+ * copies), arithmetic accumulates in fp32; training minimises the mean binary cross-entropy
+ * with Adam. Parameter block (fp32, CSMV_MLP_PARAMS floats):
+ *   W1 [64][128] | b1 [128] | W2 [128][128] | b2 [128] | w3 [128] | b3 [1] | 3 zeros
+ * Features are bf16 [n][64]; labels fp32 [n] in {0, 1}. Device pointers are dev_*.
+ * ------------------------------------------------------------------------------------------ */
+#define CSMV_MLP_IN 64
+#define CSMV_MLP_HIDDEN 128
+#define CSMV_MLP_PARAMS 24964
+typedef struct csmv_mlp_t csmv_mlp_t;
+csmv_status csmv_mlp_create(int32_t device, uint64_t seed, csmv_mlp_t** out);
+csmv_status csmv_mlp_set_params(csmv_mlp_t* m, const float* host_params); /* resets Adam */
+csmv_status csmv_mlp_get_params(csmv_mlp_t* m, float* host_params);
+/* dev_p[i] = predicted abort probability of sample i */
+csmv_status csmv_mlp_forward(csmv_mlp_t* m, uint32_t n, const uint16_t* dev_x, float* dev_p);
+/* Adds the gradient of the mean loss over the n samples to the handle's accumulator;
+ * *host_loss (optional) = that mean loss. */
+csmv_status csmv_mlp_grad(csmv_mlp_t* m, uint32_t n, const uint16_t* dev_x, const float* dev_y,
+                          float* host_loss);
+csmv_status csmv_mlp_get_grads(csmv_mlp_t* m, float* host_grads);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) from the accumulated gradient, then clears it. */
+csmv_status csmv_mlp_adam_step(csmv_mlp_t* m, float lr);
+void csmv_mlp_destroy(csmv_mlp_t* m);
+
 /* Page-locked host buffers for staging streams (the e2e path copies from pinned memory).
  * Replaces CUDA_DUAL_ALLOC's cudaMallocHost half (memcachedGPU/cuda_util.h:50-60). */
 csmv_status csmv_pinned_alloc(size_t bytes, void** out);
