@@ -104,6 +104,32 @@ class MemcdConfig(C.Structure):
         "max_req", "spin_limit_log2")] + [("device", C.c_int32)]
 
 
+class SchedConfig(C.Structure):
+    _fields_ = [("n_accounts", C.c_uint32), ("max_txn", C.c_uint32),
+                ("probe_rounds_pct", C.c_uint32), ("train_steps", C.c_uint32),
+                ("lr", C.c_float), ("threshold", C.c_float), ("defer_threshold", C.c_float),
+                ("deferred_warps", C.c_uint32), ("seed", C.c_uint64), ("device", C.c_int32)]
+
+
+class SchedReport(C.Structure):
+    _fields_ = [("probe", Stats), ("planned", Stats), ("loss", C.c_float),
+                ("n_probe", C.c_uint32), ("n_planned", C.c_uint32), ("n_flagged", C.c_uint32),
+                ("n_deferred_rounds", C.c_uint32), ("train_ms", C.c_double),
+                ("plan_ms", C.c_double)]
+
+    @property
+    def commits(self) -> int:
+        return self.probe.commits + self.planned.commits
+
+    @property
+    def aborts(self) -> int:
+        return self.probe.aborts + self.planned.aborts
+
+    @property
+    def kernel_ms(self) -> float:
+        return self.probe.kernel_ms + self.planned.kernel_ms
+
+
 _lib = None
 
 
@@ -150,6 +176,14 @@ def lib() -> C.CDLL:
         "csmv_mlp_get_grads": (I32, [P, P]),
         "csmv_mlp_adam_step": (I32, [P, C.c_float]),
         "csmv_mlp_destroy": (None, [P]),
+        "csmv_sched_config_default": (None, [C.POINTER(SchedConfig)]),
+        "csmv_sched_create": (I32, [C.POINTER(SchedConfig), C.POINTER(P)]),
+        "csmv_sched_run": (I32, [P, P, C.POINTER(BankStream), C.POINTER(SchedReport)]),
+        "csmv_sched_probe": (I32, [P, P, C.POINTER(BankStream), C.POINTER(SchedReport)]),
+        "csmv_sched_plan_run": (I32, [P, P, C.POINTER(BankStream), C.POINTER(SchedReport)]),
+        "csmv_sched_read_plan": (I32, [P, P, U32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+        "csmv_sched_mlp": (P, [P]),
+        "csmv_sched_destroy": (None, [P]),
         "csmv_pinned_alloc": (I32, [C.c_size_t, C.POINTER(P)]),
         "csmv_pinned_free": (None, [P]),
         "csmv_last_error": (C.c_char_p, []),
@@ -529,6 +563,73 @@ class Mlp:
 
     def adam_step(self, lr: float) -> None:
         _check(lib().csmv_mlp_adam_step(self._h, lr), "csmv_mlp_adam_step")
+
+
+# ---------------------------------------------------------------------------------------------
+# learned conflict scheduler
+# ---------------------------------------------------------------------------------------------
+
+def sched_config(**kw) -> SchedConfig:
+    cfg = SchedConfig()
+    lib().csmv_sched_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        if not hasattr(cfg, k):
+            raise KeyError(f"unknown scheduler config field {k}")
+        setattr(cfg, k, v)
+    return cfg
+
+
+class Scheduler:
+    """The learned conflict scheduler (csmv_sched_*) in front of a Bank. Chunks are device
+    streams (BankStream with device pointers)."""
+
+    def __init__(self, cfg: SchedConfig | None = None, **kw):
+        self.cfg = cfg if cfg is not None else sched_config(**kw)
+        h = C.c_void_p()
+        _check(lib().csmv_sched_create(C.byref(self.cfg), C.byref(h)), "csmv_sched_create")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            lib().csmv_sched_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _call(self, name: str, bank: Bank, dev_stream: BankStream) -> SchedReport:
+        rep = SchedReport()
+        rc = getattr(lib(), name)(self._h, bank._h, C.byref(dev_stream), C.byref(rep))
+        bank.last_stats = rep.planned if name != "csmv_sched_probe" else rep.probe
+        _check(rc, name)
+        return rep
+
+    def run(self, bank: Bank, dev_stream: BankStream) -> SchedReport:
+        return self._call("csmv_sched_run", bank, dev_stream)
+
+    def probe(self, bank: Bank, dev_stream: BankStream) -> SchedReport:
+        return self._call("csmv_sched_probe", bank, dev_stream)
+
+    def plan_run(self, bank: Bank, dev_stream: BankStream) -> SchedReport:
+        return self._call("csmv_sched_plan_run", bank, dev_stream)
+
+    def plan(self, n: int):
+        """(perm, probe_rounds, split_round) of the last planned run."""
+        perm = np.empty(max(1, n), np.uint32)
+        pr, sp = C.c_uint32(), C.c_uint32()
+        _check(lib().csmv_sched_read_plan(self._h, _ptr(perm), max(1, n), C.byref(pr), C.byref(sp)),
+               "csmv_sched_read_plan")
+        n1 = n - 32 * pr.value
+        return perm[:n1], pr.value, sp.value
 
 
 def cuda_device_present() -> bool:

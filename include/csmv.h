@@ -370,6 +370,63 @@ csmv_status csmv_mlp_get_grads(csmv_mlp_t* m, float* host_grads);
 csmv_status csmv_mlp_adam_step(csmv_mlp_t* m, float lr);
 void csmv_mlp_destroy(csmv_mlp_t* m);
 
+/* ------------------------------------------------------------------------------------------
+ * Learned conflict scheduler (no counterpart in the reference). It reorders a chunk of a bank
+ * stream before the unchanged commit engine runs it - every transaction is still validated by
+ * the engine, so results stay exact - to keep transfers that are likely to conflict apart:
+ *  1. probe: the first probe_rounds_pct % of the chunk's rounds run in stream order, with
+ *     per-transaction abort counts; their transfers label the network's training data
+ *     (aborted or not) and refresh per-range abort rates; train_steps Adam steps follow;
+ *  2. plan: the network scores the remaining transfers from 64 features (hashed access counts
+ *     of the accounts in the chunk, recent abort rates of their ranges); a transfer scoring
+ *     above threshold is keyed by its more frequent written account, and the k-th of c
+ *     transfers with one key is placed at (k + u)/c of the chunk (u a hash in [0, 1)), the
+ *     others at u; read-only rounds are interleaved evenly; transfers scoring above
+ *     defer_threshold go to the engine's deferred queue (deferred_warps warps). The planned
+ *     rounds run as one engine call.
+ * Streams are device-resident (csmv_bank_run_device); the bank needs max_txn >= chunk size.
+ * ------------------------------------------------------------------------------------------ */
+typedef struct csmv_sched_config {
+  uint32_t n_accounts;        /* accounts of the bank (range bins of the abort-rate features) */
+  uint32_t max_txn;           /* largest chunk, multiple of 32                                */
+  uint32_t probe_rounds_pct;  /* % of each chunk's rounds run in stream order to label data   */
+  uint32_t train_steps;       /* Adam steps per chunk on the probe slice                      */
+  float lr;                   /* Adam learning rate                                           */
+  float threshold;            /* predicted abort probability above which a transfer is spaced */
+  float defer_threshold;      /* above this it is deferred (> 1 = never)                      */
+  uint32_t deferred_warps;    /* warps serving the deferred queue                             */
+  uint64_t seed;
+  int32_t device;
+} csmv_sched_config;
+
+typedef struct csmv_sched_report {
+  csmv_stats probe;           /* engine statistics of the probe run                          */
+  csmv_stats planned;         /* ... and of the planned run                                  */
+  float loss;                 /* mean cross-entropy on the probe slice before this chunk's steps */
+  uint32_t n_probe, n_planned, n_flagged, n_deferred_rounds;
+  double train_ms, plan_ms;   /* device time of training / of features, inference and planning */
+} csmv_sched_report;
+
+typedef struct csmv_sched_t csmv_sched_t;
+void csmv_sched_config_default(csmv_sched_config* cfg);
+csmv_status csmv_sched_create(const csmv_sched_config* cfg, csmv_sched_t** out);
+/* Both steps on one chunk (dev_stream: device pointers). */
+csmv_status csmv_sched_run(csmv_sched_t* s, csmv_bank_t* bank, const csmv_bank_stream* dev_stream,
+                           csmv_sched_report* out);
+/* The two steps separately (same chunk, in this order), so a caller can read the engine's
+ * commit log after each run. */
+csmv_status csmv_sched_probe(csmv_sched_t* s, csmv_bank_t* bank,
+                             const csmv_bank_stream* dev_stream, csmv_sched_report* out);
+csmv_status csmv_sched_plan_run(csmv_sched_t* s, csmv_bank_t* bank,
+                                const csmv_bank_stream* dev_stream, csmv_sched_report* out);
+/* Last plan: host_perm[i] = chunk index of the transaction the planned run executed as its
+ * i-th (n >= chunk size - 32 * probe_rounds); probe_rounds / split_round as used. */
+csmv_status csmv_sched_read_plan(csmv_sched_t* s, uint32_t* host_perm, uint32_t n,
+                                 uint32_t* probe_rounds, uint32_t* split_round);
+/* The scheduler's network (owned by the scheduler). */
+csmv_mlp_t* csmv_sched_mlp(csmv_sched_t* s);
+void csmv_sched_destroy(csmv_sched_t* s);
+
 /* Page-locked host buffers for staging streams (the e2e path copies from pinned memory).
  * Replaces CUDA_DUAL_ALLOC's cudaMallocHost half (memcachedGPU/cuda_util.h:50-60). */
 csmv_status csmv_pinned_alloc(size_t bytes, void** out);

@@ -76,3 +76,15 @@ def defer_plan(s, risky):
     perm = np.concatenate([main, risky_u, safe_u[:pad]])
     return cg.Stream(np.ascontiguousarray(s.op[perm]), np.ascontiguousarray(s.off[perm]),
                      s.addr), len(main) // 32
+
+
+def to_device(torch, s):
+    """Device copy of a host stream: (BankStream with device pointers, tensors to keep alive)."""
+    d = [torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).cuda() for a in (s.op, s.off, s.addr)]
+    return cg.BankStream(s.n_txn, d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(),
+                         int(s.addr.shape[0])), d
+
+
+def sub_stream(s, lo, hi):
+    """Transactions [lo, hi) of a host stream (addresses shared)."""
+    return cg.Stream(np.ascontiguousarray(s.op[lo:hi]), np.ascontiguousarray(s.off[lo:hi]), s.addr)
