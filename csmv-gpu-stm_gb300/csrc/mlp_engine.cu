@@ -44,9 +44,6 @@ uint64_t splitmix(uint64_t& s) {
 }
 }  // namespace
 
-// Shared-memory bytes the network kernels need (the scheduler launches them too).
-size_t csmv_mlp_smem_bytes() { return sizeof(MlpSmem); }
-
 extern "C" csmv_status csmv_mlp_create(int32_t device, uint64_t seed, csmv_mlp_t** out) {
   if (!out) return CSMV_ERR_INVALID_ARG;
   *out = nullptr;
@@ -74,11 +71,15 @@ extern "C" csmv_status csmv_mlp_create(int32_t device, uint64_t seed, csmv_mlp_t
     if ((st = cuda_status(cudaMalloc(a.p, a.bytes), "cudaMalloc")) != CSMV_OK) return fail(st);
   if ((st = cuda_status(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream")) != CSMV_OK)
     return fail(st);
-  for (auto* k : {(const void*)mlp_forward_kernel, (const void*)mlp_grad_kernel})
-    if ((st = cuda_status(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)sizeof(MlpSmem)),
-                          "cudaFuncSetAttribute")) != CSMV_OK)
-      return fail(st);
+  if ((st = cuda_status(cudaFuncSetAttribute((const void*)mlp_grad_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sizeof(MlpSmem)),
+                        "cudaFuncSetAttribute")) != CSMV_OK ||
+      (st = cuda_status(cudaFuncSetAttribute((const void*)mlp_forward_tc_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sizeof(MlpTcSmem)),
+                        "cudaFuncSetAttribute")) != CSMV_OK)
+    return fail(st);
   // uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights, zero biases
   std::vector<float> p(kMlpParams, 0.f);
   uint64_t s = seed;
@@ -129,11 +130,12 @@ extern "C" csmv_status csmv_mlp_get_grads(csmv_mlp_t* h, float* host_grads) {
 csmv_status csmv_mlp_launch_forward(csmv_mlp_t* h, uint32_t n, const void* dev_x, float* dev_p,
                                     cudaStream_t stream) {
   if (n == 0) return CSMV_OK;
-  const uint32_t tiles = (n + kMlpTile - 1) / kMlpTile;
-  const uint32_t grid = tiles < (uint32_t)h->n_sms ? tiles : (uint32_t)h->n_sms;
-  mlp_forward_kernel<<<grid, kMlpThreads, sizeof(MlpSmem), stream>>>(
+  // two 104 KB CTAs per SM
+  const uint32_t tiles = (n + kTcTile - 1) / kTcTile, cap = 2u * (uint32_t)h->n_sms;
+  const uint32_t grid = tiles < cap ? tiles : cap;
+  mlp_forward_tc_kernel<<<grid, 256, sizeof(MlpTcSmem), stream>>>(
       static_cast<const __nv_bfloat16*>(dev_x), n, h->w1, h->w2, h->w3, h->master, dev_p);
-  return cuda_status(cudaGetLastError(), "mlp_forward_kernel");
+  return cuda_status(cudaGetLastError(), "mlp_forward_tc_kernel");
 }
 
 csmv_status csmv_mlp_launch_grad(csmv_mlp_t* h, uint32_t n, const void* dev_x, const float* dev_y,

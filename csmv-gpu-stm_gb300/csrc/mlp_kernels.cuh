@@ -6,8 +6,10 @@
 // fp32. A CTA of 256 threads works on tiles of 64 samples with every operand in shared memory;
 // thread (ty, tx) = (tid / 16, tid % 16) owns samples 4ty..4ty+3 x hidden units tx + 16b
 // (b < 8) of an activation tile (interleaved so a warp's weight reads hit 16 distinct banks).
-// The tile GEMMs run on the FP32 pipes: the whole network is ~25 K multiply-adds per sample,
-// well under 1 % of the per-transaction time of the commit kernel whose input it schedules.
+// Inference (every planned transaction) runs on the tensor cores (mlp_forward_tc_kernel, bf16
+// warp MMAs with fp32 accumulation); training (the probe slice, a few percent of the chunk)
+// runs its fused forward + backward tile GEMMs on the FP32 pipes. Both feed layer 2 with bf16
+// activations, so they compute the same network.
 #pragma once
 #include <cuda_bf16.h>
 
@@ -29,7 +31,7 @@ struct MlpSmem {
   float w2[kMlpHid * kHs];       // [i][j], row stride kHs
   float b1[kMlpHid], b2[kMlpHid], w3[kMlpHid];
   float x[kMlpTile * kXs];       // [s][k]
-  float h1[kMlpTile * kHs];      // [s][i] post-ReLU
+  float h1[kMlpTile * kHs];      // [s][i] post-ReLU, rounded to bf16
   float h2[kMlpTile * kHs];      // [s][j] post-ReLU, then dL/dh2 pre-activation
   float dz[kMlpTile];
   float b3;
@@ -84,7 +86,8 @@ __device__ __forceinline__ void mlp_tile_forward(MlpSmem& sm, float zq[4]) {
 #pragma unroll
   for (int q = 0; q < 4; q++)
 #pragma unroll
-    for (int j = 0; j < 8; j++) sm.h1[(s0 + q) * kHs + tx + 16 * j] = fmaxf(acc[q][j], 0.f);
+    for (int j = 0; j < 8; j++)  // layer-2 operands are bf16, as on the tensor-core path
+      sm.h1[(s0 + q) * kHs + tx + 16 * j] = __bfloat162float(__float2bfloat16_rn(fmaxf(acc[q][j], 0.f)));
   __syncthreads();
   // layer 2: h2 = relu(h1 W2 + b2)
 #pragma unroll
@@ -120,29 +123,6 @@ __device__ __forceinline__ void mlp_tile_forward(MlpSmem& sm, float zq[4]) {
 }
 
 __device__ __forceinline__ float mlp_sigmoid(float z) { return 1.f / (1.f + expf(-z)); }
-
-// p[s] = sigmoid(z) for every sample. Grid-stride over tiles.
-__global__ void __launch_bounds__(kMlpThreads) mlp_forward_kernel(
-    const __nv_bfloat16* __restrict__ x, uint32_t n, const __nv_bfloat16* w1,
-    const __nv_bfloat16* w2, const __nv_bfloat16* w3, const float* master, float* __restrict__ p) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  MlpSmem& sm = *reinterpret_cast<MlpSmem*>(smem_raw);
-  mlp_load_weights(sm, w1, w2, w3, master);
-  const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
-  for (uint32_t s0 = blockIdx.x * kMlpTile; s0 < n; s0 += gridDim.x * kMlpTile) {
-    __syncthreads();  // weights loaded / previous tile's reads done
-    mlp_load_x(sm, x, s0, n);
-    __syncthreads();
-    float zq[4];
-    mlp_tile_forward(sm, zq);
-    if (tx == 0)
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const uint32_t s = s0 + ty * 4 + q;
-        if (s < n) p[s] = mlp_sigmoid(zq[q]);
-      }
-  }
-}
 
 // Gradient of the mean binary cross-entropy over n samples, accumulated (atomicAdd) into
 // grad[kMlpParams] (fp32, same packing as the master block); the summed loss into *loss.
@@ -323,6 +303,140 @@ __global__ void mlp_round_weights_kernel(const float* master, __nv_bfloat16* w1,
       w2[i - kOffW2] = __float2bfloat16_rn(w);
     else if (i >= kOffW3 && i < kOffB3)
       w3[i - kOffW3] = __float2bfloat16_rn(w);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Inference on the tensor cores: bf16 x bf16 -> fp32 warp MMAs (m16n8k16). A CTA of 8 warps
+// takes 128 samples; warp w owns samples 16w..16w+15 and all 128 hidden units (16 n-tiles), so
+// layer 2 reads only the layer-1 rows the same warp wrote. Weights sit in shared memory
+// transposed (unit-major, k contiguous) so every B fragment register is one 32-bit load; rows
+// are padded by 8 bf16 so a warp's fragment loads hit 32 distinct banks.
+// ---------------------------------------------------------------------------------------------
+constexpr int kTcTile = 128, kTcX = kMlpIn + 8, kTcH = kMlpHid + 8;
+
+struct MlpTcSmem {
+  __nv_bfloat16 w1t[kMlpHid * kTcX];   // [j][k]
+  __nv_bfloat16 w2t[kMlpHid * kTcH];   // [j][i]
+  __nv_bfloat16 x[kTcTile * kTcX];     // [s][k]
+  __nv_bfloat16 h1[kTcTile * kTcH];    // [s][i]
+  float b1[kMlpHid], b2[kMlpHid], w3[kMlpHid];
+  float b3;
+};
+
+__device__ __forceinline__ void mma_bf16_16816(float c[4], const uint32_t a[4], uint32_t b0,
+                                               uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t ld_pair(const __nv_bfloat16* p) {
+  return *reinterpret_cast<const uint32_t*>(p);
+}
+
+__global__ void __launch_bounds__(256) mlp_forward_tc_kernel(
+    const __nv_bfloat16* __restrict__ x, uint32_t n, const __nv_bfloat16* w1,
+    const __nv_bfloat16* w2, const __nv_bfloat16* w3, const float* master, float* __restrict__ p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  MlpTcSmem& sm = *reinterpret_cast<MlpTcSmem*>(smem_raw);
+  for (int i = threadIdx.x; i < kMlpIn * kMlpHid; i += blockDim.x)  // W1 [k][j] -> [j][k]
+    sm.w1t[(i % kMlpHid) * kTcX + i / kMlpHid] = w1[i];
+  for (int i = threadIdx.x; i < kMlpHid * kMlpHid; i += blockDim.x)  // W2 [i][j] -> [j][i]
+    sm.w2t[(i % kMlpHid) * kTcH + i / kMlpHid] = w2[i];
+  for (int i = threadIdx.x; i < kMlpHid; i += blockDim.x) {
+    sm.b1[i] = master[kOffB1 + i];
+    sm.b2[i] = master[kOffB2 + i];
+    sm.w3[i] = __bfloat162float(w3[i]);
+  }
+  if (threadIdx.x == 0) sm.b3 = master[kOffB3];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, g = lane / 4, tig = lane % 4;
+  const int r0 = warp * 16;  // this warp's rows
+  for (uint32_t s0 = blockIdx.x * kTcTile; s0 < n; s0 += gridDim.x * kTcTile) {
+    __syncthreads();
+    // x tile: 128 rows x 128 bytes, 16-byte pieces
+    for (int i = threadIdx.x; i < kTcTile * 8; i += blockDim.x) {
+      const uint32_t s = i / 8, q = i % 8;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (s0 + s < n) v = reinterpret_cast<const uint4*>(x + (size_t)(s0 + s) * kMlpIn)[q];
+      *reinterpret_cast<uint4*>(&sm.x[s * kTcX + q * 8]) = v;
+    }
+    __syncthreads();
+    float acc[16][4];
+    // layer 1
+#pragma unroll
+    for (int nt = 0; nt < 16; nt++) {
+      const int c = nt * 8 + tig * 2;
+      acc[nt][0] = acc[nt][2] = sm.b1[c];
+      acc[nt][1] = acc[nt][3] = sm.b1[c + 1];
+    }
+#pragma unroll
+    for (int ks = 0; ks < kMlpIn / 16; ks++) {
+      uint32_t a[4];
+      const __nv_bfloat16* xa = &sm.x[(r0 + g) * kTcX + ks * 16 + tig * 2];
+      a[0] = ld_pair(xa);
+      a[1] = ld_pair(xa + 8 * kTcX);
+      a[2] = ld_pair(xa + 8);
+      a[3] = ld_pair(xa + 8 * kTcX + 8);
+#pragma unroll
+      for (int nt = 0; nt < 16; nt++) {
+        const __nv_bfloat16* wb = &sm.w1t[(nt * 8 + g) * kTcX + ks * 16 + tig * 2];
+        mma_bf16_16816(acc[nt], a, ld_pair(wb), ld_pair(wb + 8));
+      }
+    }
+    // ReLU, bf16, into this warp's rows of h1
+#pragma unroll
+    for (int nt = 0; nt < 16; nt++) {
+      const int c = nt * 8 + tig * 2;
+      *reinterpret_cast<__nv_bfloat162*>(&sm.h1[(r0 + g) * kTcH + c]) =
+          __floats2bfloat162_rn(fmaxf(acc[nt][0], 0.f), fmaxf(acc[nt][1], 0.f));
+      *reinterpret_cast<__nv_bfloat162*>(&sm.h1[(r0 + g + 8) * kTcH + c]) =
+          __floats2bfloat162_rn(fmaxf(acc[nt][2], 0.f), fmaxf(acc[nt][3], 0.f));
+    }
+    __syncwarp();
+    // layer 2
+#pragma unroll
+    for (int nt = 0; nt < 16; nt++) {
+      const int c = nt * 8 + tig * 2;
+      acc[nt][0] = acc[nt][2] = sm.b2[c];
+      acc[nt][1] = acc[nt][3] = sm.b2[c + 1];
+    }
+#pragma unroll
+    for (int ks = 0; ks < kMlpHid / 16; ks++) {
+      uint32_t a[4];
+      const __nv_bfloat16* ha = &sm.h1[(r0 + g) * kTcH + ks * 16 + tig * 2];
+      a[0] = ld_pair(ha);
+      a[1] = ld_pair(ha + 8 * kTcH);
+      a[2] = ld_pair(ha + 8);
+      a[3] = ld_pair(ha + 8 * kTcH + 8);
+#pragma unroll
+      for (int nt = 0; nt < 16; nt++) {
+        const __nv_bfloat16* wb = &sm.w2t[(nt * 8 + g) * kTcH + ks * 16 + tig * 2];
+        mma_bf16_16816(acc[nt], a, ld_pair(wb), ld_pair(wb + 8));
+      }
+    }
+    // layer 3: rows g and g+8, reduced over the 4 lanes of the group
+    float z0 = 0.f, z1 = 0.f;
+#pragma unroll
+    for (int nt = 0; nt < 16; nt++) {
+      const int c = nt * 8 + tig * 2;
+      z0 = fmaf(fmaxf(acc[nt][0], 0.f), sm.w3[c], z0);
+      z0 = fmaf(fmaxf(acc[nt][1], 0.f), sm.w3[c + 1], z0);
+      z1 = fmaf(fmaxf(acc[nt][2], 0.f), sm.w3[c], z1);
+      z1 = fmaf(fmaxf(acc[nt][3], 0.f), sm.w3[c + 1], z1);
+    }
+#pragma unroll
+    for (int o = 1; o <= 2; o <<= 1) {
+      z0 += __shfl_xor_sync(0xFFFFFFFFu, z0, o);
+      z1 += __shfl_xor_sync(0xFFFFFFFFu, z1, o);
+    }
+    if (tig == 0) {
+      const uint32_t sa = s0 + r0 + g, sb = sa + 8;
+      if (sa < n) p[sa] = mlp_sigmoid(z0 + sm.b3);
+      if (sb < n) p[sb] = mlp_sigmoid(z1 + sm.b3);
+    }
   }
 }
 

@@ -52,7 +52,7 @@ extern "C" void csmv_sched_config_default(csmv_sched_config* c) {
   std::memset(c, 0, sizeof(*c));
   c->n_accounts = 1u << 20;
   c->max_txn = 1u << 20;
-  c->probe_rounds_pct = 12;
+  c->probe_rounds_pct = 5;
   c->train_steps = 2;
   c->lr = 3e-3f;
   c->threshold = 0.05f;

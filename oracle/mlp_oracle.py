@@ -1,9 +1,9 @@
 """CPU oracle of the conflict predictor network (float64 numpy). TEST INFRASTRUCTURE ONLY.
 
 Restates the network the CUDA kernels compute (csmv-gpu-stm_gb300/csrc/mlp_kernels.cuh):
-64 -> 128 -> 128 -> 1 with ReLU, ReLU, sigmoid, the weights W1, W2, w3 rounded to bf16 (round to
-nearest even) as the kernels use them, biases in fp32, and the gradient of the mean binary
-cross-entropy, so the kernels' forward and backward can be checked against it. Only tests/
+64 -> 128 -> 128 -> 1 with ReLU, ReLU, sigmoid, the weights W1, W2, w3 and the layer-1
+activations rounded to bf16 (round to nearest even) as the kernels use them, biases in fp32,
+and the gradient of the mean binary cross-entropy (straight through the activation rounding), so the kernels' forward and backward can be checked against it. Only tests/
 import this module.
 """
 from __future__ import annotations
@@ -41,12 +41,16 @@ def unpack(params):
             float(p[OFF_B3]))
 
 
-def forward(params, x):
-    """x: [n, 64] (already bf16-representable). Returns (p, cache)."""
+def forward(params, x, round_act=True):
+    """x: [n, 64] (already bf16-representable). Returns (p, cache). round_act=False keeps the
+    layer-1 activations in float64 (for checking the gradient by finite differences)."""
     w1, b1, w2, b2, w3, b3 = unpack(params)
     x = np.asarray(x, np.float64)
     a1 = x @ w1 + b1
+    # the kernels feed layer 2 with bf16 activations
     h1 = np.maximum(a1, 0.0)
+    if round_act:
+        h1 = bf16_round(h1.astype(np.float32)).astype(np.float64)
     a2 = h1 @ w2 + b2
     h2 = np.maximum(a2, 0.0)
     z = h2 @ w3 + b3
@@ -54,10 +58,10 @@ def forward(params, x):
     return p, (x, h1, h2, z, w2, w3)
 
 
-def loss_and_grads(params, x, y):
+def loss_and_grads(params, x, y, round_act=True):
     """Mean BCE and its gradient w.r.t. the parameter block (bf16 weights treated as the
     variables, i.e. the straight-through gradient the kernels compute)."""
-    p, (x, h1, h2, z, w2, w3) = forward(params, x)
+    p, (x, h1, h2, z, w2, w3) = forward(params, x, round_act)
     y = np.asarray(y, np.float64)
     n = x.shape[0]
     loss = float(np.mean(np.maximum(z, 0) - y * z + np.log1p(np.exp(-np.abs(z)))))

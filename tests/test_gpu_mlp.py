@@ -3,7 +3,9 @@
 the Adam update, and that training learns a separable labelling.
 
 Tolerances (fp32 accumulation of bf16 weights against float64 on the same bf16 weights):
-probabilities 2e-5 absolute; gradients 1e-4 relative to the gradient's max-norm, per entry."""
+probabilities 2e-5 absolute for 0/1 features (2e-4 for dense features, where a layer-1
+activation may round to the neighbouring bf16 value); gradients 1e-4 relative to the
+gradient's max-norm, per entry."""
 import numpy as np
 import pytest
 
@@ -44,7 +46,12 @@ def test_forward_and_gradient_match_oracle(n, dense):
         loss = m.grad(n, dx.data_ptr(), dy.data_ptr())
         g_gpu = m.grads().astype(np.float64)
     p_ref, _ = mo.forward(params, x)
-    np.testing.assert_allclose(p_gpu, p_ref, rtol=0, atol=2e-5)
+    # binary features (the scheduler's) give exactly representable layer-1 sums; with dense
+    # inputs an fp32 sum can land on the other side of a bf16 rounding boundary than the float64
+    # one, moving one activation by one bf16 step (2^-8 relative) and p by up to ~1e-4
+    np.testing.assert_allclose(p_gpu, p_ref, rtol=0, atol=2e-4 if dense else 2e-5)
+    if dense:
+        assert np.mean(np.abs(p_gpu - p_ref) > 2e-5) < 1e-3
     loss_ref, g_ref = mo.loss_and_grads(params, x, y)
     assert abs(loss - loss_ref) < 1e-4 * max(1.0, abs(loss_ref))
     scale = np.abs(g_ref).max()

@@ -35,7 +35,7 @@ def test_gradient_matches_finite_differences():
 
     # the oracle with bf16-exact weights equals the float64 function
     p = mo.bf16_round(p.astype(np.float32)).astype(np.float64)
-    _, g = mo.loss_and_grads(p.astype(np.float32), x, y)
+    _, g = mo.loss_and_grads(p.astype(np.float32), x, y, round_act=False)
     idx = np.concatenate([rng.integers(mo.OFF_W1, mo.OFF_B1, 20), rng.integers(mo.OFF_W2, mo.OFF_B2, 20),
                           np.arange(mo.OFF_W3, mo.OFF_W3 + 5), [mo.OFF_B3], [mo.OFF_B1 + 3]])
     for i in idx:
