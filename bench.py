@@ -1,23 +1,33 @@
 """Benchmark of the CSMV commit path on GB300 (contract: one JSON line from rank 0).
 
-Workload (the configuration the headline metric is quoted on): contended bank at scale -
-2^20 int32 accounts, Zipf(0.99) account choice, transfers read 4 / write 2, 20% read-only scans
-of 32 accounts, 2^24 transactions per step, persistent kernel over every SM. One step = one run
-of the whole stream through the engine; the account state carries over between steps.
+Workload (the configuration the headline metric is quoted on): the contended bank at scale -
+2^20 int32 accounts at 1000, Zipf(0.99) account choice, transfers that read 4 and write 2
+accounts (skipped when funds are short), 20 % read-only rounds summing 32 accounts. The stream
+is 2^24 transactions, seeded; a step is one batch of 2^20 consecutive transactions of it
+(batch i = transactions [i 2^20, (i+1) 2^20)), so warm-up and timed steps see different
+transactions and the account state carries over between steps. Stream arrays are larger than
+L2 (28 MB per batch), so no L2 flush is needed between steps.
 
-  value   committed tx/s with the stream resident in HBM (csmv_bank_run_device), device time of
-          the persistent kernel from CUDA events on the engine's own stream
-  e2e     committed tx/s through csmv_bank_run with pinned HOST buffers: host->device copy of the
-          stream and device->host read of the statistics inside the timed region
-  roofline  algorithmic bytes per committed transaction (16 B per versioned read, 12 B per
-          written item: 88 B per transfer, 512 B per 32-account scan) / kernel time vs the
-          measured HBM copy bandwidth (MEASURED_PEAKS.json)
-  cpu_baseline  the oracle's host-threaded lock-based execution of a bounded sample of the
-          same stream on this host's cores (the reference has no CPU implementation)
+Two arms run the same batches on separate banks:
+  plain    the commit engine alone (csmv_bank_run_device): every transfer through the stamp
+           protocol, client warps + per-CTA commit server on every SM
+  learned  the learned conflict scheduler in front of the same engine (csmv_sched_run): a probe
+           slice in stream order trains the conflict predictor, the predictor routes likely-
+           conflicting transfers to the serial lane and spaces the rest
+value = the learned arm's committed tx/s (GPU time of the whole step, inputs resident in HBM);
+e2e = the same through host buffers (pinned -> device copies and the statistics read inside
+the timed region). Both arms' throughput and abort rate are in "plain" / "learned".
 
---impl reference runs that CPU execution as the reference arm (the reference's own code is
-GPU-only; its CPU semantics are the oracle port). Multi-GPU: replicas only (no collective in the
-path); each rank runs its own instance, value sums the ranks' transactions over the max time.
+Extra sections: "hotspot" (1 % hot set drawing 30 % of the accesses, moving every 2^20
+transactions: learned vs plain), "uniform" (the same bank with uniform accounts, plain engine)
+and "memcd" (8-way cache of 2^20 sets, Zipf(0.99) keys over 4 M, 99 % GET rounds, 64 K-request
+batches: throughput and p50/p99 batch latency).
+
+--impl reference runs the reference arm: the path's CPU execution (the oracle port, striped
+locks on every host core) on the same batches. --case NAME runs one small invocation of one
+kernel for profiling (engine, serial, mlp, memcd, sched). Multi-GPU: replicas only (no
+collective on the path); each rank runs its own instance on its own GPU, value sums the ranks'
+transactions over the slowest rank's time.
 """
 from __future__ import annotations
 
@@ -36,11 +46,13 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "csmv-gpu-stm_gb300"))
 
 N_ACCOUNTS = 1 << 20
-N_TXN = 1 << 24
+STREAM_TXN = 1 << 24
+BATCH = 1 << 20
 WORKLOAD = dict(seed=2026, pr_read_pct=20, ro_reads=32, up_reads=4, amt_lo=1, amt_hi=10,
                 zipf_theta=0.99)
-B_UPDATE = 16 * 4 + 12 * 2
-B_RO = 16 * 32
+B_UPDATE = 16 * 4 + 12 * 2   # algorithmic bytes of a transfer: 4 versioned reads, 2 writes
+B_RO = 16 * 32               # a 32-account read-only scan
+SCHED = dict(serial_lane=1, defer_threshold=0.0, probe_every=4, probe_rounds_pct=2)
 
 
 def parse():
@@ -49,31 +61,20 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="csmv", choices=["csmv", "reference"])
-    ap.add_argument("--n-txn", type=int, default=N_TXN)
+    ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--dist", default="zipf", choices=["zipf", "uniform", "hotspot"])
     ap.add_argument("--client-warps", type=int, default=int(os.environ.get("CSMV_CLIENT_WARPS", 2)))
     ap.add_argument("--ctas", type=int, default=int(os.environ.get("CSMV_CTAS", 152)))
     ap.add_argument("--depth", type=int, default=int(os.environ.get("CSMV_DEPTH", 8)))
+    ap.add_argument("--case", default=None, choices=["engine", "serial", "mlp", "memcd", "sched"])
+    ap.add_argument("--no-extras", action="store_true", help="skip hotspot/uniform/memcd sections")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
 
-def dist_id(name):
-    import csmv_gb300 as cg
-    return {"zipf": cg.DIST_ZIPF, "uniform": cg.DIST_UNIFORM, "hotspot": cg.DIST_HOTSPOT}[name]
-
-
-def workload(args):
-    import csmv_gb300 as cg
-    return cg.bank_workload(N_ACCOUNTS, args.n_txn, dist=dist_id(args.dist), kind=cg.KIND_TRANSFER,
-                            **WORKLOAD)
-
-
 def dist_env():
-    rank = int(os.environ.get("RANK", 0))
-    world = int(os.environ.get("WORLD_SIZE", 1))
-    local = int(os.environ.get("LOCAL_RANK", 0))
-    return rank, world, local
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
 
 
 def reduce_max(x: float, world: int) -> float:
@@ -141,54 +142,310 @@ def peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def cpu_baseline(stream, args, sample_txn=1 << 21):
-    """Oracle's host-threaded lock-based execution of the first sample_txn transactions."""
+def generate_batches(dist: str, batch: int, count: int, pinned: bool = True, seed: int = None,
+                     **over):
+    """The first `count` batches of a seeded stream (the generator is counter-based, so a prefix
+    of the stream holds the same transactions as the whole stream)."""
+    import csmv_gb300 as cg
+    d = dict(WORKLOAD)
+    if seed is not None:
+        d["seed"] = seed
+    d.update(over)
+    dist_id = {"zipf": cg.DIST_ZIPF, "uniform": cg.DIST_UNIFORM, "hotspot": cg.DIST_HOTSPOT}[dist]
+    w = cg.bank_workload(N_ACCOUNTS, batch * count, dist=dist_id, kind=cg.KIND_TRANSFER, **d)
+    s = cg.generate(w, pinned=pinned)
+    return s, [cg.Stream(s.op[i * batch:(i + 1) * batch], s.off[i * batch:(i + 1) * batch], s.addr)
+               for i in range(count)]
+
+
+class DevBatch:
+    """A batch's op/off arrays staged in device memory (the address array is shared)."""
+
+    def __init__(self, torch, b):
+        self.t = [torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).cuda()
+                  for a in (b.op, b.off)]
+        self.n = b.n_txn
+
+    def stream(self, cg, addr_dev, n_addr):
+        return cg.BankStream(self.n, self.t[0].data_ptr(), self.t[1].data_ptr(),
+                             addr_dev.data_ptr(), n_addr)
+
+
+def launches_learned(rep) -> int:
+    """Kernels the scheduler and the engine launched for one chunk (see sched_engine.cu)."""
+    n = 1  # access counts
+    if rep.n_probe:
+        n += 1 + 1 + 2 + 4  # features, probe engine run, labels + rates, 2 x (grad + adam)
+    n += 2 + 2  # features and network forward; read-only flags and scan
+    if rep.n_planned:
+        n += 6  # keys, buckets, scan, scatter, read-only list, emit
+        n += 1 if rep.planned.commits else 0  # concurrent engine run
+        n += 1 if rep.n_serial else 0         # serial lane
+    return n
+
+
+def new_bank(cg, args, local, max_txn, **over):
+    kw = dict(n_accounts=N_ACCOUNTS, version_depth=args.depth, client_warps=args.client_warps,
+              ctas=args.ctas, max_txn=max_txn, log_commits=0, device=local)
+    kw.update(over)
+    bank = cg.Bank(**kw)
+    bank.load()
+    return bank
+
+
+# ---------------------------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------------------------
+
+def run_plain(cg, dev, addr_dev, n_addr, args, local, warm, timed):
+    bank = new_bank(cg, args, local, args.batch)
+    res = dict(ms=0.0, commits=0, aborts=0, ro=0, upd=0)
+    for i in range(warm + timed):
+        st = bank.run_device(dev[i].stream(cg, addr_dev, n_addr))
+        if i >= warm:
+            res["ms"] += st.kernel_ms
+            res["commits"] += st.commits
+            res["aborts"] += st.aborts
+            res["ro"] += st.commits_readonly
+            res["upd"] += st.commits_update + st.commits_nowrite
+    info = bank.device_info()
+    bank.close()
+    return res, info
+
+
+def run_learned(torch, cg, dev, addr_dev, n_addr, args, local, warm, timed):
+    bank = new_bank(cg, args, local, args.batch)
+    sched = cg.Scheduler(n_accounts=N_ACCOUNTS, max_txn=args.batch, device=local, **SCHED)
+    res = dict(wall=0.0, commits=0, aborts=0, launches=0, serial_ms=0.0, serial_txn=0,
+               plan_ms=0.0, train_ms=0.0)
+    for i in range(warm + timed):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rep = sched.run(bank, dev[i].stream(cg, addr_dev, n_addr))
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        if i >= warm:
+            res["wall"] += dt
+            res["commits"] += rep.commits
+            res["aborts"] += rep.aborts
+            res["launches"] += launches_learned(rep)
+            res["serial_ms"] += rep.serial.kernel_ms
+            res["serial_txn"] += rep.n_serial
+            res["plan_ms"] += rep.plan_ms
+            res["train_ms"] += rep.train_ms
+    sched.close()
+    bank.close()
+    return res
+
+
+def e2e_learned(torch, cg, host, s_addr, args, local, warm, timed):
+    """Host buffers through the public calls: each step copies the batch's op/off arrays and its
+    range of the address array from pinned host memory, runs the scheduler (which returns the
+    statistics to the host) and is timed on the host clock."""
+    bank = new_bank(cg, args, local, args.batch)
+    sched = cg.Scheduler(n_accounts=N_ACCOUNTS, max_txn=args.batch, device=local, **SCHED)
+    n = args.batch
+    d_op = torch.empty(n, dtype=torch.int32, device="cuda")
+    d_off = torch.empty(n, dtype=torch.int32, device="cuda")
+    d_addr = torch.empty(s_addr.shape[0], dtype=torch.int32, device="cuda")
+    h_addr = torch.from_numpy(s_addr.view(np.int32))
+    commits, wall, h2d = 0, 0.0, 0
+    for i in range(warm + timed):
+        b = host[i]
+        lo = int(b.off[0])
+        hi = int(b.off[-1]) + int((b.op[-1] >> 2) & 63)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d_op.copy_(torch.from_numpy(b.op.view(np.int32)), non_blocking=True)
+        d_off.copy_(torch.from_numpy(b.off.view(np.int32)), non_blocking=True)
+        d_addr[lo:hi].copy_(h_addr[lo:hi], non_blocking=True)
+        torch.cuda.synchronize()
+        ds = cg.BankStream(n, d_op.data_ptr(), d_off.data_ptr(), d_addr.data_ptr(),
+                           int(s_addr.shape[0]))
+        rep = sched.run(bank, ds)
+        dt = time.perf_counter() - t0
+        if i >= warm:
+            wall += dt
+            commits += rep.commits
+            h2d += b.op.nbytes + b.off.nbytes + (hi - lo) * 4
+    sched.close()
+    bank.close()
+    return commits, wall, h2d // max(1, timed)
+
+
+def hotspot_section(torch, cg, local):
+    """Learned vs plain on the shifting hotspot: 8 batches of 2^18 transactions."""
+    chunk, count = 1 << 18, 8
+    s, bs = generate_batches("hotspot", chunk, count, pinned=False, seed=3, pr_read_pct=10,
+                             ro_reads=8, up_reads=2, hot_frac=0.01, hot_prob=0.3,
+                             shift_every=1 << 20)
+    addr = torch.from_numpy(s.addr.view(np.int32)).cuda()
+    dev = [DevBatch(torch, b) for b in bs]
+    out = {}
+    for arm in ("plain", "learned"):
+        bank = cg.Bank(n_accounts=N_ACCOUNTS, version_depth=8, client_warps=2, ctas=152,
+                       max_txn=chunk, log_commits=0, device=local)
+        bank.load()
+        sched = cg.Scheduler(n_accounts=N_ACCOUNTS, max_txn=chunk, device=local) \
+            if arm == "learned" else None
+        c = a = 0
+        t = 0.0
+        for d in dev:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if sched is None:
+                st = bank.run_device(d.stream(cg, addr, s.addr.shape[0]))
+                c, a = c + st.commits, a + st.aborts
+            else:
+                r = sched.run(bank, d.stream(cg, addr, s.addr.shape[0]))
+                c, a = c + r.commits, a + r.aborts
+            torch.cuda.synchronize()
+            t += time.perf_counter() - t0
+        if sched is not None:
+            sched.close()
+        bank.close()
+        out[arm] = {"tx_s": c / t, "abort_rate": a / (a + c)}
+    out["workload"] = ("2^20 accounts, 1% hot set drawing 30% of the accesses, moving every 2^20 "
+                       "txn; 90% 2-account transfers, 10% read-only sums of 8; 8 batches of 2^18")
+    return out
+
+
+def uniform_section(torch, cg, args, local):
+    s, bs = generate_batches("uniform", args.batch, 4, pinned=False)
+    addr = torch.from_numpy(s.addr.view(np.int32)).cuda()
+    dev = [DevBatch(torch, b) for b in bs]
+    res, _ = run_plain(cg, dev, addr, s.addr.shape[0], args, local, 1, 3)
+    return {"tx_s": res["commits"] / (res["ms"] * 1e-3),
+            "abort_rate": res["aborts"] / (res["aborts"] + res["commits"]),
+            "workload": "same bank, uniform account choice, plain engine, 3 batches of 2^20"}
+
+
+def memcd_section(cg, local, n_batches=40):
+    """Cache: 2^20 sets x 8 ways, Zipf(0.99) keys over 4 M ids, 99 % GET rounds, 64 K-request
+    batches through csmv_memcd_run (host buffers); latency = wall time of one batch call."""
+    n = 1 << 16
+    cache = cg.Memcd(n_sets=1 << 20, client_warps=4, max_req=n, log_commits=0, device=local)
+    for i in range(8):  # fill
+        cache.run(cg.memcd_generate(cg.memcd_workload(1 << 22, n, seed=500 + i, get_pct=0)))
+    reqs = [cg.memcd_generate(cg.memcd_workload(1 << 22, n, seed=1000 + i, get_pct=99), pinned=True)
+            for i in range(n_batches)]
+    lat, kern, aborts, commits = [], [], 0, 0
+    for r in reqs:
+        _, _, st = cache.run(r)
+        lat.append(st.total_ms)
+        kern.append(st.kernel_ms)
+        aborts += st.aborts
+        commits += st.commits
+    cache.close()
+    lat, kern = np.array(lat[4:]), np.array(kern[4:])
+    return {"req_s": n * len(lat) / (lat.sum() * 1e-3),
+            "kernel_req_s": n * len(kern) / (kern.sum() * 1e-3),
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "abort_rate": aborts / max(1, aborts + commits),
+            "workload": "2^20 sets x 8 ways, 16 B keys / 32 B values, Zipf(0.99) over 4M keys, "
+                        "99% GET rounds, 64K-request batches, host buffers"}
+
+
+def cpu_baseline(bs, sample_txn=1 << 21):
+    """The oracle's CPU executions of a bounded sample of the same batches: striped locks on
+    every host core (reported) and one thread in stream order (for comparison)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as orc
-    n = min(sample_txn, stream.n_txn)
-    op, off = stream.op[:n], stream.off[:n]
+    op = np.concatenate([b.op for b in bs])[:sample_txn]
+    off = np.concatenate([b.off for b in bs])[:sample_txn]
+    addr = bs[0].addr
     init = np.full(N_ACCOUNTS, 1000, np.int32)
     threads = orc.cpu_threads()
-    best = None
-    for _ in range(3):
-        _, ns = orc.locked(op, off, stream.addr, N_ACCOUNTS, init, threads)
-        best = ns if best is None else min(best, ns)
+    best = min(orc.locked(op, off, addr, N_ACCOUNTS, init, threads)[1] for _ in range(3))
+    ser = min(orc.serial(op, off, addr, N_ACCOUNTS, init)[1] for _ in range(2))
+    n = op.shape[0]
     return {"value": n / (best * 1e-9), "unit": "committed tx/s", "cores": threads, "kind": "port",
-            "sample": f"first {n} transactions of the stream, striped-lock threads, best of 3"}
+            "sample": f"first {n} transactions of the stream, striped-lock threads on all cores, "
+                      f"best of 3", "single_thread_stream_order_tx_s": n / (ser * 1e-9)}
+
+
+def workload_name(args):
+    return (f"bank {args.dist}(0.99) 2^20 int32 accounts, transfers r4/w2, 20% read-only scans "
+            f"of 32; 2^24-txn stream in batches of {args.batch}")
 
 
 def run_reference(args, rank, world):
-    """Reference arm: the CPU execution of the path on the host cores (oracle port)."""
+    """Reference arm: the path's CPU execution (oracle port, striped locks, all host threads)."""
     if rank != 0:
         return
-    import csmv_gb300 as cg  # generator only (host code)
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as orc
-    sample = min(args.n_txn, 1 << 21)
-    w = workload(args)
-    w.n_txn = sample
-    s = cg.generate(w)
-    init = np.full(N_ACCOUNTS, 1000, np.int32)
+    s, bs = generate_batches(args.dist, args.batch, args.warmup + args.steps, pinned=False)
+    vals = np.full(N_ACCOUNTS, 1000, np.int32)
     threads = orc.cpu_threads()
-    for _ in range(args.warmup):
-        orc.locked(s.op, s.off, s.addr, N_ACCOUNTS, init, threads)
-    t = 0
-    for _ in range(args.steps):
-        _, ns = orc.locked(s.op, s.off, s.addr, N_ACCOUNTS, init, threads)
-        t += ns * 1e-9
-    v = sample * args.steps / t
-    line = {"impl": "reference", "metric": "committed tx/s", "value": v, "unit": "committed tx/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": f"bank {args.dist}(0.99) 2^20 accounts r4/w2, 20% RO scans of 32",
-                       "sample_txn": sample},
-            "cpu_baseline": {"value": v, "unit": "committed tx/s", "cores": threads, "kind": "port",
-                             "sample": f"{sample} transactions per step, striped-lock threads"},
-            "e2e": {"value": v, "unit": "committed tx/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
+    t, commits = 0.0, 0
+    for i, b in enumerate(bs):
+        vals, ns = orc.locked(b.op, b.off, b.addr, N_ACCOUNTS, vals, threads)
+        if i >= args.warmup:
+            t += ns * 1e-9
+            commits += b.n_txn
+    v = commits / t
+    print(json.dumps({
+        "impl": "reference", "metric": "committed tx/s", "value": v, "unit": "committed tx/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": workload_name(args)},
+        "cpu_baseline": {"value": v, "unit": "committed tx/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.batch} transactions per step, striped-lock threads"},
+        "e2e": {"value": v, "unit": "committed tx/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}))
 
+
+# ---------------------------------------------------------------------------------------------
+# profiling cases: one small invocation of one kernel (run under ncu)
+# ---------------------------------------------------------------------------------------------
+
+def run_case(args, local):
+    import torch
+
+    import csmv_gb300 as cg
+    torch.cuda.set_device(local)
+    if args.case in ("engine", "serial", "sched"):
+        dist = "uniform" if args.case == "engine" else "zipf"
+        n = (1 << 15) if args.case == "serial" else (1 << 18)
+        s, bs = generate_batches(dist, n, 2, pinned=False)
+        addr = torch.from_numpy(s.addr.view(np.int32)).cuda()
+        dev = [DevBatch(torch, b) for b in bs]
+        bank = new_bank(cg, args, local, n)
+        if args.case == "sched":
+            sched = cg.Scheduler(n_accounts=N_ACCOUNTS, max_txn=n, device=local, **SCHED)
+            for d in dev:
+                r = sched.run(bank, d.stream(cg, addr, s.addr.shape[0]))
+            sched.close()
+            out = {"case": "sched", "commits": r.commits}
+        else:
+            run = bank.run_device if args.case == "engine" else bank.run_serial_device
+            for d in dev:  # a warm-up launch, then the profiled one
+                st = run(d.stream(cg, addr, s.addr.shape[0]))
+            out = {"case": args.case, "commits": st.commits, "kernel_ms": st.kernel_ms}
+        bank.close()
+    elif args.case == "mlp":
+        n = 1 << 18
+        rng = np.random.default_rng(0)
+        x = (rng.random((n, 64)) < 0.2).astype(np.float32)
+        bits = (x.view(np.uint32) >> 16).astype(np.uint16).view(np.int16)  # 0/1 exact in bf16
+        dx = torch.from_numpy(bits).cuda()
+        dp = torch.zeros(n, dtype=torch.float32, device="cuda")
+        with cg.Mlp(seed=1, device=local) as m:
+            m.forward(n, dx.data_ptr(), dp.data_ptr())
+            m.forward(n, dx.data_ptr(), dp.data_ptr())
+        out = {"case": "mlp", "mean_p": float(dp.mean())}
+    else:
+        n = 1 << 16
+        with cg.Memcd(n_sets=1 << 20, client_warps=4, max_req=n, log_commits=0, device=local) as c:
+            c.run(cg.memcd_generate(cg.memcd_workload(1 << 22, n, seed=5, get_pct=0)))
+            _, _, st = c.run(cg.memcd_generate(cg.memcd_workload(1 << 22, n, seed=6, get_pct=99)))
+        out = {"case": "memcd", "commits": st.commits}
+    print(json.dumps(out))
+
+
+# ---------------------------------------------------------------------------------------------
 
 def main():
     args = parse()
@@ -199,82 +456,82 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
+    if args.case:
+        run_case(args, local)
+        return
     import torch
 
     import csmv_gb300 as cg
 
     torch.cuda.set_device(local)
-    w = workload(args)
-    s = cg.generate(w, pinned=True)
-    n = s.n_txn
-    h2d = (s.op.nbytes + s.off.nbytes + s.addr.nbytes)
-    dev = [torch.from_numpy(np.asarray(a).view(np.int32).copy()).cuda() for a in (s.op, s.off, s.addr)]
-    ds = cg.BankStream(n, dev[0].data_ptr(), dev[1].data_ptr(), dev[2].data_ptr(), s.addr.shape[0])
-    bank = cg.Bank(n_accounts=N_ACCOUNTS, version_depth=args.depth, client_warps=args.client_warps,
-                   ctas=args.ctas, max_txn=n, log_commits=0, device=local)
-    bank.load()
-    for _ in range(args.warmup):
-        bank.run_device(ds)
-    torch.cuda.synchronize()
+    warm, timed = args.warmup, args.steps
+    s, host = generate_batches(args.dist, args.batch, warm + timed, pinned=True)
+    addr_dev = torch.from_numpy(np.asarray(s.addr).view(np.int32).copy()).cuda()
+    n_addr = int(s.addr.shape[0])
+    dev = [DevBatch(torch, b) for b in host]
+
     barrier(world)
-    totals = dict(ms=0.0, commits=0, ro=0, aborts=0, upd=0)
+    plain, info = run_plain(cg, dev, addr_dev, n_addr, args, local, warm, timed)
+    barrier(world)
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            st = bank.run_device(ds)
-            totals["ms"] += st.kernel_ms
-            totals["commits"] += st.commits
-            totals["ro"] += st.commits_readonly
-            totals["upd"] += st.commits_update + st.commits_nowrite
-            totals["aborts"] += st.aborts
-    torch.cuda.synchronize()
+        learned = run_learned(torch, cg, dev, addr_dev, n_addr, args, local, warm, timed)
     barrier(world)
-    t_dev = reduce_max(totals["ms"] * 1e-3, world)
-    value = totals["commits"] * world / t_dev
-    # e2e: host buffers through the public call (copies inside the timed region)
-    barrier(world)
-    t0 = time.perf_counter()
-    e_commits = 0
-    for _ in range(args.steps):
-        st = bank.run(s)
-        e_commits += st.commits
-    t_e2e = reduce_max(time.perf_counter() - t0, world)
-    e2e = e_commits * world / t_e2e
-    info = bank.device_info()
-    bank.close()
+    t_learned = reduce_max(learned["wall"], world)
+    value = learned["commits"] * world / t_learned
+    t_plain = reduce_max(plain["ms"] * 1e-3, world)
+    e_commits, e_wall, h2d = e2e_learned(torch, cg, host, np.asarray(s.addr), args, local, warm,
+                                         timed)
+    e2e = e_commits * world / reduce_max(e_wall, world)
     if rank != 0:
         return
     pk, pk_kind = peaks()
-    bytes_per_tx = (totals["upd"] * B_UPDATE + totals["ro"] * B_RO) / max(1, totals["commits"])
-    achieved = bytes_per_tx * totals["commits"] / (totals["ms"] * 1e-3) / 1e9
+    # roofline of the dominant kernel of the learned step (the serial lane): algorithmic bytes
+    # of the transfers it committed over its device time
+    s_ms = learned["serial_ms"]
+    achieved = learned["serial_txn"] * B_UPDATE / (s_ms * 1e-3) / 1e9 if s_ms > 0 else 0.0
     traffic = None
-    prof = ROOT / "profiles" / "traffic.json"
-    if prof.exists():
+    tr = ROOT / "profiles" / "traffic.json"
+    if tr.exists():
         try:
-            traffic = json.loads(prof.read_text()).get("bytes_per_launch_scaled")
+            traffic = json.loads(tr.read_text()).get("bank_serial_kernel_bytes_per_launch")
         except Exception:
             traffic = None
+    plain_gbs = (plain["upd"] * B_UPDATE + plain["ro"] * B_RO) / (plain["ms"] * 1e-3) / 1e9
+    l_abort = learned["aborts"] / max(1, learned["aborts"] + learned["commits"])
     line = {
         "metric": "committed tx/s", "value": value, "unit": "committed tx/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": totals["ms"] / args.steps,
+        "steps": timed, "warmup": warm, "ms_per_step": t_learned / timed * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": "synthetic",
-        "config": {"workload": f"bank {args.dist}(0.99), 2^20 int32 accounts, transfers r4/w2, "
-                               f"20% read-only scans of 32, {n} txn/step, depth {args.depth}",
-                   "l2": "inputs larger than L2 (stream ~%d MB)" % (h2d >> 20),
+        "data": "synthetic (seeded generator with the configured shapes)",
+        "config": {"workload": workload_name(args), "l2": "inputs larger than L2 (28 MB/batch)",
                    "ctas": info["ctas"], "threads_per_cta": info["threads_per_cta"],
+                   "version_depth": args.depth, "scheduler": SCHED,
                    "parallelism": f"replicas x{world}"},
-        "abort_rate": totals["aborts"] / max(1, totals["aborts"] + totals["commits"]),
+        "abort_rate": l_abort,
+        "learned": {"tx_s": value, "abort_rate": l_abort,
+                    "serial_lane_txn_per_step": learned["serial_txn"] // timed,
+                    "plan_ms_per_step": learned["plan_ms"] / timed,
+                    "train_ms_per_step": learned["train_ms"] / timed},
+        "plain": {"tx_s": plain["commits"] * world / t_plain,
+                  "abort_rate": plain["aborts"] / max(1, plain["aborts"] + plain["commits"]),
+                  "roofline_frac_of_measured_hbm": plain_gbs / pk["hbm_gbs"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
-                     "peak_source": pk_kind,
-                     "bytes_per_tx": bytes_per_tx},
+                     "kernel": "bank_serial_kernel", "peak_source": pk_kind,
+                     "bytes_per_txn": B_UPDATE},
         "e2e": {"value": e2e, "unit": "committed tx/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": 2 * 8 * 9 + 640},
-        "gpu_launches": args.steps,
+                # per engine run: statistics (80 B) + commit-order words (768 B); up to three runs
+                # per step, plus the scheduler's 16 B of plan sizes and loss
+                "d2h_bytes_per_step": 3 * (80 + 768) + 16},
+        "gpu_launches": learned["launches"],
         "clocks": clk.summary(),
     }
+    if not args.no_extras:
+        line["hotspot"] = hotspot_section(torch, cg, local)
+        line["uniform"] = uniform_section(torch, cg, args, local)
+        line["memcd"] = memcd_section(cg, local)
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(s, args)
+        line["cpu_baseline"] = cpu_baseline(host)
     print(json.dumps(line))
 
 

@@ -106,28 +106,30 @@ class MemcdConfig(C.Structure):
 
 class SchedConfig(C.Structure):
     _fields_ = [("n_accounts", C.c_uint32), ("max_txn", C.c_uint32),
-                ("probe_rounds_pct", C.c_uint32), ("train_steps", C.c_uint32),
+                ("probe_rounds_pct", C.c_uint32), ("probe_every", C.c_uint32),
+                ("train_steps", C.c_uint32),
                 ("lr", C.c_float), ("threshold", C.c_float), ("defer_threshold", C.c_float),
-                ("deferred_warps", C.c_uint32), ("seed", C.c_uint64), ("device", C.c_int32)]
+                ("deferred_warps", C.c_uint32), ("serial_lane", C.c_uint32),
+                ("seed", C.c_uint64), ("device", C.c_int32)]
 
 
 class SchedReport(C.Structure):
-    _fields_ = [("probe", Stats), ("planned", Stats), ("loss", C.c_float),
+    _fields_ = [("probe", Stats), ("planned", Stats), ("serial", Stats), ("loss", C.c_float),
                 ("n_probe", C.c_uint32), ("n_planned", C.c_uint32), ("n_flagged", C.c_uint32),
-                ("n_deferred_rounds", C.c_uint32), ("train_ms", C.c_double),
-                ("plan_ms", C.c_double)]
+                ("n_deferred_rounds", C.c_uint32), ("n_serial", C.c_uint32),
+                ("train_ms", C.c_double), ("plan_ms", C.c_double)]
 
     @property
     def commits(self) -> int:
-        return self.probe.commits + self.planned.commits
+        return self.probe.commits + self.planned.commits + self.serial.commits
 
     @property
     def aborts(self) -> int:
-        return self.probe.aborts + self.planned.aborts
+        return self.probe.aborts + self.planned.aborts + self.serial.aborts
 
     @property
     def kernel_ms(self) -> float:
-        return self.probe.kernel_ms + self.planned.kernel_ms
+        return self.probe.kernel_ms + self.planned.kernel_ms + self.serial.kernel_ms
 
 
 _lib = None
@@ -181,6 +183,8 @@ def lib() -> C.CDLL:
         "csmv_sched_run": (I32, [P, P, C.POINTER(BankStream), C.POINTER(SchedReport)]),
         "csmv_sched_probe": (I32, [P, P, C.POINTER(BankStream), C.POINTER(SchedReport)]),
         "csmv_sched_plan_run": (I32, [P, P, C.POINTER(BankStream), C.POINTER(SchedReport)]),
+        "csmv_sched_serial_run": (I32, [P, P, C.POINTER(BankStream), C.POINTER(SchedReport)]),
+        "csmv_bank_run_serial_device": (I32, [P, C.POINTER(BankStream), C.POINTER(Stats)]),
         "csmv_sched_read_plan": (I32, [P, P, U32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
         "csmv_sched_mlp": (P, [P]),
         "csmv_sched_destroy": (None, [P]),
@@ -342,6 +346,14 @@ class Bank:
         rc = lib().csmv_bank_run_device(self._h, C.byref(dev_stream), C.byref(st))
         self.last_stats = st
         _check(rc, "csmv_bank_run_device")
+        return st
+
+    def run_serial_device(self, dev_stream: BankStream) -> Stats:
+        """The serial lane: stream order, one warp, exclusive (csmv_bank_run_serial_device)."""
+        st = Stats()
+        rc = lib().csmv_bank_run_serial_device(self._h, C.byref(dev_stream), C.byref(st))
+        self.last_stats = st
+        _check(rc, "csmv_bank_run_serial_device")
         return st
 
     def values(self) -> np.ndarray:
@@ -609,7 +621,8 @@ class Scheduler:
     def _call(self, name: str, bank: Bank, dev_stream: BankStream) -> SchedReport:
         rep = SchedReport()
         rc = getattr(lib(), name)(self._h, bank._h, C.byref(dev_stream), C.byref(rep))
-        bank.last_stats = rep.planned if name != "csmv_sched_probe" else rep.probe
+        bank.last_stats = {"csmv_sched_probe": rep.probe,
+                           "csmv_sched_serial_run": rep.serial}.get(name, rep.planned)
         _check(rc, name)
         return rep
 
@@ -621,6 +634,9 @@ class Scheduler:
 
     def plan_run(self, bank: Bank, dev_stream: BankStream) -> SchedReport:
         return self._call("csmv_sched_plan_run", bank, dev_stream)
+
+    def serial_run(self, bank: Bank, dev_stream: BankStream) -> SchedReport:
+        return self._call("csmv_sched_serial_run", bank, dev_stream)
 
     def plan(self, n: int):
         """(perm, probe_rounds, split_round) of the last planned run."""

@@ -32,6 +32,16 @@ KernelFn pick_kernel(uint32_t depth) {
     default: return nullptr;
   }
 }
+
+KernelFn pick_serial(uint32_t depth) {
+  switch (depth) {
+    case 2: return bank_serial_kernel<2, kMaxR>;
+    case 4: return bank_serial_kernel<4, kMaxR>;
+    case 8: return bank_serial_kernel<8, kMaxR>;
+    case 16: return bank_serial_kernel<16, kMaxR>;
+    default: return nullptr;
+  }
+}
 }  // namespace
 
 struct csmv_bank_t {
@@ -228,7 +238,8 @@ static csmv_status check_stream(const csmv_bank_t* h, const csmv_bank_stream* s)
 
 static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* off,
                           const uint32_t* addr, uint32_t n_txn, uint32_t* txn_aborts,
-                          uint32_t split_round, uint32_t deferred_warps, csmv_stats* out) {
+                          uint32_t split_round, uint32_t deferred_warps, csmv_stats* out,
+                          bool serial = false) {
   const csmv_bank_config& c = h->cfg;
   BankParams p{};
   p.op = op;
@@ -266,8 +277,13 @@ static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* of
   CSMV_CUDA(cudaMemsetAsync(h->stats, 0, ST_COUNT * 8, h->stream));
   void* args[] = {&p};
   CSMV_CUDA(cudaEventRecord(h->ev0, h->stream));
-  CSMV_CUDA(cudaLaunchCooperativeKernel((const void*)h->kernel, dim3(h->ctas), dim3(h->threads),
-                                        args, h->smem, h->stream));
+  if (serial) {
+    pick_serial(c.version_depth)<<<1, 32, 0, h->stream>>>(p);
+    CSMV_CUDA(cudaGetLastError());
+  } else {
+    CSMV_CUDA(cudaLaunchCooperativeKernel((const void*)h->kernel, dim3(h->ctas), dim3(h->threads),
+                                          args, h->smem, h->stream));
+  }
   CSMV_CUDA(cudaEventRecord(h->ev1, h->stream));
   unsigned long long st[ST_COUNT];
   GlobalSync gs;
@@ -316,6 +332,27 @@ extern "C" csmv_status csmv_bank_run_device(csmv_bank_t* h, const csmv_bank_stre
   auto t0 = std::chrono::steady_clock::now();
   st = launch(h, s->op, s->off, s->addr, s->n_txn, s->txn_aborts, s->split_round,
               s->deferred_warps, out);
+  if (out)
+    out->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return st;
+}
+
+extern "C" csmv_status csmv_bank_run_serial_device(csmv_bank_t* h, const csmv_bank_stream* s,
+                                                   csmv_stats* out) {
+  if (!h) return CSMV_ERR_INVALID_ARG;
+  if (!h->loaded) {
+    set_error("csmv_bank_load must come first");
+    return CSMV_ERR_STATE;
+  }
+  csmv_status st = check_stream(h, s);
+  if (st != CSMV_OK) return st;
+  if (h->cfg.validate != CSMV_VALIDATE_STAMP) {
+    set_error("the serial lane continues the stamp protocol's commit order only");
+    return CSMV_ERR_INVALID_ARG;
+  }
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  auto t0 = std::chrono::steady_clock::now();
+  st = launch(h, s->op, s->off, s->addr, s->n_txn, s->txn_aborts, 0, 0, out, true);
   if (out)
     out->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return st;

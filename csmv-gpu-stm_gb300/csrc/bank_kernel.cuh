@@ -301,7 +301,8 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
       bad |= a[k] >= p.n_items;
     }
     if (ro)
-      for (uint32_t k = 0; k < nr; k++) bad |= p.addr[off + k] >= p.n_items;
+#pragma unroll 8
+      for (uint32_t k = 0; k < nr; k++) bad |= p.addr[off + k] >= p.n_items;  // loads batch up
     if (bad) raise_error(&p.gs->error, ERR_DATA);  // no access outside the accounts
     if (__any_sync(0xFFFFFFFFu, bad)) {
       failed = true;
@@ -1221,6 +1222,208 @@ __device__ void server_warp_ring(const BankParams& p, CtaShared<MAXR, MAXW>& sm)
       stat_add(sm.stat, ST_ABORT_READ_WRITE, stat_rw);
       stat_add(sm.stat, ST_ABORT_RECORD_AGE, stat_ra);
     }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Serial lane: one warp runs a stream in stream order with the GPU to itself (no other commit
+// kernel in flight), for transfers a scheduler predicts to conflict. A round's 32 transfers
+// read the latest versions, then resolve their intra-round dependencies as one chain in lane
+// order (each lane takes the values written by the nearest lower lane, as the chain mode of the
+// commit kernel does), take consecutive timestamps in lane order and install their versions:
+// the lowest lane writing an account installs every version of that account written in the
+// round, in lane order, into its slots (victim = empty, else oldest), then stores them. No locks,
+// no timestamp server, no validation: the lane is exclusive by construction, and every round
+// commits. The timestamp order continues gs->ts_next and leaves the clock at the last one.
+// ---------------------------------------------------------------------------------------------
+template <int DEPTH, int MAXR>
+__device__ __forceinline__ int32_t latest_of(const unsigned long long (&s)[DEPTH]) {
+  uint32_t best = 0;
+  int32_t v = 0;
+  bool any = false;
+#pragma unroll
+  for (int d = 0; d < DEPTH; d++) {
+    const uint32_t t = version_ts(s[d]);
+    if (t != kEmptyTs && (!any || t > best)) {
+      any = true;
+      best = t;
+      v = version_val(s[d]);
+    }
+  }
+  return v;
+}
+
+template <int DEPTH, int MAXR>
+__global__ void __launch_bounds__(32, 1) bank_serial_kernel(BankParams p) {
+  const uint32_t lane = lane_id();
+  const VersionStore vs{p.slots, p.n_items};
+  const uint32_t base0 = ld_acquire_gpu(&p.gs->ts_next);  // == clock: nothing in flight
+  uint32_t base = base0;
+  unsigned long long n_upd = 0, n_nowrite = 0, n_ro = 0;
+  for (uint32_t g = 0; g < p.n_rounds; g++) {
+    const uint32_t t = g * 32u + lane;
+    const uint32_t op = p.op[t];
+    const uint32_t kind = CSMV_OP_KIND(op), nr = CSMV_OP_NREADS(op), off = p.off[t];
+    const bool ro = __all_sync(0xFFFFFFFFu, kind == CSMV_KIND_READONLY);
+    bool bad = (ro != (kind == CSMV_KIND_READONLY)) || (!ro && (nr < 2 || nr > (uint32_t)MAXR));
+#pragma unroll 8
+    for (uint32_t k = 0; k < nr; k++) bad |= p.addr[off + k] >= p.n_items;  // loads batch up
+    if (__any_sync(0xFFFFFFFFu, bad)) {
+      if (lane == 0) raise_error(&p.gs->error, ERR_DATA);
+      break;
+    }
+    if (ro) {  // read-only: the state after every earlier transaction of the stream
+      uint32_t sum = 0;
+      for (uint32_t k0 = 0; k0 < nr; k0 += 8) {
+        int32_t v8[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          v8[j] = 0;
+          if (k0 + j < nr) {
+            unsigned long long sl[DEPTH];
+            const unsigned long long* item = vs.slots + (size_t)p.addr[off + k0 + j] * DEPTH;
+#pragma unroll
+            for (int d = 0; d < DEPTH; d += 2) ld_relaxed_gpu_v2(item + d, sl[d], sl[d + 1]);
+            v8[j] = latest_of<DEPTH, MAXR>(sl);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) sum += (uint32_t)v8[j];
+      }
+      if (p.log) {
+        p.outcome[t] = base | kSnapFlag;
+        p.result[t] = (int32_t)sum;
+      }
+      n_ro += 32;
+      __syncwarp();
+      continue;
+    }
+    uint32_t a[MAXR];
+    int32_t v[MAXR];
+    SlotEditor<DEPTH> ed[2];  // the two written accounts' slots, as of the round's start
+#pragma unroll
+    for (int k = 0; k < MAXR; k++) {
+      a[k] = k < (int)nr ? p.addr[off + k] : 0xFFFFFFFFu;
+      v[k] = 0;
+    }
+    ed[0].load(vs.slots + (size_t)a[0] * DEPTH);
+    ed[1].load(vs.slots + (size_t)a[1] * DEPTH);
+    v[0] = latest_of<DEPTH, MAXR>(ed[0].s);
+    v[1] = latest_of<DEPTH, MAXR>(ed[1].s);
+#pragma unroll
+    for (int k = 2; k < MAXR; k++) {
+      if (k < (int)nr) {
+        unsigned long long sl[DEPTH];
+        const unsigned long long* item = vs.slots + (size_t)a[k] * DEPTH;
+#pragma unroll
+        for (int d = 0; d < DEPTH; d += 2) ld_relaxed_gpu_v2(item + d, sl[d], sl[d + 1]);
+        v[k] = latest_of<DEPTH, MAXR>(sl);
+      }
+    }
+    // one pass over the lanes: lower lanes that may write what I read (dep), and lanes that
+    // may write the same account as each of my writes (pot0, pot1). A transfer with a0 == a1
+    // writes that account once (the later value, as TXWrite overwrites).
+    uint32_t dep = 0, pot0 = 0, pot1 = 0;
+    const uint32_t b1 = a[1] != a[0] ? a[1] : 0xFFFFFFFFu;
+    for (uint32_t i = 0; i < 32; i++) {
+      const uint32_t x0 = __shfl_sync(0xFFFFFFFFu, a[0], i), x1r = __shfl_sync(0xFFFFFFFFu, a[1], i);
+      const uint32_t x1 = x1r != x0 ? x1r : 0xFFFFFFFFu;
+      bool hit = false;
+#pragma unroll
+      for (int k = 0; k < MAXR; k++) hit |= (k < (int)nr) && (a[k] == x0 || a[k] == x1r);
+      if (i < lane && hit) dep |= 1u << i;
+      if (a[0] == x0 || a[0] == x1) pot0 |= 1u << i;
+      if (b1 != 0xFFFFFFFFu && (b1 == x0 || b1 == x1)) pot1 |= 1u << i;
+    }
+    // forward the writes of each source lane, in lane order
+    for (uint32_t m = __reduce_or_sync(0xFFFFFFFFu, dep); m; m &= m - 1) {
+      const uint32_t i = __ffs(m) - 1;
+      int32_t w0, w1;
+      const bool hw = transfer_writes<MAXR>(op, nr, v, w0, w1);
+      const bool hwi = __shfl_sync(0xFFFFFFFFu, hw, i);
+      const uint32_t x0 = __shfl_sync(0xFFFFFFFFu, a[0], i), x1 = __shfl_sync(0xFFFFFFFFu, a[1], i);
+      const int32_t y0 = __shfl_sync(0xFFFFFFFFu, w0, i), y1 = __shfl_sync(0xFFFFFFFFu, w1, i);
+      if (lane > i && hwi) {
+#pragma unroll
+        for (int k = 0; k < MAXR; k++) {
+          if (k >= (int)nr) continue;
+          if (a[k] == x1)  // a transfer with a0 == a1 leaves the later value
+            v[k] = y1;
+          else if (a[k] == x0)
+            v[k] = y0;
+        }
+      }
+    }
+    int32_t w0, w1;
+    const bool has_w = transfer_writes<MAXR>(op, nr, v, w0, w1);
+    const uint32_t wm = __ballot_sync(0xFFFFFFFFu, has_w);
+    const uint32_t rank = __popc(wm & lanemask_lt());
+    const uint32_t my_ts = base + rank + 1u;
+    // installs: a version newer than every kept one replaces the victim (empty, else oldest),
+    // so the round's n writers of an account fill its slots in the victim order of the slots
+    // as the round found them - writer r (lane order) takes order[r % DEPTH] - and only the last
+    // DEPTH of them survive; the last one also stamps the commit word (stamp = last writer,
+    // unlocked), through which the stamp protocol reads the latest version
+    if (has_w) {
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        if (k == 1 && b1 == 0xFFFFFFFFu) continue;
+        const uint32_t same = (k ? pot1 : pot0) & wm;
+        const uint32_t total = __popc(same), r = __popc(same & lanemask_lt());
+        if (r + DEPTH < total) continue;
+        const uint32_t want = r % DEPTH;
+        int slot = 0;
+#pragma unroll
+        for (int d = 0; d < DEPTH; d++) {
+          const uint32_t kd = version_ts(ed[k].s[d]) + 1u;
+          uint32_t before = 0;
+#pragma unroll
+          for (int e = 0; e < DEPTH; e++) {
+            const uint32_t ke = version_ts(ed[k].s[e]) + 1u;
+            before += (ke < kd || (ke == kd && e < d)) ? 1u : 0u;
+          }
+          if (before == want) slot = d;
+        }
+        const int32_t val = (k == 0 && b1 != 0xFFFFFFFFu) ? w0 : w1;
+        st_relaxed_gpu(vs.slots + (size_t)a[k] * DEPTH + slot, pack_version(my_ts, val));
+        if (r + 1u == total) st_relaxed_gpu(&p.cw[a[k]], (unsigned long long)my_ts);
+      }
+    }
+    if (p.log) {
+      if (has_w) {
+        const uint32_t li = my_ts - 1u - p.log_base;
+        if (li < p.log_cap)
+          p.log_txn[li] = t;
+        else
+          raise_error(&p.gs->error, ERR_CAPACITY);
+        p.outcome[t] = my_ts;
+      } else {
+        p.outcome[t] = (base + rank) | kSnapFlag;  // serialised after the lower writers
+      }
+      p.result[t] = 0;
+    }
+    if (p.txn_aborts) p.txn_aborts[t] = 0u;
+    n_upd += __popc(wm);
+    n_nowrite += 32u - __popc(wm);
+    base += __popc(wm);
+    __syncwarp();  // this round's versions before the next round's reads
+  }
+  // completion-bitmap words whose timestamps this lane passed over without setting bits: clear
+  // them as the clock advance of the commit kernel would, before a later lap reuses them
+  if (base > base0) {
+    const uint32_t w_lo = (base0 + 1u) >> 5, w_end = (base + 1u) >> 5;  // words [w_lo, w_end)
+    const uint32_t cnt = min(w_end > w_lo ? w_end - w_lo : 0u, p.done_mask + 1u);
+    for (uint32_t i = lane; i < cnt; i += 32) st_relaxed_gpu(&p.done[(w_lo + i) & p.done_mask], 0u);
+  }
+  __threadfence();
+  if (lane == 0) {
+    st_relaxed_gpu(&p.gs->ts_next, base);
+    st_release_gpu(&p.gs->clock, base);
+    atomicAdd(&p.stats[ST_COMMIT_UPDATE], n_upd);
+    atomicAdd(&p.stats[ST_COMMIT_NOWRITE], n_nowrite);
+    atomicAdd(&p.stats[ST_COMMIT_RO], n_ro);
+    atomicAdd(&p.stats[ST_SECTIONS], (unsigned long long)p.n_rounds);
+    atomicAdd(&p.stats[ST_ROUNDS], (unsigned long long)p.n_rounds);
   }
 }
 

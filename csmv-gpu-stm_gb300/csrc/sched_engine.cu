@@ -43,7 +43,7 @@ struct csmv_sched_t {
   uint32_t *ro_flag = nullptr, *ro_scan = nullptr, *ro_list = nullptr, *n_flagged = nullptr;
   uint64_t chunks = 0;
   // the current chunk
-  uint32_t n = 0, probe_rounds = 0, split_round = 0, planned = 0;
+  uint32_t n = 0, probe_rounds = 0, split_round = 0, planned = 0, serial_rounds = 0;
   bool probed = false;
 };
 
@@ -53,11 +53,13 @@ extern "C" void csmv_sched_config_default(csmv_sched_config* c) {
   c->n_accounts = 1u << 20;
   c->max_txn = 1u << 20;
   c->probe_rounds_pct = 5;
+  c->probe_every = 1;
   c->train_steps = 2;
   c->lr = 3e-3f;
   c->threshold = 0.05f;
   c->defer_threshold = 2.0f;  // > 1: no deferral
   c->deferred_warps = 64;
+  c->serial_lane = 0;
   c->seed = 1;
   c->device = 0;
 }
@@ -78,7 +80,8 @@ extern "C" csmv_status csmv_sched_create(const csmv_sched_config* cfg, csmv_sche
   if (!out || !cfg) return CSMV_ERR_INVALID_ARG;
   *out = nullptr;
   if (cfg->n_accounts < 2 || cfg->max_txn == 0 || cfg->max_txn % 32 || cfg->max_txn > (1u << 26) ||
-      cfg->probe_rounds_pct > 100 || !(cfg->lr > 0.f) || cfg->deferred_warps == 0) {
+      cfg->probe_rounds_pct > 100 || cfg->probe_every == 0 || !(cfg->lr > 0.f) ||
+      cfg->deferred_warps == 0) {
     set_error("invalid scheduler config");
     return CSMV_ERR_INVALID_ARG;
   }
@@ -154,11 +157,13 @@ extern "C" csmv_status csmv_sched_probe(csmv_sched_t* s, csmv_bank_t* bank,
   const uint32_t n = d->n_txn, R = n / 32;
   uint32_t P = (uint32_t)(((uint64_t)R * s->cfg.probe_rounds_pct + 99) / 100);
   if (P > R) P = R;
+  if (s->chunks % s->cfg.probe_every) P = 0;  // this chunk is planned with the model as it is
   s->n = n;
   s->probe_rounds = P;
   s->probed = true;
   s->planned = 0;
   s->split_round = 0;
+  s->serial_rounds = 0;
   if (rep) std::memset(rep, 0, sizeof(*rep));
   // hashed access counts of the whole chunk
   CSMV_CUDA(cudaMemsetAsync(s->sketch, 0, ((size_t)1 << kSketchLog2) * 4, s->stream));
@@ -287,8 +292,14 @@ extern "C" csmv_status csmv_sched_plan_run(csmv_sched_t* s, csmv_bank_t* bank,
   rs.txn_aborts = nullptr;
   rs.split_round = s->split_round;
   rs.deferred_warps = s->split_round ? s->cfg.deferred_warps : 0;
+  if (s->cfg.serial_lane && s->split_round) {  // the deferred rounds wait for the serial lane
+    s->serial_rounds = Rp - s->split_round;
+    rs.n_txn = s->split_round * 32;
+    rs.split_round = rs.deferred_warps = 0;
+  }
   csmv_stats bst;
-  st = csmv_bank_run_device(bank, &rs, &bst);
+  std::memset(&bst, 0, sizeof(bst));
+  if (rs.n_txn) st = csmv_bank_run_device(bank, &rs, &bst);
   s->chunks++;
   if (rep) {
     rep->planned = bst;
@@ -302,6 +313,31 @@ extern "C" csmv_status csmv_sched_plan_run(csmv_sched_t* s, csmv_bank_t* bank,
   return st;
 }
 
+extern "C" csmv_status csmv_sched_serial_run(csmv_sched_t* s, csmv_bank_t* bank,
+                                             const csmv_bank_stream* d, csmv_sched_report* rep) {
+  if (!s || !bank || !d) return CSMV_ERR_INVALID_ARG;
+  if (rep) {
+    std::memset(&rep->serial, 0, sizeof(rep->serial));
+    rep->n_serial = 0;
+  }
+  if (!s->serial_rounds) return CSMV_OK;
+  const uint32_t first = s->split_round * 32, n = s->serial_rounds * 32;
+  s->serial_rounds = 0;
+  csmv_bank_stream rs = *d;
+  rs.n_txn = n;
+  rs.op = s->op2 + first;
+  rs.off = s->off2 + first;
+  rs.txn_aborts = nullptr;
+  rs.split_round = rs.deferred_warps = 0;
+  csmv_stats bst;
+  csmv_status st = csmv_bank_run_serial_device(bank, &rs, &bst);
+  if (rep) {
+    rep->serial = bst;
+    rep->n_serial = n;
+  }
+  return st;
+}
+
 extern "C" csmv_status csmv_sched_run(csmv_sched_t* s, csmv_bank_t* bank,
                                       const csmv_bank_stream* d, csmv_sched_report* rep) {
   csmv_sched_report a;
@@ -310,15 +346,21 @@ extern "C" csmv_status csmv_sched_run(csmv_sched_t* s, csmv_bank_t* bank,
     if (rep) *rep = a;
     return st;
   }
-  csmv_sched_report b;
+  csmv_sched_report b, c;
+  std::memset(&b, 0, sizeof(b));
+  std::memset(&c, 0, sizeof(c));
   st = csmv_sched_plan_run(s, bank, d, &b);
+  if (st == CSMV_OK) st = csmv_sched_serial_run(s, bank, d, &c);
+  else std::memset(&c, 0, sizeof(c));
   if (rep) {
     *rep = a;
     rep->planned = b.planned;
+    rep->serial = c.serial;
     rep->plan_ms = b.plan_ms;
     rep->n_flagged = b.n_flagged;
     rep->n_deferred_rounds = b.n_deferred_rounds;
     rep->n_planned = b.n_planned;
+    rep->n_serial = c.n_serial;
   }
   return st;
 }

@@ -198,6 +198,15 @@ csmv_status csmv_bank_run(csmv_bank_t* h, const csmv_bank_stream* host_stream,
 csmv_status csmv_bank_run_device(csmv_bank_t* h, const csmv_bank_stream* dev_stream,
                                  csmv_stats* out);
 
+/* Serial lane (no counterpart in the reference): one warp runs the device-resident stream in
+ * stream order with the GPU to itself - a round's 32 transfers resolve their dependencies as a
+ * chain in lane order and commit together, with no locks, timestamp server or validation -
+ * continuing the commit order of the handle (stamp protocol only). Meant for transactions a
+ * scheduler predicts to conflict; no other run of the handle may be in flight. Every
+ * transaction commits; read-only ones see the state after all earlier ones. */
+csmv_status csmv_bank_run_serial_device(csmv_bank_t* h, const csmv_bank_stream* dev_stream,
+                                        csmv_stats* out);
+
 /* Replaces TXEnd (bank/csmv_sh/API.cu:335-359): latest value of every account. */
 csmv_status csmv_bank_read_values(csmv_bank_t* h, int32_t* host_values);
 
@@ -390,20 +399,23 @@ typedef struct csmv_sched_config {
   uint32_t n_accounts;        /* accounts of the bank (range bins of the abort-rate features) */
   uint32_t max_txn;           /* largest chunk, multiple of 32                                */
   uint32_t probe_rounds_pct;  /* % of each chunk's rounds run in stream order to label data   */
+  uint32_t probe_every;       /* probe (and train on) one chunk in this many (>= 1)           */
   uint32_t train_steps;       /* Adam steps per chunk on the probe slice                      */
   float lr;                   /* Adam learning rate                                           */
   float threshold;            /* predicted abort probability above which a transfer is spaced */
   float defer_threshold;      /* above this it is deferred (> 1 = never)                      */
   uint32_t deferred_warps;    /* warps serving the deferred queue                             */
+  uint32_t serial_lane;       /* 1: deferred transfers run on the serial lane after the rest  */
   uint64_t seed;
   int32_t device;
 } csmv_sched_config;
 
 typedef struct csmv_sched_report {
   csmv_stats probe;           /* engine statistics of the probe run                          */
-  csmv_stats planned;         /* ... and of the planned run                                  */
+  csmv_stats planned;         /* ... of the planned run                                      */
+  csmv_stats serial;          /* ... and of the serial-lane run (serial_lane = 1)            */
   float loss;                 /* mean cross-entropy on the probe slice before this chunk's steps */
-  uint32_t n_probe, n_planned, n_flagged, n_deferred_rounds;
+  uint32_t n_probe, n_planned, n_flagged, n_deferred_rounds, n_serial;
   double train_ms, plan_ms;   /* device time of training / of features, inference and planning */
 } csmv_sched_report;
 
@@ -413,14 +425,18 @@ csmv_status csmv_sched_create(const csmv_sched_config* cfg, csmv_sched_t** out);
 /* Both steps on one chunk (dev_stream: device pointers). */
 csmv_status csmv_sched_run(csmv_sched_t* s, csmv_bank_t* bank, const csmv_bank_stream* dev_stream,
                            csmv_sched_report* out);
-/* The two steps separately (same chunk, in this order), so a caller can read the engine's
- * commit log after each run. */
+/* The steps separately (same chunk, in this order), so a caller can read the engine's commit
+ * log after each run: probe; plan and run the concurrent part; run the serial part (a no-op
+ * unless serial_lane is set and the plan deferred transfers). */
 csmv_status csmv_sched_probe(csmv_sched_t* s, csmv_bank_t* bank,
                              const csmv_bank_stream* dev_stream, csmv_sched_report* out);
 csmv_status csmv_sched_plan_run(csmv_sched_t* s, csmv_bank_t* bank,
                                 const csmv_bank_stream* dev_stream, csmv_sched_report* out);
-/* Last plan: host_perm[i] = chunk index of the transaction the planned run executed as its
- * i-th (n >= chunk size - 32 * probe_rounds); probe_rounds / split_round as used. */
+csmv_status csmv_sched_serial_run(csmv_sched_t* s, csmv_bank_t* bank,
+                                  const csmv_bank_stream* dev_stream, csmv_sched_report* out);
+/* Last plan: host_perm[i] = chunk index of the transaction the planned runs executed as their
+ * i-th (n >= chunk size - 32 * probe_rounds): the concurrent part is perm[0, 32 * split_round)
+ * when the serial lane took the rest (split_round = 0: one concurrent run of everything). */
 csmv_status csmv_sched_read_plan(csmv_sched_t* s, uint32_t* host_perm, uint32_t n,
                                  uint32_t* probe_rounds, uint32_t* split_round);
 /* The scheduler's network (owned by the scheduler). */

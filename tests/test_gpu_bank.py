@@ -12,7 +12,7 @@ import pytest
 
 import csmv_gb300 as cg
 import oracle as orc
-from gpu_util import c1_workload, defer_plan, run_checked
+from gpu_util import c1_workload, defer_plan, run_checked, sub_stream, to_device
 
 pytestmark = pytest.mark.gpu
 
@@ -192,3 +192,56 @@ def test_deferred_queue_and_per_transaction_aborts_exact(deferred_warps):
     ab0 = np.zeros(w.n_txn, np.uint32)
     st0, _, _ = run_checked(w, txn_aborts=ab0, ctas=16, client_warps=4)
     assert int(ab0.sum()) == st0.aborts and st0.aborts > 0
+
+
+@pytest.mark.parametrize("dist", [cg.DIST_UNIFORM, cg.DIST_ZIPF])
+def test_serial_lane_equals_stream_order_execution(dist):
+    """The serial lane commits every transaction in stream order: its final balances, read-only
+    sums and commit log equal a serial execution of the stream, and the replay check holds."""
+    torch = pytest.importorskip("torch")
+    n_acc, n = 2048, 32 * 600
+    w = c1_workload(n_txn=n, n_accounts=n_acc, dist=dist, zipf_theta=0.99, up_reads=4,
+                    pr_read_pct=20, seed=12)
+    s = cg.generate(w)
+    ds, keep = to_device(torch, s)
+    with cg.Bank(n_accounts=n_acc, max_txn=n, version_depth=4) as bank:
+        bank.load()
+        st = bank.run_serial_device(ds)
+        log_txn, outcome, result = bank.log(n, st.final_ts)
+        slots = bank.versions()
+        vals = bank.values()
+    init = np.full(n_acc, 1000, np.int32)
+    assert st.commits == n and st.aborts == 0
+    err = orc.check(s.op, s.off, s.addr, n_acc, init, 4, st.final_ts, log_txn, outcome, result,
+                    slots)
+    assert err is None, err
+    ref, _ = orc.serial(s.op, s.off, s.addr, n_acc, init)
+    np.testing.assert_array_equal(vals, ref)
+    writers = np.flatnonzero((outcome & cg.SNAP_FLAG) == 0)
+    assert (np.diff(writers) > 0).all() and (log_txn == writers).all()  # stream order
+
+
+def test_engine_and_serial_lane_runs_interleave_exactly():
+    """Concurrent run, serial-lane run, concurrent run on one bank: the commit order carries
+    across them and the concatenated log replays exactly."""
+    torch = pytest.importorskip("torch")
+    n_acc, n = 4096, 32 * 512
+    w = c1_workload(n_txn=3 * n, n_accounts=n_acc, seed=13)
+    s = cg.generate(w)
+    parts = [sub_stream(s, i * n, (i + 1) * n) for i in range(3)]
+    logs, outs, ress = [], [], []
+    with cg.Bank(n_accounts=n_acc, max_txn=n, ctas=8, client_warps=4) as bank:
+        bank.load()
+        prev = 0
+        for i, part in enumerate(parts):
+            ds, keep = to_device(torch, part)
+            st = bank.run_serial_device(ds) if i == 1 else bank.run_device(ds)
+            lt, oc, rs = bank.log(n, st.final_ts - prev)
+            logs.append(np.where(lt != 0xFFFFFFFF, lt + i * n, lt).astype(np.uint32))
+            outs.append(oc)
+            ress.append(rs)
+            prev = st.final_ts
+        slots = bank.versions()
+    err = orc.check(s.op, s.off, s.addr, n_acc, np.full(n_acc, 1000, np.int32), 4, prev,
+                    np.concatenate(logs), np.concatenate(outs), np.concatenate(ress), slots)
+    assert err is None, err

@@ -93,3 +93,39 @@ def test_trained_scheduler_lowers_abort_rate_on_shifting_hotspot():
         res[arm] = (aborts / (aborts + commits), commits / ms / 1e3)
     print("abort rate / Mtx/s:", res)
     assert res["learned"][0] <= 0.7 * res["plain"][0], res
+
+
+def test_serial_lane_plan_replays_exactly():
+    """With serial_lane set, transfers scored above defer_threshold run on the serial lane after
+    the concurrent part; probe, concurrent and serial runs replay exactly together."""
+    torch = pytest.importorskip("torch")
+    n_acc, n = 1 << 14, 1 << 15
+    w = c1_workload(n_txn=n, n_accounts=n_acc, dist=cg.DIST_ZIPF, zipf_theta=0.99, seed=9,
+                    up_reads=4, pr_read_pct=20)
+    s = cg.generate(w)
+    ds, keep = to_device(torch, s)
+    with cg.Bank(n_accounts=n_acc, max_txn=n, ctas=16, client_warps=4) as bank, \
+            cg.Scheduler(n_accounts=n_acc, max_txn=n, threshold=0.0, defer_threshold=0.0,
+                         serial_lane=1, train_steps=2) as sched:
+        bank.load()
+        r1 = sched.probe(bank, ds)
+        f1, np_ = r1.probe.final_ts, r1.n_probe
+        log1, out1, res1 = bank.log(np_, f1)
+        r2 = sched.plan_run(bank, ds)
+        perm, _, split = sched.plan(n)
+        f2 = r2.planned.final_ts if r2.planned.commits else f1
+        n2 = 32 * split
+        log2, out2, res2 = bank.log(n2, f2 - f1) if n2 else (np.zeros(0, np.uint32),) * 3
+        r3 = sched.serial_run(bank, ds)
+        f3 = r3.serial.final_ts
+        log3, out3, res3 = bank.log(len(perm) - n2, f3 - f2)
+        slots = bank.versions()
+    assert r3.n_serial == len(perm) - n2 > 0 and r3.serial.aborts == 0
+    op_c = np.concatenate([s.op[:np_], s.op[perm]])
+    off_c = np.concatenate([s.off[:np_], s.off[perm]])
+    sh = lambda lg, k: np.where(lg != HOLE, lg + k, HOLE).astype(np.uint32)
+    log_c = np.concatenate([log1, sh(log2, np_), sh(log3, np_ + n2)]).astype(np.uint32)
+    err = orc.check(op_c, off_c, s.addr, n_acc, np.full(n_acc, 1000, np.int32), 4, f3, log_c,
+                    np.concatenate([out1, out2[:n2], out3]).astype(np.uint32),
+                    np.concatenate([res1, res2[:n2], res3]).astype(np.int32), slots)
+    assert err is None, err
