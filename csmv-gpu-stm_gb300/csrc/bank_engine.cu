@@ -33,6 +33,16 @@ KernelFn pick_kernel(uint32_t depth) {
   }
 }
 
+size_t serial_smem(uint32_t depth) {
+  switch (depth) {
+    case 2: return serial_smem_bytes<2, kMaxR>();
+    case 4: return serial_smem_bytes<4, kMaxR>();
+    case 8: return serial_smem_bytes<8, kMaxR>();
+    case 16: return serial_smem_bytes<16, kMaxR>();
+    default: return 0;
+  }
+}
+
 KernelFn pick_serial(uint32_t depth) {
   switch (depth) {
     case 2: return bank_serial_kernel<2, kMaxR>;
@@ -158,6 +168,10 @@ extern "C" csmv_status csmv_bank_create(const csmv_bank_config* cfg, csmv_bank_t
   if ((st = cuda_status(cudaFuncSetAttribute((const void*)h->kernel,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)h->smem),
+                        "cudaFuncSetAttribute")) != CSMV_OK ||
+      (st = cuda_status(cudaFuncSetAttribute((const void*)pick_serial(cfg->version_depth),
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)serial_smem(cfg->version_depth)),
                         "cudaFuncSetAttribute")) != CSMV_OK)
     return fail(st);
   int per_sm = 0;
@@ -278,7 +292,7 @@ static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* of
   void* args[] = {&p};
   CSMV_CUDA(cudaEventRecord(h->ev0, h->stream));
   if (serial) {
-    pick_serial(c.version_depth)<<<1, 32, 0, h->stream>>>(p);
+    pick_serial(c.version_depth)<<<1, 32, serial_smem(c.version_depth), h->stream>>>(p);
     CSMV_CUDA(cudaGetLastError());
   } else {
     CSMV_CUDA(cudaLaunchCooperativeKernel((const void*)h->kernel, dim3(h->ctas), dim3(h->threads),

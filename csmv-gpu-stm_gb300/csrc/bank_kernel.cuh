@@ -164,6 +164,30 @@ __device__ __forceinline__ bool transfer_writes(uint32_t op, uint32_t nr, const 
   return CSMV_OP_KIND(op) == CSMV_KIND_TRANSFER_ALWAYS || v[0] >= (int32_t)amt;
 }
 
+// acc % d for a divisor fixed over a round, without a hardware divide: q = umulhi(acc, m) with
+// m = floor((2^32 - 1) / d) is floor(acc / d) or one less, so one correction gives the remainder.
+struct ModMagic {
+  uint32_t d, m;
+  __device__ __forceinline__ explicit ModMagic(uint32_t div) : d(div), m(0xFFFFFFFFu / div) {}
+  __device__ __forceinline__ uint32_t mod(uint32_t acc) const {
+    uint32_t r = acc - __umulhi(acc, m) * d;
+    return r >= d ? r - d : r;
+  }
+};
+
+template <int MAXR>
+__device__ __forceinline__ bool transfer_writes(uint32_t op, uint32_t nr, const int32_t (&v)[MAXR],
+                                                const ModMagic& mm, int32_t& w0, int32_t& w1) {
+  uint32_t acc = CSMV_OP_AMT0(op) - 1u;
+#pragma unroll
+  for (int k = 2; k < MAXR; k++)
+    if (k < (int)nr) acc += (uint32_t)v[k];
+  const uint32_t amt = 1u + mm.mod(acc);
+  w0 = (int32_t)((uint32_t)v[0] - amt);
+  w1 = (int32_t)((uint32_t)v[1] + amt);
+  return CSMV_OP_KIND(op) == CSMV_KIND_TRANSFER_ALWAYS || v[0] >= (int32_t)amt;
+}
+
 // Install versions (ts, value) into an item whose lock the caller holds: `n` insertions applied
 // to the item's slots in registers (victim = empty, else oldest), then stored back.
 template <int DEPTH>
@@ -1253,25 +1277,168 @@ __device__ __forceinline__ int32_t latest_of(const unsigned long long (&s)[DEPTH
   return v;
 }
 
+constexpr int kLaneHash = 128;  // writer table of one serial-lane round (<= 64 accounts)
+
+__device__ __forceinline__ uint32_t lane_hash(uint32_t a) { return (a * 0x9E3779B1u) >> 25; }
+
+// Mask of the round's lanes writing account x (0 if none), from the shared-memory table.
+__device__ __forceinline__ uint32_t writers_of(const uint32_t* hk, const uint32_t* hm, uint32_t x) {
+  for (uint32_t h = lane_hash(x), probes = 0; probes < (uint32_t)kLaneHash; probes++) {
+    const uint32_t k = hk[h];
+    if (k == x) return hm[h];
+    if (k == 0xFFFFFFFFu) return 0u;
+    h = (h + 1u) & (kLaneHash - 1u);
+  }
+  return 0u;
+}
+
+// Slot of the want-th victim (empty first, else oldest; lowest index on ties) of DEPTH slots.
+template <int DEPTH>
+__device__ __forceinline__ int victim_rank_slot(const unsigned long long (&sl)[DEPTH], uint32_t want) {
+  int slot = 0;
+  if (want == 0) {  // the common case: the account's only (or first) writer of the round
+    uint32_t best = version_ts(sl[0]) + 1u;
+#pragma unroll
+    for (int d = 1; d < DEPTH; d++) {
+      const uint32_t k = version_ts(sl[d]) + 1u;
+      if (k < best) {
+        best = k;
+        slot = d;
+      }
+    }
+    return slot;
+  }
+#pragma unroll
+  for (int d = 0; d < DEPTH; d++) {
+    const uint32_t kd = version_ts(sl[d]) + 1u;
+    uint32_t before = 0;
+#pragma unroll
+    for (int e = 0; e < DEPTH; e++) {
+      const uint32_t ke = version_ts(sl[e]) + 1u;
+      before += (ke < kd || (ke == kd && e < d)) ? 1u : 0u;
+    }
+    if (before == want) slot = d;
+  }
+  return slot;
+}
+
+// Shared memory of the serial lane. Round g's version slots are copied (cp.async, one round
+// ahead) into stage[g & 1]; tables[g & 1] maps each account round g writes to the mask of its
+// writer lanes and, after the round's installs, to its slots - round g+1 patches the slots it
+// staged before round g's stores from there. 16-byte chunks of a lane's row are XOR-swizzled by
+// lane so a quarter-warp's 16-byte reads hit distinct banks.
+template <int DEPTH, int MAXR>
+struct SerialSmem {
+  unsigned long long stage[2][MAXR][32][DEPTH];
+  unsigned long long ent[2][kLaneHash][DEPTH];
+  uint32_t hk[2][kLaneHash], hm[2][kLaneHash];
+};
+
+template <int DEPTH, int MAXR>
+__host__ __device__ constexpr size_t serial_smem_bytes() { return sizeof(SerialSmem<DEPTH, MAXR>); }
+
+constexpr uint32_t kTomb = 0xFFFFFFFEu;  // table key of an account the round did not write
+
+// Table slot of account x in table (hk) or -1.
+__device__ __forceinline__ int table_slot(const uint32_t* hk, uint32_t x) {
+  for (uint32_t h = lane_hash(x), probes = 0; probes < (uint32_t)kLaneHash; probes++) {
+    const uint32_t k = hk[h];
+    if (k == x) return (int)h;
+    if (k == 0xFFFFFFFFu) return -1;
+    h = (h + 1u) & (kLaneHash - 1u);
+  }
+  return -1;
+}
+
 template <int DEPTH, int MAXR>
 __global__ void __launch_bounds__(32, 1) bank_serial_kernel(BankParams p) {
+  extern __shared__ __align__(16) unsigned char serial_smem_raw[];
+  SerialSmem<DEPTH, MAXR>& S = *reinterpret_cast<SerialSmem<DEPTH, MAXR>*>(serial_smem_raw);
+  constexpr uint32_t kCh = DEPTH / 2, kSw = (kCh - 1u) < 3u ? (kCh - 1u) : 3u;
   const uint32_t lane = lane_id();
   const VersionStore vs{p.slots, p.n_items};
   const uint32_t base0 = ld_acquire_gpu(&p.gs->ts_next);  // == clock: nothing in flight
   uint32_t base = base0;
   unsigned long long n_upd = 0, n_nowrite = 0, n_ro = 0;
-  for (uint32_t g = 0; g < p.n_rounds; g++) {
+  const uint32_t R = p.n_rounds;
+
+  auto load_opoff = [&](uint32_t r, uint32_t& op, uint32_t& off) {
+    op = 0u;
+    off = 0u;
+    if (r < R) {
+      op = p.op[r * 32u + lane];
+      off = p.off[r * 32u + lane];
+    }
+  };
+  auto load_addr = [&](uint32_t r, uint32_t op, uint32_t off, uint32_t (&a)[MAXR]) {
+    const uint32_t nr = CSMV_OP_NREADS(op);
+    const bool upd = r < R && CSMV_OP_KIND(op) != CSMV_KIND_READONLY;
+#pragma unroll
+    for (int k = 0; k < MAXR; k++) a[k] = (upd && k < (int)nr) ? p.addr[off + k] : 0u;
+  };
+  // copies of round r's slots into stage[buf] (transfers only; out-of-range ids are skipped here
+  // and reported when the round is processed); one commit group per round, empty or not
+  auto stage_round = [&](uint32_t r, uint32_t op, const uint32_t (&a)[MAXR], int buf) {
+    if (r < R && CSMV_OP_KIND(op) != CSMV_KIND_READONLY) {
+      const uint32_t nr = CSMV_OP_NREADS(op);
+#pragma unroll
+      for (int k = 0; k < MAXR; k++) {
+        if (k >= (int)nr || a[k] >= p.n_items) continue;
+        const unsigned long long* item = vs.slots + (size_t)a[k] * DEPTH;
+#pragma unroll
+        for (uint32_t c = 0; c < kCh; c++)
+          cp_async16(&S.stage[buf][k][lane][(c ^ (lane & kSw)) * 2u], item + c * 2u);
+      }
+    }
+    cp_async_commit();
+  };
+  auto staged = [&](int buf, int k, unsigned long long (&sl)[DEPTH]) {
+#pragma unroll
+    for (uint32_t c = 0; c < kCh; c++) {
+      const unsigned long long* q = &S.stage[buf][k][lane][(c ^ (lane & kSw)) * 2u];
+      sl[2 * c] = q[0];
+      sl[2 * c + 1] = q[1];
+    }
+  };
+
+  // pipeline: round g's addresses and staged slots are ready when g starts; round g+1's
+  // addresses too; round g+2's op / offset
+  uint32_t op_c, off_c, op_1, off_1, op_2, off_2, a_c[MAXR], a_1[MAXR];
+  load_opoff(0, op_c, off_c);
+  load_opoff(1, op_1, off_1);
+  load_opoff(2, op_2, off_2);
+  load_addr(0, op_c, off_c, a_c);
+  load_addr(1, op_1, off_1, a_1);
+  for (uint32_t i = lane; i < (uint32_t)kLaneHash; i += 32) S.hk[1][i] = 0xFFFFFFFFu;  // "round -1"
+  stage_round(0, op_c, a_c, 0);
+  __syncwarp();
+
+  for (uint32_t g = 0; g < R; g++) {
+    const int cb = (int)(g & 1u), pb = cb ^ 1;
     const uint32_t t = g * 32u + lane;
-    const uint32_t op = p.op[t];
-    const uint32_t kind = CSMV_OP_KIND(op), nr = CSMV_OP_NREADS(op), off = p.off[t];
+    // ahead: round g+1's slots, round g+2's addresses, round g+3's op / offset
+    stage_round(g + 1, op_1, a_1, pb);
+    uint32_t a_2[MAXR], op_3, off_3;
+    load_addr(g + 2, op_2, off_2, a_2);
+    load_opoff(g + 3, op_3, off_3);
+
+    const uint32_t op = op_c, off = off_c;
+    const uint32_t kind = CSMV_OP_KIND(op), nr = CSMV_OP_NREADS(op);
     const bool ro = __all_sync(0xFFFFFFFFu, kind == CSMV_KIND_READONLY);
     bool bad = (ro != (kind == CSMV_KIND_READONLY)) || (!ro && (nr < 2 || nr > (uint32_t)MAXR));
+    if (!ro) {
+#pragma unroll
+      for (int k = 0; k < MAXR; k++) bad |= (k < (int)nr) && a_c[k] >= p.n_items;
+    } else {
 #pragma unroll 8
-    for (uint32_t k = 0; k < nr; k++) bad |= p.addr[off + k] >= p.n_items;  // loads batch up
+      for (uint32_t k = 0; k < nr; k++) bad |= p.addr[off + k] >= p.n_items;
+    }
     if (__any_sync(0xFFFFFFFFu, bad)) {
       if (lane == 0) raise_error(&p.gs->error, ERR_DATA);
       break;
     }
+    cp_async_wait_group<1>();  // round g's copies (round g+1's may still be in flight)
+    __syncwarp();
     if (ro) {  // read-only: the state after every earlier transaction of the stream
       uint32_t sum = 0;
       for (uint32_t k0 = 0; k0 < nr; k0 += 8) {
@@ -1294,120 +1461,154 @@ __global__ void __launch_bounds__(32, 1) bank_serial_kernel(BankParams p) {
         p.outcome[t] = base | kSnapFlag;
         p.result[t] = (int32_t)sum;
       }
+      if (p.txn_aborts) p.txn_aborts[t] = 0u;
       n_ro += 32;
-      __syncwarp();
-      continue;
-    }
-    uint32_t a[MAXR];
-    int32_t v[MAXR];
-    SlotEditor<DEPTH> ed[2];  // the two written accounts' slots, as of the round's start
-#pragma unroll
-    for (int k = 0; k < MAXR; k++) {
-      a[k] = k < (int)nr ? p.addr[off + k] : 0xFFFFFFFFu;
-      v[k] = 0;
-    }
-    ed[0].load(vs.slots + (size_t)a[0] * DEPTH);
-    ed[1].load(vs.slots + (size_t)a[1] * DEPTH);
-    v[0] = latest_of<DEPTH, MAXR>(ed[0].s);
-    v[1] = latest_of<DEPTH, MAXR>(ed[1].s);
-#pragma unroll
-    for (int k = 2; k < MAXR; k++) {
-      if (k < (int)nr) {
-        unsigned long long sl[DEPTH];
-        const unsigned long long* item = vs.slots + (size_t)a[k] * DEPTH;
-#pragma unroll
-        for (int d = 0; d < DEPTH; d += 2) ld_relaxed_gpu_v2(item + d, sl[d], sl[d + 1]);
-        v[k] = latest_of<DEPTH, MAXR>(sl);
+      for (uint32_t i = lane; i < (uint32_t)kLaneHash; i += 32) S.hk[cb][i] = 0xFFFFFFFFu;
+    } else {
+      uint32_t* hk = S.hk[cb];
+      uint32_t* hm = S.hm[cb];
+      const uint32_t* hk_prev = S.hk[pb];
+      const uint32_t b1 = a_c[1] != a_c[0] ? a_c[1] : 0xFFFFFFFFu;
+      for (uint32_t i = lane; i < (uint32_t)kLaneHash; i += 32) {
+        hk[i] = 0xFFFFFFFFu;
+        hm[i] = 0u;
       }
-    }
-    // one pass over the lanes: lower lanes that may write what I read (dep), and lanes that
-    // may write the same account as each of my writes (pot0, pot1). A transfer with a0 == a1
-    // writes that account once (the later value, as TXWrite overwrites).
-    uint32_t dep = 0, pot0 = 0, pot1 = 0;
-    const uint32_t b1 = a[1] != a[0] ? a[1] : 0xFFFFFFFFu;
-    for (uint32_t i = 0; i < 32; i++) {
-      const uint32_t x0 = __shfl_sync(0xFFFFFFFFu, a[0], i), x1r = __shfl_sync(0xFFFFFFFFu, a[1], i);
-      const uint32_t x1 = x1r != x0 ? x1r : 0xFFFFFFFFu;
-      bool hit = false;
+      __syncwarp();
+      // the round's writers: account -> lane mask (a transfer with a0 == a1 writes it once)
+      int hs[2] = {-1, -1};
 #pragma unroll
-      for (int k = 0; k < MAXR; k++) hit |= (k < (int)nr) && (a[k] == x0 || a[k] == x1r);
-      if (i < lane && hit) dep |= 1u << i;
-      if (a[0] == x0 || a[0] == x1) pot0 |= 1u << i;
-      if (b1 != 0xFFFFFFFFu && (b1 == x0 || b1 == x1)) pot1 |= 1u << i;
-    }
-    // forward the writes of each source lane, in lane order
-    for (uint32_t m = __reduce_or_sync(0xFFFFFFFFu, dep); m; m &= m - 1) {
-      const uint32_t i = __ffs(m) - 1;
-      int32_t w0, w1;
-      const bool hw = transfer_writes<MAXR>(op, nr, v, w0, w1);
-      const bool hwi = __shfl_sync(0xFFFFFFFFu, hw, i);
-      const uint32_t x0 = __shfl_sync(0xFFFFFFFFu, a[0], i), x1 = __shfl_sync(0xFFFFFFFFu, a[1], i);
-      const int32_t y0 = __shfl_sync(0xFFFFFFFFu, w0, i), y1 = __shfl_sync(0xFFFFFFFFu, w1, i);
-      if (lane > i && hwi) {
-#pragma unroll
-        for (int k = 0; k < MAXR; k++) {
-          if (k >= (int)nr) continue;
-          if (a[k] == x1)  // a transfer with a0 == a1 leaves the later value
-            v[k] = y1;
-          else if (a[k] == x0)
-            v[k] = y0;
+      for (int w = 0; w < 2; w++) {
+        const uint32_t x = w ? b1 : a_c[0];
+        if (x == 0xFFFFFFFFu) continue;
+        for (uint32_t h = lane_hash(x), probes = 0; probes < (uint32_t)kLaneHash; probes++) {
+          const uint32_t prev = atomicCAS(&hk[h], 0xFFFFFFFFu, x);
+          if (prev == 0xFFFFFFFFu || prev == x) {
+            atomicOr(&hm[h], 1u << lane);
+            hs[w] = (int)h;
+            break;
+          }
+          h = (h + 1u) & (kLaneHash - 1u);
         }
       }
-    }
-    int32_t w0, w1;
-    const bool has_w = transfer_writes<MAXR>(op, nr, v, w0, w1);
-    const uint32_t wm = __ballot_sync(0xFFFFFFFFu, has_w);
-    const uint32_t rank = __popc(wm & lanemask_lt());
-    const uint32_t my_ts = base + rank + 1u;
-    // installs: a version newer than every kept one replaces the victim (empty, else oldest),
-    // so the round's n writers of an account fill its slots in the victim order of the slots
-    // as the round found them - writer r (lane order) takes order[r % DEPTH] - and only the last
-    // DEPTH of them survive; the last one also stamps the commit word (stamp = last writer,
-    // unlocked), through which the stamp protocol reads the latest version
-    if (has_w) {
+      // my slots as round g found them: staged, or patched from round g-1's installs
+      int32_t v[MAXR];
+      unsigned long long ed[2][DEPTH];
+#pragma unroll
+      for (int k = 0; k < MAXR; k++) {
+        v[k] = 0;
+        if (k >= (int)nr) continue;
+        unsigned long long sl[DEPTH];
+        const int e = table_slot(hk_prev, a_c[k]);
+        if (e >= 0) {
+#pragma unroll
+          for (int d = 0; d < DEPTH; d++) sl[d] = S.ent[pb][e][d];
+        } else {
+          staged(cb, k, sl);
+        }
+        v[k] = latest_of<DEPTH, MAXR>(sl);
+        if (k < 2)
+#pragma unroll
+          for (int d = 0; d < DEPTH; d++) ed[k][d] = sl[d];
+      }
+      __syncwarp();
+      // lower lanes that may write what I read; writers of each of my written accounts
+      uint32_t dep = 0;
+#pragma unroll
+      for (int k = 0; k < MAXR; k++)
+        if (k < (int)nr) dep |= writers_of(hk, hm, a_c[k]);
+      dep &= lanemask_lt();
+      const uint32_t pot0 = hs[0] >= 0 ? hm[hs[0]] : 0u;
+      const uint32_t pot1 = hs[1] >= 0 ? hm[hs[1]] : 0u;
+      // forward the writes of each source lane, in lane order
+      const ModMagic mm(CSMV_OP_AMOD(op));
+      for (uint32_t m = __reduce_or_sync(0xFFFFFFFFu, dep); m; m &= m - 1) {
+        const uint32_t i = __ffs(m) - 1;
+        int32_t w0, w1;
+        const bool hw = transfer_writes<MAXR>(op, nr, v, mm, w0, w1);
+        const bool hwi = __shfl_sync(0xFFFFFFFFu, hw, i);
+        const uint32_t x0 = __shfl_sync(0xFFFFFFFFu, a_c[0], i), x1 = __shfl_sync(0xFFFFFFFFu, a_c[1], i);
+        const int32_t y0 = __shfl_sync(0xFFFFFFFFu, w0, i), y1 = __shfl_sync(0xFFFFFFFFu, w1, i);
+        if (lane > i && hwi) {
+#pragma unroll
+          for (int k = 0; k < MAXR; k++) {
+            if (k >= (int)nr) continue;
+            if (a_c[k] == x1)
+              v[k] = y1;
+            else if (a_c[k] == x0)
+              v[k] = y0;
+          }
+        }
+      }
+      int32_t w0, w1;
+      const bool has_w = transfer_writes<MAXR>(op, nr, v, mm, w0, w1);
+      const uint32_t wm = __ballot_sync(0xFFFFFFFFu, has_w);
+      const uint32_t rank = __popc(wm & lanemask_lt());
+      const uint32_t my_ts = base + rank + 1u;
+      // installs: a version newer than every kept one replaces the victim (empty, else oldest),
+      // so the round's n writers of an account fill its slots in the victim order of the slots
+      // as the round found them - writer r (lane order) takes order[r % DEPTH] - and only the
+      // last DEPTH of them survive; the last one also stamps the commit word (stamp = last
+      // writer, unlocked), through which the stamp protocol reads the latest version. The
+      // account's table entry receives the same slots for the next round.
+      uint32_t same[2], total[2], r[2];
 #pragma unroll
       for (int k = 0; k < 2; k++) {
-        if (k == 1 && b1 == 0xFFFFFFFFu) continue;
-        const uint32_t same = (k ? pot1 : pot0) & wm;
-        const uint32_t total = __popc(same), r = __popc(same & lanemask_lt());
-        if (r + DEPTH < total) continue;
-        const uint32_t want = r % DEPTH;
-        int slot = 0;
+        const uint32_t potk = k ? pot1 : pot0;
+        same[k] = potk & wm;
+        total[k] = __popc(same[k]);
+        r[k] = __popc(same[k] & lanemask_lt());
+        if (has_w && hs[k] >= 0 && r[k] == 0)  // the first writer copies the round-start slots
 #pragma unroll
-        for (int d = 0; d < DEPTH; d++) {
-          const uint32_t kd = version_ts(ed[k].s[d]) + 1u;
-          uint32_t before = 0;
-#pragma unroll
-          for (int e = 0; e < DEPTH; e++) {
-            const uint32_t ke = version_ts(ed[k].s[e]) + 1u;
-            before += (ke < kd || (ke == kd && e < d)) ? 1u : 0u;
-          }
-          if (before == want) slot = d;
-        }
-        const int32_t val = (k == 0 && b1 != 0xFFFFFFFFu) ? w0 : w1;
-        st_relaxed_gpu(vs.slots + (size_t)a[k] * DEPTH + slot, pack_version(my_ts, val));
-        if (r + 1u == total) st_relaxed_gpu(&p.cw[a[k]], (unsigned long long)my_ts);
+          for (int d = 0; d < DEPTH; d++) S.ent[cb][hs[k]][d] = ed[k][d];
+        // an account none of its would-be writers wrote (funds short) holds no entry for the
+        // next round: its key becomes a tombstone that lookups step over
+        if (hs[k] >= 0 && same[k] == 0u && (potk & lanemask_lt()) == 0u) S.hk[cb][hs[k]] = kTomb;
       }
-    }
-    if (p.log) {
+      __syncwarp();
       if (has_w) {
-        const uint32_t li = my_ts - 1u - p.log_base;
-        if (li < p.log_cap)
-          p.log_txn[li] = t;
-        else
-          raise_error(&p.gs->error, ERR_CAPACITY);
-        p.outcome[t] = my_ts;
-      } else {
-        p.outcome[t] = (base + rank) | kSnapFlag;  // serialised after the lower writers
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+          if (hs[k] < 0 || r[k] + DEPTH < total[k]) continue;
+          const int slot = victim_rank_slot<DEPTH>(ed[k], r[k] % DEPTH);
+          const int32_t val = (k == 0 && b1 != 0xFFFFFFFFu) ? w0 : w1;
+          const unsigned long long ver = pack_version(my_ts, val);
+          S.ent[cb][hs[k]][slot] = ver;
+          st_relaxed_gpu(vs.slots + (size_t)a_c[k] * DEPTH + slot, ver);
+          if (r[k] + 1u == total[k]) st_relaxed_gpu(&p.cw[a_c[k]], (unsigned long long)my_ts);
+        }
       }
-      p.result[t] = 0;
+      if (p.log) {
+        if (has_w) {
+          const uint32_t li = my_ts - 1u - p.log_base;
+          if (li < p.log_cap)
+            p.log_txn[li] = t;
+          else
+            raise_error(&p.gs->error, ERR_CAPACITY);
+          p.outcome[t] = my_ts;
+        } else {
+          p.outcome[t] = (base + rank) | kSnapFlag;  // serialised after the lower writers
+        }
+        p.result[t] = 0;
+      }
+      if (p.txn_aborts) p.txn_aborts[t] = 0u;
+      n_upd += __popc(wm);
+      n_nowrite += 32u - __popc(wm);
+      base += __popc(wm);
     }
-    if (p.txn_aborts) p.txn_aborts[t] = 0u;
-    n_upd += __popc(wm);
-    n_nowrite += 32u - __popc(wm);
-    base += __popc(wm);
-    __syncwarp();  // this round's versions before the next round's reads
+    __syncwarp();  // this round's versions, table and stage reads before the next round
+    op_c = op_1;
+    off_c = off_1;
+    op_1 = op_2;
+    off_1 = off_2;
+    op_2 = op_3;
+    off_2 = off_3;
+#pragma unroll
+    for (int k = 0; k < MAXR; k++) {
+      a_c[k] = a_1[k];
+      a_1[k] = a_2[k];
+    }
   }
+  cp_async_wait_all();
   // completion-bitmap words whose timestamps this lane passed over without setting bits: clear
   // them as the clock advance of the commit kernel would, before a later lap reuses them
   if (base > base0) {
