@@ -104,6 +104,12 @@ class MemcdConfig(C.Structure):
         "max_req", "spin_limit_log2")] + [("device", C.c_int32)]
 
 
+class ServeConfig(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in ("n_sets", "client_warps", "ctas", "arena_requests",
+                                          "max_inflight_sets", "idle_timeout_ms")] + [
+        ("device", C.c_int32)]
+
+
 class SchedConfig(C.Structure):
     _fields_ = [("n_accounts", C.c_uint32), ("max_txn", C.c_uint32),
                 ("probe_rounds_pct", C.c_uint32), ("probe_every", C.c_uint32),
@@ -178,6 +184,15 @@ def lib() -> C.CDLL:
         "csmv_mlp_get_grads": (I32, [P, P]),
         "csmv_mlp_adam_step": (I32, [P, C.c_float]),
         "csmv_mlp_destroy": (None, [P]),
+        "csmv_serve_config_default": (None, [C.POINTER(ServeConfig)]),
+        "csmv_serve_create": (I32, [C.POINTER(ServeConfig), C.POINTER(P)]),
+        "csmv_serve_start": (I32, [P]),
+        "csmv_serve_submit": (I32, [P, C.POINTER(MemcdBatch), C.POINTER(C.c_uint64)]),
+        "csmv_serve_poll": (I32, [P, C.c_uint64, C.POINTER(C.c_uint32), P, P,
+                                  C.POINTER(C.c_uint64)]),
+        "csmv_serve_stop": (I32, [P, C.POINTER(Stats)]),
+        "csmv_serve_read_table": (I32, [P, P, P]),
+        "csmv_serve_destroy": (None, [P]),
         "csmv_sched_config_default": (None, [C.POINTER(SchedConfig)]),
         "csmv_sched_create": (I32, [C.POINTER(SchedConfig), C.POINTER(P)]),
         "csmv_sched_run": (I32, [P, P, C.POINTER(BankStream), C.POINTER(SchedReport)]),
@@ -515,6 +530,100 @@ class Memcd:
                                             C.byref(d)), "csmv_memcd_device_info")
         return {"n_sms": a.value, "ctas": b.value, "threads_per_cta": c_.value,
                 "device_bytes": d.value}
+
+
+# ---------------------------------------------------------------------------------------------
+# serving loop
+# ---------------------------------------------------------------------------------------------
+
+def serve_config(**kw) -> ServeConfig:
+    cfg = ServeConfig()
+    lib().csmv_serve_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        if not hasattr(cfg, k):
+            raise KeyError(f"unknown serve config field {k}")
+        setattr(cfg, k, v)
+    return cfg
+
+
+class Server:
+    """The cache's serving loop (csmv_serve_*): a persistent kernel per session, request
+    batches admitted from a mapped host ring as they arrive."""
+
+    def __init__(self, cfg: ServeConfig | None = None, **kw):
+        self.cfg = cfg if cfg is not None else serve_config(**kw)
+        h = C.c_void_p()
+        _check(lib().csmv_serve_create(C.byref(self.cfg), C.byref(h)), "csmv_serve_create")
+        self._h = h
+        self.tick = 1
+        self._sizes = {}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            lib().csmv_serve_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def start(self) -> None:
+        _check(lib().csmv_serve_start(self._h), "csmv_serve_start")
+        self._sizes = {}
+
+    def submit(self, req: Requests, tick: int | None = None):
+        """Batch id, or None when admission refuses it for now (no room)."""
+        t = self.tick if tick is None else tick
+        b = MemcdBatch(req.n_req, t, _ptr(req.kind), _ptr(req.key), _ptr(req.val), None, None)
+        bid = C.c_uint64()
+        rc = lib().csmv_serve_submit(self._h, C.byref(b), C.byref(bid))
+        if rc == 5:
+            return None
+        _check(rc, "csmv_serve_submit")
+        if tick is None:
+            self.tick += 1
+        self._sizes[bid.value] = req.n_req
+        return bid.value
+
+    def poll(self, batch_id: int, results: bool = True):
+        """None while running; else (found, val_out, device_ns) (arrays None if not asked)."""
+        n = self._sizes[batch_id]
+        done = C.c_uint32()
+        ns = C.c_uint64()
+        found = np.empty(n, np.uint32) if results else None
+        out = np.empty((n, 8), np.uint32) if results else None
+        _check(lib().csmv_serve_poll(self._h, batch_id, C.byref(done),
+                                     _ptr(found) if results else None,
+                                     _ptr(out) if results else None, C.byref(ns)),
+               "csmv_serve_poll")
+        if not done.value:
+            return None
+        return found, out, ns.value
+
+    def stop(self) -> Stats:
+        st = Stats()
+        _check(lib().csmv_serve_stop(self._h, C.byref(st)), "csmv_serve_stop")
+        return st
+
+    def table(self):
+        nv = self.cfg.n_sets * MEMCD_WAYS * MEMCD_DEPTH
+        tags = np.empty(nv, np.uint64)
+        recs = np.empty((nv, 16), np.uint32)
+        _check(lib().csmv_serve_read_table(self._h, _ptr(tags), _ptr(recs)), "csmv_serve_read_table")
+        return tags, recs
+
+
+def requests_slice(req: Requests, lo: int, hi: int) -> Requests:
+    return Requests(np.ascontiguousarray(req.kind[lo:hi]), np.ascontiguousarray(req.key[lo:hi]),
+                    np.ascontiguousarray(req.val[lo:hi]))
 
 
 # ---------------------------------------------------------------------------------------------

@@ -361,3 +361,385 @@ extern "C" void csmv_memcd_destroy(csmv_memcd_t* h) {
   free_all(h);
   delete h;
 }
+
+// =============================================================================================
+// Serving loop (csmv_serve_*): the table on the device, a persistent kernel replayed from a
+// captured CUDA graph, request batches admitted from a pinned, mapped host ring as room frees up.
+//
+// Host-side admission: a batch of n requests is admitted when the arena has n free request
+// slots (slots free when the batches holding them complete, in admission order), when it keeps
+// the SETs in flight within max_inflight_sets (every SET installs a version; bounding them
+// bounds how fast versions a GET still needs can be overwritten) and when fewer than 1024
+// batches are in flight.
+// =============================================================================================
+#include <atomic>
+
+struct csmv_serve_t {
+  csmv_serve_config cfg{};
+  int n_sms = 0, ctas = 0, threads = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  // table
+  unsigned long long* tag = nullptr;
+  uint4* rec = nullptr;
+  unsigned long long* cw = nullptr;
+  uint32_t* done = nullptr;
+  GlobalSync* gs = nullptr;
+  unsigned long long* stats = nullptr;
+  uint32_t* dummy_log = nullptr;  // log/outcome pointers of the params (logging is off)
+  // serving state (device)
+  ServeDev* dev = nullptr;
+  uint2* rq = nullptr;
+  uint32_t* remaining = nullptr;
+  uint32_t* tick = nullptr;
+  // mapped host memory
+  ServeHostCtl* ctl = nullptr;
+  ServeBatchDesc* desc = nullptr;
+  uint32_t *h_kind = nullptr, *h_key = nullptr, *h_val = nullptr, *h_found = nullptr,
+           *h_out = nullptr;
+  // host bookkeeping
+  bool running = false;
+  uint64_t submitted = 0, retired = 0, arena_head = 0, arena_tail = 0, inflight_sets = 0;
+  bool collected[kServeSlots] = {};  // polled done: its slots may be reused
+};
+
+extern "C" void csmv_serve_config_default(csmv_serve_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->n_sets = 1u << 20;
+  c->client_warps = 4;
+  c->ctas = 0;
+  c->arena_requests = 1u << 18;
+  c->max_inflight_sets = 1u << 15;
+  c->idle_timeout_ms = 10000;
+  c->device = 0;
+}
+
+static void serve_free(csmv_serve_t* h) {
+  if (h->exec) cudaGraphExecDestroy(h->exec);
+  if (h->graph) cudaGraphDestroy(h->graph);
+  void* dptr[] = {h->tag, h->rec, h->cw, h->done, h->gs, h->stats, h->dummy_log,
+                  h->dev, h->rq, h->remaining, h->tick};
+  for (void* p : dptr) cudaFree(p);
+  void* hptr[] = {h->ctl, h->desc, h->h_kind, h->h_key, h->h_val, h->h_found, h->h_out};
+  for (void* p : hptr)
+    if (p) cudaFreeHost(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+template <class T>
+static T* dev_ptr_of(T* host) {
+  void* d = nullptr;
+  if (cudaHostGetDevicePointer(&d, host, 0) != cudaSuccess) return nullptr;
+  return static_cast<T*>(d);
+}
+
+extern "C" csmv_status csmv_serve_create(const csmv_serve_config* cfg, csmv_serve_t** out) {
+  if (!out || !cfg) return CSMV_ERR_INVALID_ARG;
+  *out = nullptr;
+  const uint32_t A = cfg->arena_requests;
+  if (cfg->n_sets < 1 || cfg->n_sets > (1u << 26) || cfg->client_warps < 1 ||
+      cfg->client_warps > (uint32_t)kMaxClientWarps || A < 1024 || (A & (A - 1)) ||
+      A > (1u << 24) || cfg->max_inflight_sets == 0 || cfg->idle_timeout_ms == 0) {
+    set_error("invalid serve config (arena_requests: power of two 1024..2^24)");
+    return CSMV_ERR_INVALID_ARG;
+  }
+  int n_sms = 0;
+  csmv_status st = check_device(cfg->device, &n_sms);
+  if (st != CSMV_OK) return st;
+  CSMV_CUDA(cudaSetDevice(cfg->device));
+  csmv_serve_t* h = new csmv_serve_t;
+  h->cfg = *cfg;
+  h->n_sms = n_sms;
+  h->threads = (int)(cfg->client_warps + 1) * 32;
+  auto fail = [&](csmv_status s) {
+    serve_free(h);
+    delete h;
+    return s;
+  };
+  int per_sm = 0;
+  if ((st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, memcd_serve_kernel,
+                                                                       h->threads, 0),
+                        "occupancy")) != CSMV_OK)
+    return fail(st);
+  const int max_ctas = per_sm * n_sms;
+  h->ctas = cfg->ctas ? (int)cfg->ctas : max_ctas;
+  if (h->ctas < 1 || h->ctas > max_ctas) {
+    set_error("%d CTAs requested, %d can be co-resident", h->ctas, max_ctas);
+    return fail(CSMV_ERR_INVALID_ARG);
+  }
+  const size_t ent = (size_t)cfg->n_sets * kWays, D = kMemcdDepth;
+  const uint32_t qcap = A / 32;  // rounds of a full arena
+  struct {
+    void** p;
+    size_t bytes;
+  } dallocs[] = {
+      {(void**)&h->tag, ent * D * 8}, {(void**)&h->rec, ent * D * 64}, {(void**)&h->cw, ent * 8},
+      {(void**)&h->done, (size_t)kDoneWords * 4}, {(void**)&h->gs, sizeof(GlobalSync)},
+      {(void**)&h->stats, ST_COUNT * 8}, {(void**)&h->dummy_log, 64},
+      {(void**)&h->dev, sizeof(ServeDev)}, {(void**)&h->rq, (size_t)qcap * 8},
+      {(void**)&h->remaining, kServeSlots * 4}, {(void**)&h->tick, kServeSlots * 4},
+  };
+  for (auto& a : dallocs)
+    if ((st = cuda_status(cudaMalloc(a.p, a.bytes), "cudaMalloc")) != CSMV_OK) return fail(st);
+  struct {
+    void** p;
+    size_t bytes;
+  } hallocs[] = {
+      {(void**)&h->ctl, sizeof(ServeHostCtl)}, {(void**)&h->desc, kServeSlots * sizeof(ServeBatchDesc)},
+      {(void**)&h->h_kind, (size_t)A * 4}, {(void**)&h->h_key, (size_t)A * 16},
+      {(void**)&h->h_val, (size_t)A * 32}, {(void**)&h->h_found, (size_t)A * 4},
+      {(void**)&h->h_out, (size_t)A * 32},
+  };
+  for (auto& a : hallocs)
+    if ((st = cuda_status(cudaHostAlloc(a.p, a.bytes, cudaHostAllocMapped), "cudaHostAlloc")) != CSMV_OK)
+      return fail(st);
+  std::memset(h->ctl, 0, sizeof(ServeHostCtl));
+  std::memset(h->desc, 0, kServeSlots * sizeof(ServeBatchDesc));
+  if ((st = cuda_status(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream")) != CSMV_OK)
+    return fail(st);
+  // empty table (memcdSH.cu:567-574), commit order at 0
+  memcd_clear_kernel<<<n_sms * 4, 256, 0, h->stream>>>(h->tag, ent * D);
+  if ((st = cuda_status(cudaGetLastError(), "clear")) != CSMV_OK ||
+      (st = cuda_status(cudaMemsetAsync(h->rec, 0, ent * D * 64, h->stream), "memset")) != CSMV_OK ||
+      (st = cuda_status(cudaMemsetAsync(h->cw, 0, ent * 8, h->stream), "memset")) != CSMV_OK ||
+      (st = cuda_status(cudaMemsetAsync(h->done, 0, (size_t)kDoneWords * 4, h->stream), "memset")) != CSMV_OK ||
+      (st = cuda_status(cudaMemsetAsync(h->gs, 0, sizeof(GlobalSync), h->stream), "memset")) != CSMV_OK ||
+      (st = cuda_status(cudaStreamSynchronize(h->stream), "sync")) != CSMV_OK)
+    return fail(st);
+  // the session graph: reset the serving cursors and statistics, run the persistent kernel
+  MemcdParams p{};
+  p.kind = dev_ptr_of(h->h_kind);
+  p.key = reinterpret_cast<const uint4*>(dev_ptr_of(h->h_key));
+  p.val = reinterpret_cast<const uint4*>(dev_ptr_of(h->h_val));
+  p.found = dev_ptr_of(h->h_found);
+  p.val_out = reinterpret_cast<uint4*>(dev_ptr_of(h->h_out));
+  ServeParams sp{};
+  sp.ctl = dev_ptr_of(h->ctl);
+  sp.desc = dev_ptr_of(h->desc);
+  if (!p.kind || !p.key || !p.val || !p.found || !p.val_out || !sp.ctl || !sp.desc) {
+    set_error("cudaHostGetDevicePointer failed");
+    return fail(CSMV_ERR_CUDA);
+  }
+  p.n_rounds = 0;
+  p.tick = 1;
+  p.n_sets = cfg->n_sets;
+  p.tag = h->tag;
+  p.rec = h->rec;
+  p.cw = h->cw;
+  p.done = h->done;
+  p.done_mask = kDoneWords - 1;
+  p.gs = h->gs;
+  p.log_txn = h->dummy_log;
+  p.outcome = h->dummy_log;
+  p.log = 0;
+  p.log_base = 0;
+  p.log_cap = 1;
+  p.stats = h->stats;
+  p.nc = cfg->client_warps;
+  p.batch = CSMV_BATCH_CTA;
+  p.spin_log2 = 24;
+  sp.dev = h->dev;
+  sp.rq = h->rq;
+  sp.q_mask = qcap - 1;
+  sp.arena_mask = A - 1;
+  sp.remaining = h->remaining;
+  sp.tick = h->tick;
+  sp.idle_ns = (unsigned long long)cfg->idle_timeout_ms * 1000000ull;
+  cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->dev, 0, sizeof(ServeDev), h->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(&h->gs->round_next, 0, 4, h->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(&h->gs->error, 0, 4, h->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->stats, 0, ST_COUNT * 8, h->stream);
+  if (e == cudaSuccess) {
+    memcd_serve_kernel<<<h->ctas, h->threads, 0, h->stream>>>(p, sp);
+    e = cudaGetLastError();
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
+  if (e == cudaSuccess) e = e2;
+  h->graph = g;
+  if ((st = cuda_status(e, "capture of the serving graph")) != CSMV_OK) return fail(st);
+  if ((st = cuda_status(cudaGraphInstantiate(&h->exec, h->graph, 0), "cudaGraphInstantiate")) != CSMV_OK)
+    return fail(st);
+  *out = h;
+  return CSMV_OK;
+}
+
+extern "C" csmv_status csmv_serve_start(csmv_serve_t* h) {
+  if (!h) return CSMV_ERR_INVALID_ARG;
+  if (h->running) {
+    set_error("serving session already running");
+    return CSMV_ERR_STATE;
+  }
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  std::memset(h->ctl, 0, sizeof(ServeHostCtl));
+  std::memset(h->desc, 0, kServeSlots * sizeof(ServeBatchDesc));
+  std::atomic_thread_fence(std::memory_order_seq_cst);
+  h->submitted = h->retired = h->arena_head = h->arena_tail = h->inflight_sets = 0;
+  CSMV_CUDA(cudaGraphLaunch(h->exec, h->stream));
+  h->running = true;
+  return CSMV_OK;
+}
+
+static bool batch_done(const csmv_serve_t* h, uint64_t b) {
+  const volatile uint32_t* d = &h->desc[b % kServeSlots].done;
+  const bool done = *d != 0u;
+  std::atomic_thread_fence(std::memory_order_acquire);
+  return done;
+}
+
+// Retire collected batches in admission order (frees arena slots and the SET budget).
+static void serve_retire(csmv_serve_t* h) {
+  while (h->retired < h->submitted && h->collected[h->retired % kServeSlots]) {
+    const ServeBatchDesc& d = h->desc[h->retired % kServeSlots];
+    h->arena_tail += d.n_req;
+    h->inflight_sets -= d.sets;
+    h->retired++;
+  }
+}
+
+extern "C" csmv_status csmv_serve_submit(csmv_serve_t* h, const csmv_memcd_batch* b,
+                                         uint64_t* batch_id) {
+  if (!h || !b || !b->kind || !b->key || !b->val || b->n_req == 0 || b->n_req % 32) {
+    set_error("serve submit: n_req must be a positive multiple of 32 with kind/key/val set");
+    return CSMV_ERR_INVALID_ARG;
+  }
+  if (!h->running) {
+    set_error("serve submit: no session running");
+    return CSMV_ERR_STATE;
+  }
+  const uint32_t A = h->cfg.arena_requests, n = b->n_req;
+  if (n > A) {
+    set_error("batch of %u requests exceeds the arena (%u)", n, A);
+    return CSMV_ERR_INVALID_ARG;
+  }
+  uint32_t sets = 0;
+  for (uint32_t i = 0; i < n; i++) sets += b->kind[i] == CSMV_MEMCD_SET;
+  serve_retire(h);
+  if (h->arena_head + n - h->arena_tail > A || h->inflight_sets + sets > h->cfg.max_inflight_sets ||
+      h->submitted - h->retired >= kServeSlots) {
+    set_error("serve submit: no room (arena slots, SET budget or descriptors); retry later");
+    return CSMV_ERR_CAPACITY;
+  }
+  const uint32_t first = (uint32_t)(h->arena_head & (A - 1));
+  const uint32_t n1 = std::min(n, A - first), n2 = n - n1;
+  std::memcpy(h->h_kind + first, b->kind, (size_t)n1 * 4);
+  std::memcpy(h->h_key + (size_t)first * 4, b->key, (size_t)n1 * 16);
+  std::memcpy(h->h_val + (size_t)first * 8, b->val, (size_t)n1 * 32);
+  if (n2) {
+    std::memcpy(h->h_kind, b->kind + n1, (size_t)n2 * 4);
+    std::memcpy(h->h_key, b->key + (size_t)n1 * 4, (size_t)n2 * 16);
+    std::memcpy(h->h_val, b->val + (size_t)n1 * 8, (size_t)n2 * 32);
+  }
+  ServeBatchDesc& d = h->desc[h->submitted % kServeSlots];
+  h->collected[h->submitted % kServeSlots] = false;
+  d.first = first;
+  d.n_req = n;
+  d.tick = b->tick;
+  d.seq = (uint32_t)h->submitted;
+  d.sets = sets;
+  d.admit_ns = d.done_ns = 0;
+  d.done = 0;
+  std::atomic_thread_fence(std::memory_order_seq_cst);  // requests and descriptor, then publish
+  *reinterpret_cast<volatile uint32_t*>(&h->ctl->submitted) = (uint32_t)(h->submitted + 1);
+  if (batch_id) *batch_id = h->submitted;
+  h->submitted++;
+  h->arena_head += n;
+  h->inflight_sets += sets;
+  return CSMV_OK;
+}
+
+extern "C" csmv_status csmv_serve_poll(csmv_serve_t* h, uint64_t batch_id, uint32_t* done,
+                                       uint32_t* host_found, uint32_t* host_val_out,
+                                       uint64_t* device_ns) {
+  if (!h || !done) return CSMV_ERR_INVALID_ARG;
+  *done = 0;
+  if (batch_id >= h->submitted) {
+    set_error("batch %llu not submitted", (unsigned long long)batch_id);
+    return CSMV_ERR_INVALID_ARG;
+  }
+  if (batch_id < h->retired) {  // collected earlier and its slots reused: done, no results
+    *done = 1;
+    return CSMV_OK;
+  }
+  if (!batch_done(h, batch_id)) return CSMV_OK;
+  h->collected[batch_id % kServeSlots] = true;
+  const ServeBatchDesc& d = h->desc[batch_id % kServeSlots];
+  const uint32_t A = h->cfg.arena_requests, n = d.n_req, first = d.first;
+  const uint32_t n1 = std::min(n, A - first), n2 = n - n1;
+  if (host_found) {
+    std::memcpy(host_found, h->h_found + first, (size_t)n1 * 4);
+    if (n2) std::memcpy(host_found + n1, h->h_found, (size_t)n2 * 4);
+  }
+  if (host_val_out) {
+    std::memcpy(host_val_out, h->h_out + (size_t)first * 8, (size_t)n1 * 32);
+    if (n2) std::memcpy(host_val_out + (size_t)n1 * 8, h->h_out, (size_t)n2 * 32);
+  }
+  if (device_ns) *device_ns = d.done_ns > d.admit_ns ? d.done_ns - d.admit_ns : 0;
+  *done = 1;
+  return CSMV_OK;
+}
+
+extern "C" csmv_status csmv_serve_stop(csmv_serve_t* h, csmv_stats* out) {
+  if (!h) return CSMV_ERR_INVALID_ARG;
+  if (!h->running) {
+    set_error("no serving session running");
+    return CSMV_ERR_STATE;
+  }
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  std::atomic_thread_fence(std::memory_order_seq_cst);
+  *reinterpret_cast<volatile uint32_t*>(&h->ctl->stop) = 1u;
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  h->running = false;
+  CSMV_CUDA(e);
+  unsigned long long st[ST_COUNT];
+  GlobalSync gs;
+  CSMV_CUDA(cudaMemcpy(st, h->stats, sizeof(st), cudaMemcpyDeviceToHost));
+  CSMV_CUDA(cudaMemcpy(&gs, h->gs, sizeof(gs), cudaMemcpyDeviceToHost));
+  serve_retire(h);
+  if (out) {
+    std::memset(out, 0, sizeof(*out));
+    out->commits_update = st[ST_COMMIT_UPDATE];
+    out->commits_readonly = st[ST_COMMIT_RO];
+    out->aborts_data_age = st[ST_ABORT_DATA_AGE];
+    out->aborts_read_write = st[ST_ABORT_READ_WRITE];
+    out->aborts_prevalid = st[ST_ABORT_PREVALID];
+    out->aborts_write_write = st[ST_ABORT_WRITE_WRITE];
+    out->sections = st[ST_SECTIONS];
+    out->rounds = st[ST_ROUNDS];
+    out->final_ts = gs.ts_next;
+    out->error = gs.error;
+  }
+  if (gs.error) {
+    set_error("serving kernel ended with device error %u (4: idle timeout)", gs.error);
+    return CSMV_ERR_TIMEOUT;
+  }
+  return CSMV_OK;
+}
+
+extern "C" csmv_status csmv_serve_read_table(csmv_serve_t* h, uint64_t* host_tags,
+                                             uint32_t* host_recs) {
+  if (!h) return CSMV_ERR_INVALID_ARG;
+  if (h->running) {
+    set_error("stop the serving session first");
+    return CSMV_ERR_STATE;
+  }
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  const size_t nv = (size_t)h->cfg.n_sets * kWays * kMemcdDepth;
+  if (host_tags) CSMV_CUDA(cudaMemcpy(host_tags, h->tag, nv * 8, cudaMemcpyDeviceToHost));
+  if (host_recs) CSMV_CUDA(cudaMemcpy(host_recs, h->rec, nv * 64, cudaMemcpyDeviceToHost));
+  return CSMV_OK;
+}
+
+extern "C" void csmv_serve_destroy(csmv_serve_t* h) {
+  if (!h) return;
+  cudaSetDevice(h->cfg.device);
+  if (h->running) {
+    *reinterpret_cast<volatile uint32_t*>(&h->ctl->stop) = 1u;
+    cudaStreamSynchronize(h->stream);
+  }
+  serve_free(h);
+  delete h;
+}

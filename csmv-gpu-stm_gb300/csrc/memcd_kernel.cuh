@@ -94,25 +94,19 @@ __device__ __forceinline__ void st_relaxed_gpu_v4(uint4* p, uint4 v) {
 }
 __device__ __forceinline__ uint32_t tag_ts(unsigned long long t) { return (uint32_t)(t >> 32); }
 
-__device__ void memcd_client(const MemcdParams& p, MemcdShared& sm, uint32_t w) {
+// One round of 32 requests (request r on this lane), run until every request has committed.
+// Returns false when the warp must stop (device error raised).
+__device__ bool memcd_round(const MemcdParams& p, MemcdShared& sm, MemcdMail& ms, uint32_t me,
+                            uint32_t r, uint32_t& seq, uint32_t tick) {
   constexpr int D = kMemcdDepth;
-  MemcdMail& ms = sm.mail[w];
   const uint32_t lane = lane_id();
-  const uint32_t me = blockIdx.x * p.nc + w + 1;
-  uint32_t seq = 0;
   bool failed = false;
-  for (;;) {
-    uint32_t g = 0;
-    if (lane == 0) g = atomicAdd(&p.gs->round_next, 1u);
-    g = __shfl_sync(0xFFFFFFFFu, g, 0);
-    if (g >= p.n_rounds) break;
-    const uint32_t r = g * 32u + lane;
+  {
     const uint32_t kind = p.kind[r];
     const bool is_set = __all_sync(0xFFFFFFFFu, kind == 1u);
     if (__any_sync(0xFFFFFFFFu, (kind == 1u) != is_set || kind > 1u)) {  // mixed round
       if (lane == 0) raise_error(&p.gs->error, ERR_DATA);
-      failed = true;
-      break;
+      return false;
     }
     const uint4 key = p.key[r];
     const uint32_t hmix = memcd_mix(key.x, key.y, key.z, key.w);
@@ -380,7 +374,7 @@ __device__ void memcd_client(const MemcdParams& p, MemcdShared& sm, uint32_t w) 
         const size_t v = v0 + vic;
         st_relaxed_gpu(p.tag + v, (unsigned long long)kEmptyTs << 32);  // readers: moving
         __threadfence();
-        st_relaxed_gpu_v4(p.rec + v * 4, make_uint4(p.tick, 0u, 0u, 0u));
+        st_relaxed_gpu_v4(p.rec + v * 4, make_uint4(tick, 0u, 0u, 0u));
         st_relaxed_gpu_v4(p.rec + v * 4 + 1, key);
         st_relaxed_gpu_v4(p.rec + v * 4 + 2, nv0);
         st_relaxed_gpu_v4(p.rec + v * 4 + 3, nv1);
@@ -411,7 +405,21 @@ __device__ void memcd_client(const MemcdParams& p, MemcdShared& sm, uint32_t w) 
         break;
       }
     }
-    if (failed) break;
+  }
+  return !failed;
+}
+
+__device__ void memcd_client(const MemcdParams& p, MemcdShared& sm, uint32_t w) {
+  MemcdMail& ms = sm.mail[w];
+  const uint32_t lane = lane_id();
+  const uint32_t me = blockIdx.x * p.nc + w + 1;
+  uint32_t seq = 0;
+  for (;;) {
+    uint32_t g = 0;
+    if (lane == 0) g = atomicAdd(&p.gs->round_next, 1u);
+    g = __shfl_sync(0xFFFFFFFFu, g, 0);
+    if (g >= p.n_rounds) break;
+    if (!memcd_round(p, sm, ms, me, g * 32u + lane, seq, p.tick)) break;
   }
   __syncwarp();
   if (lane == 0) atomicAdd(&sm.done_warps, 1u);
@@ -431,6 +439,184 @@ __global__ void __launch_bounds__(512, 1) memcd_kernel(MemcdParams p) {
     server_warp_stamp(p.nc, p.batch, p.gs, sm);
   else
     memcd_client(p, sm, warp - 1);
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < ST_COUNT; i += blockDim.x)
+    if (sm.stat[i]) atomicAdd(&p.stats[i], sm.stat[i]);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Serving: a persistent kernel that admits request batches as the host publishes them.
+//
+// Requests live in a ring ("arena") of pinned, mapped host memory that the kernel reads and
+// writes in place (coherent over the C2C link of a Grace-Blackwell node): request i of a batch
+// that starts at arena index f is request (f + i) mod arena size. The host publishes a batch by
+// filling its descriptor and then bumping ctl->submitted (release). Any client warp that finds
+// the round queue empty takes the admission lock, turns newly published batches into rounds of
+// 32 requests appended to the device round queue, and releases the queue tail; warps claim
+// rounds in order and run them with the cache's commit protocol, so rounds of different batches
+// overlap on the device. After a round, the warp makes its results visible to the host and
+// counts the round off its batch; the batch's last round stamps done_ns and sets done (release).
+// The kernel returns once ctl->stop is set and every published batch has completed, or after
+// idle_ns without work (error ERR_WAIT_REQUEST).
+// ---------------------------------------------------------------------------------------------
+constexpr uint32_t kServeSlots = 1024;  // batch descriptors in flight at most
+
+struct ServeHostCtl {     // mapped host memory, written by the host
+  uint32_t submitted;     // batches published
+  uint32_t stop;          // finish what is published, then return
+  uint32_t pad[14];
+};
+
+struct ServeBatchDesc {   // mapped host memory, one per in-flight batch (slot = batch % kServeSlots)
+  uint32_t first, n_req, tick, seq;
+  unsigned long long admit_ns, done_ns;  // device global timer
+  uint32_t done, sets, pad[6];
+};
+
+struct alignas(128) ServeDev {  // device memory
+  alignas(128) uint32_t admitted;  // batches turned into rounds
+  alignas(128) uint32_t q_head;    // rounds claimed
+  alignas(128) uint32_t q_tail;    // rounds appended
+  alignas(128) uint32_t lock;      // admission
+};
+
+struct ServeParams {
+  ServeHostCtl* ctl;
+  ServeBatchDesc* desc;
+  ServeDev* dev;
+  uint2* rq;             // [q_mask + 1] {first request index, batch slot}
+  uint32_t q_mask;
+  uint32_t arena_mask;
+  uint32_t* remaining;   // [kServeSlots] rounds left per batch
+  uint32_t* tick;        // [kServeSlots] LRU tick per batch
+  unsigned long long idle_ns;
+};
+
+// Admission, warp-collective (called by a warp whose claim found the queue empty).
+__device__ void serve_admit(const ServeParams& s) {
+  const uint32_t lane = lane_id();
+  uint32_t locked = 0;
+  if (lane == 0) locked = atomicCAS(&s.dev->lock, 0u, 1u) == 0u ? 1u : 0u;
+  if (!__shfl_sync(0xFFFFFFFFu, locked, 0)) return;
+  uint32_t sub = 0, adm = 0, qt = 0;
+  if (lane == 0) {
+    sub = ld_acquire_sys(&s.ctl->submitted);
+    adm = ld_relaxed_gpu(&s.dev->admitted);
+    qt = ld_relaxed_gpu(&s.dev->q_tail);
+  }
+  sub = __shfl_sync(0xFFFFFFFFu, sub, 0);
+  adm = __shfl_sync(0xFFFFFFFFu, adm, 0);
+  qt = __shfl_sync(0xFFFFFFFFu, qt, 0);
+  for (uint32_t guard = 0; adm < sub && guard < kServeSlots; guard++, adm++) {
+    const uint32_t slot = adm % kServeSlots;
+    uint32_t first = 0, n = 0, tk = 0;
+    if (lane == 0) {
+      const volatile ServeBatchDesc* d = s.desc + slot;
+      first = d->first;
+      n = d->n_req;
+      tk = d->tick;
+    }
+    first = __shfl_sync(0xFFFFFFFFu, first, 0);
+    n = __shfl_sync(0xFFFFFFFFu, n, 0);
+    tk = __shfl_sync(0xFFFFFFFFu, tk, 0);
+    const uint32_t rounds = n / 32u;
+    for (uint32_t i = lane; i < rounds; i += 32)
+      s.rq[(qt + i) & s.q_mask] = make_uint2((first + 32u * i) & s.arena_mask, slot);
+    if (lane == 0) {
+      s.remaining[slot] = rounds;
+      s.tick[slot] = tk;
+      s.desc[slot].admit_ns = globaltimer_ns();
+    }
+    qt += rounds;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    st_relaxed_gpu(&s.dev->admitted, adm);
+    __threadfence();
+    st_release_gpu(&s.dev->q_tail, qt);  // rounds, counts and ticks before the tail
+    st_release_gpu(&s.dev->lock, 0u);
+  }
+}
+
+__device__ void serve_client(const MemcdParams& p, const ServeParams& s, MemcdShared& sm,
+                             uint32_t w) {
+  MemcdMail& ms = sm.mail[w];
+  const uint32_t lane = lane_id();
+  const uint32_t me = blockIdx.x * p.nc + w + 1;
+  uint32_t seq = 0;
+  unsigned long long idle_since = 0;
+  for (;;) {
+    uint32_t got = 0u, first = 0u, slot = 0u;
+    if (lane == 0) {
+      for (uint32_t attempt = 0; attempt < 64u; attempt++) {
+        const uint32_t h = ld_relaxed_gpu(&s.dev->q_head), t = ld_acquire_gpu(&s.dev->q_tail);
+        if (h >= t) break;
+        if (atomicCAS(&s.dev->q_head, h, h + 1u) == h) {
+          const uint2 e = s.rq[h & s.q_mask];
+          first = e.x;
+          slot = e.y;
+          got = 1u;
+          break;
+        }
+      }
+    }
+    got = __shfl_sync(0xFFFFFFFFu, got, 0);
+    if (!got) {
+      serve_admit(s);
+      uint32_t leave = 0;
+      if (lane == 0) {
+        const uint32_t h = ld_relaxed_gpu(&s.dev->q_head), t = ld_acquire_gpu(&s.dev->q_tail);
+        const uint32_t stop = ld_acquire_sys(&s.ctl->stop);
+        const uint32_t sub = ld_acquire_sys(&s.ctl->submitted);
+        const uint32_t adm = ld_relaxed_gpu(&s.dev->admitted);
+        const unsigned long long now = globaltimer_ns();
+        if (idle_since == 0) idle_since = now;
+        if (ld_relaxed_gpu(&p.gs->error)) leave = 1;
+        else if (stop && adm == sub && h >= t) leave = 1;
+        else if (now - idle_since > s.idle_ns) {
+          raise_error(&p.gs->error, ERR_WAIT_REQUEST);
+          leave = 1;
+        }
+      }
+      if (__shfl_sync(0xFFFFFFFFu, leave, 0)) break;
+      __nanosleep(200);
+      continue;
+    }
+    idle_since = 0;
+    first = __shfl_sync(0xFFFFFFFFu, first, 0);
+    slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+    uint32_t tk = 0;
+    if (lane == 0) tk = ld_relaxed_gpu(&s.tick[slot]);
+    tk = __shfl_sync(0xFFFFFFFFu, tk, 0);
+    if (!memcd_round(p, sm, ms, me, (first + lane) & s.arena_mask, seq, tk)) break;
+    __syncwarp();
+    if (lane == 0) {
+      __threadfence_system();  // this round's results reach the host before its batch completes
+      if (atomicSub(&s.remaining[slot], 1u) == 1u) {
+        s.desc[slot].done_ns = globaltimer_ns();
+        __threadfence_system();
+        st_release_sys(&s.desc[slot].done, 1u);
+      }
+    }
+  }
+  __syncwarp();
+  if (lane == 0) atomicAdd(&sm.done_warps, 1u);
+}
+
+__global__ void __launch_bounds__(512, 1) memcd_serve_kernel(MemcdParams p, ServeParams s) {
+  __shared__ MemcdShared sm;
+  const uint32_t warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) sm.done_warps = 0;
+  for (uint32_t i = threadIdx.x; i < ST_COUNT; i += blockDim.x) sm.stat[i] = 0;
+  for (uint32_t i = threadIdx.x; i < p.nc; i += blockDim.x) {
+    sm.mail[i].req = 0;
+    sm.mail[i].rep = 0;
+  }
+  __syncthreads();
+  if (warp == 0)
+    server_warp_stamp(p.nc, p.batch, p.gs, sm);
+  else
+    serve_client(p, s, sm, warp - 1);
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < ST_COUNT; i += blockDim.x)
     if (sm.stat[i]) atomicAdd(&p.stats[i], sm.stat[i]);

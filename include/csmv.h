@@ -353,6 +353,49 @@ csmv_status csmv_memcd_device_info(csmv_memcd_t* h, int* n_sms, int* ctas, int* 
 void csmv_memcd_destroy(csmv_memcd_t* h);
 
 /* ------------------------------------------------------------------------------------------
+ * Serving loop for the cache (replaces the reference's host batch loop, memcdSH.cu:622-651,
+ * which launches one kernel per batch and waits for it). The table stays on the device; one
+ * persistent kernel, replayed from a CUDA graph captured at create, serves a session. Request
+ * batches of any size (multiple of 32) are copied into a ring of pinned, mapped host memory and
+ * published; the kernel admits them as they arrive, so batches that arrive while others run are
+ * served alongside them. A batch is admitted only while the ring has room for it, the SETs in
+ * flight stay within max_inflight_sets and fewer than 1024 batches are in flight; otherwise
+ * csmv_serve_submit returns CSMV_ERR_CAPACITY and the caller retries after completions. Each
+ * batch gets a device completion stamp; results are read with csmv_serve_poll.
+ * ------------------------------------------------------------------------------------------ */
+typedef struct csmv_serve_config {
+  uint32_t n_sets;             /* cache sets (8 ways, 2 versions per entry)                     */
+  uint32_t client_warps;       /* client warps per CTA (1..15)                                  */
+  uint32_t ctas;               /* 0 = as many as fit co-resident                                */
+  uint32_t arena_requests;     /* request ring size, power of two (1024..2^24)                  */
+  uint32_t max_inflight_sets;  /* SET requests in flight at most (admission)                    */
+  uint32_t idle_timeout_ms;    /* the kernel returns (error) after this long without work       */
+  int32_t device;
+} csmv_serve_config;
+typedef struct csmv_serve_t csmv_serve_t;
+void csmv_serve_config_default(csmv_serve_config* cfg);
+/* Allocates the table (empty), the ring and the descriptors, and captures the session graph. */
+csmv_status csmv_serve_create(const csmv_serve_config* cfg, csmv_serve_t** out);
+/* Launches a session (one replay of the captured graph); the table carries over sessions. */
+csmv_status csmv_serve_start(csmv_serve_t* s);
+/* Publishes a batch (host pointers: kind, key, val, tick; found / val_out are not used here);
+ * *batch_id numbers batches from 0 within the session. */
+csmv_status csmv_serve_submit(csmv_serve_t* s, const csmv_memcd_batch* host_batch,
+                              uint64_t* batch_id);
+/* *done = 1 once the batch completed; its results are then copied to host_found [n] and
+ * host_val_out [8 n] (either may be NULL) and *device_ns = admission -> completion (device).
+ * A batch polled done is collected: its ring slots are reused by later batches (in admission
+ * order), after which a poll still reports done but returns no results. Batches that are never
+ * collected keep their slots, so admission stalls until they are polled. */
+csmv_status csmv_serve_poll(csmv_serve_t* s, uint64_t batch_id, uint32_t* done,
+                            uint32_t* host_found, uint32_t* host_val_out, uint64_t* device_ns);
+/* Ends the session once every published batch is served; statistics of the session. */
+csmv_status csmv_serve_stop(csmv_serve_t* s, csmv_stats* out);
+/* Version store between sessions (layout as csmv_memcd_read_table). */
+csmv_status csmv_serve_read_table(csmv_serve_t* s, uint64_t* host_tags, uint32_t* host_recs);
+void csmv_serve_destroy(csmv_serve_t* s);
+
+/* ------------------------------------------------------------------------------------------
  * Conflict predictor network (no counterpart in the reference; the learned scheduler below
  * uses it). 64 input features -> 128 -> 128 -> 1, ReLU, ReLU, sigmoid = probability that a
  * transaction aborts. Weights are kept in bf16 for the kernels (rounded from fp32 master
