@@ -19,9 +19,11 @@ e2e = the same through host buffers (pinned -> device copies and the statistics 
 the timed region). Both arms' throughput and abort rate are in "plain" / "learned".
 
 Extra sections: "hotspot" (1 % hot set drawing 30 % of the accesses, moving every 2^20
-transactions: learned vs plain), "uniform" (the same bank with uniform accounts, plain engine)
-and "memcd" (8-way cache of 2^20 sets, Zipf(0.99) keys over 4 M, 99 % GET rounds, 64 K-request
-batches: throughput and p50/p99 batch latency).
+transactions: learned vs plain), "uniform" (the same bank with uniform accounts, plain engine),
+"memcd" (8-way cache of 2^20 sets, Zipf(0.99) keys over 4 M, 99 % GET rounds, 64 K-request
+batches through the batch call: throughput and p50/p99 batch latency) and "serving" (the same
+cache behind the serving loop under open-loop Poisson arrivals at 10-100 % of its closed-loop
+peak, batches of 1 K-64 K requests, 95 % GET rounds: achieved req/s and p50/p99 latency).
 
 --impl reference runs the reference arm: the path's CPU execution (the oracle port, striped
 locks on every host core) on the same batches. --case NAME runs one small invocation of one
@@ -52,7 +54,7 @@ WORKLOAD = dict(seed=2026, pr_read_pct=20, ro_reads=32, up_reads=4, amt_lo=1, am
                 zipf_theta=0.99)
 B_UPDATE = 16 * 4 + 12 * 2   # algorithmic bytes of a transfer: 4 versioned reads, 2 writes
 B_RO = 16 * 32               # a 32-account read-only scan
-SCHED = dict(serial_lane=1, defer_threshold=0.0, probe_every=8, probe_rounds_pct=2)
+SCHED = dict(serial_lane=1, defer_threshold=0.0, probe_every=3, probe_rounds_pct=2)
 
 
 def parse():
@@ -68,8 +70,16 @@ def parse():
     ap.add_argument("--depth", type=int, default=int(os.environ.get("CSMV_DEPTH", 8)))
     ap.add_argument("--case", default=None, choices=["engine", "serial", "mlp", "memcd", "sched"])
     ap.add_argument("--no-extras", action="store_true", help="skip hotspot/uniform/memcd sections")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (use the flags)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
+
+
+T_START = time.perf_counter()
+
+
+def progress(msg: str) -> None:
+    print(f"[bench {time.perf_counter() - T_START:7.1f} s] {msg}", file=sys.stderr, flush=True)
 
 
 def dist_env():
@@ -346,6 +356,94 @@ def memcd_section(cg, local, n_batches=40):
                         "99% GET rounds, 64K-request batches, host buffers"}
 
 
+def serve_section(cg, local, loads=(0.1, 0.25, 0.5, 0.75, 1.0), per_load_s=1.5):
+    """Serving loop under open-loop Poisson arrivals: 2^20 sets x 8 ways, batches of U[1K, 64K]
+    requests (multiples of 32), 95 % GET rounds, Zipf(0.99) keys over 4 M. The peak is the
+    closed-loop throughput (submit as fast as admission allows); each offered load is a fraction
+    of it. Latency of a batch = completion seen by the host - its scheduled arrival."""
+    rng = np.random.default_rng(7)
+    pool_n = 1 << 21
+    pool = cg.memcd_generate(cg.memcd_workload(1 << 22, pool_n, seed=77, get_pct=95))
+    def draw():
+        n = int(rng.integers(1024 // 32, 65536 // 32 + 1)) * 32
+        lo = int(rng.integers(0, (pool_n - n) // 32 + 1)) * 32
+        return cg.requests_slice(pool, lo, lo + n)
+    out = {"workload": "2^20 sets x 8 ways, batches U[1K,64K] requests, 95% GET rounds, "
+                       "Zipf(0.99) over 4M keys, open-loop Poisson arrivals, host ring"}
+    def deadline_check(t_end, what):
+        if time.perf_counter() > t_end:
+            raise TimeoutError(f"serving: {what} exceeded its time budget")
+
+    with cg.Server(n_sets=1 << 20, client_warps=4, arena_requests=1 << 19,
+                   max_inflight_sets=1 << 16, idle_timeout_ms=5000, device=local) as srv:
+        srv.start()
+        fill = cg.memcd_generate(cg.memcd_workload(1 << 22, 1 << 16, seed=5, get_pct=0))
+        t_end = time.perf_counter() + 30
+        for _ in range(8):
+            b = None
+            while b is None:
+                b = srv.submit(fill)
+                deadline_check(t_end, "fill")
+            while srv.poll(b, results=False) is None:
+                deadline_check(t_end, "fill")
+        progress("serving: table filled")
+        # closed loop: keep the ring full
+        inflight, n_done, t0 = [], 0, time.perf_counter()
+        t_end = t0 + 30
+        while time.perf_counter() - t0 < 1.0:
+            req = draw()
+            b = srv.submit(req)
+            if b is not None:
+                inflight.append((b, req.n_req))
+            while inflight and srv.poll(inflight[0][0], results=False) is not None:
+                n_done += inflight.pop(0)[1]
+        while inflight:
+            deadline_check(t_end, "closed loop")
+            if srv.poll(inflight[0][0], results=False) is not None:
+                n_done += inflight.pop(0)[1]
+        peak = n_done / (time.perf_counter() - t0)
+        progress(f"serving: closed-loop peak {peak:.3g} req/s")
+        out["peak_req_s"] = peak
+        mean_n = (1024 + 65536) / 2
+        rows = []
+        for load in loads:
+            rate = load * peak / mean_n  # batches per second
+            n_b = max(20, int(rate * per_load_s))
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, n_b))
+            reqs = [draw() for _ in range(n_b)]
+            lat, pending, inflight = [], 0, []
+            served = 0
+            t0 = time.perf_counter()
+            t_end = t0 + per_load_s * 4 + 10
+            while pending < n_b or inflight:
+                deadline_check(t_end, f"load {load}")
+                now = time.perf_counter() - t0
+                if pending < n_b and now >= arrivals[pending]:
+                    b = srv.submit(reqs[pending])
+                    if b is not None:
+                        inflight.append((b, arrivals[pending], reqs[pending].n_req))
+                        pending += 1
+                i = 0
+                while i < len(inflight):
+                    b, arr, n = inflight[i]
+                    if srv.poll(b, results=False) is not None:
+                        lat.append(time.perf_counter() - t0 - arr)
+                        served += n
+                        inflight.pop(i)
+                    else:
+                        i += 1
+            span = time.perf_counter() - t0
+            lat = np.array(lat) * 1e3
+            rows.append({"offered_frac": load, "offered_req_s": load * peak,
+                         "achieved_req_s": served / span, "p50_ms": float(np.percentile(lat, 50)),
+                         "p99_ms": float(np.percentile(lat, 99)), "batches": n_b})
+            progress(f"serving: load {load}: p50 {rows[-1]['p50_ms']:.3f} ms")
+        st = srv.stop()
+        out["loads"] = rows
+        out["abort_rate"] = st.aborts / max(1, st.aborts + st.commits)
+    return out
+
+
 def cpu_baseline(bs, sample_txn=1 << 21):
     """The oracle's CPU executions of a bounded sample of the same batches: striped locks on
     every host core (reported) and one thread in stream order (for comparison)."""
@@ -470,12 +568,26 @@ def main():
     n_addr = int(s.addr.shape[0])
     dev = [DevBatch(torch, b) for b in host]
 
+    tuned = None
+    if not args.no_tune:  # the engine's launch shape for this workload, measured on a sample
+        progress("autotune")
+        sample = cg.Stream(np.ascontiguousarray(host[0].op[:1 << 16]),
+                           np.ascontiguousarray(host[0].off[:1 << 16]), host[0].addr)
+        best, trials = cg.autotune(sample, repeats=2, n_accounts=N_ACCOUNTS, init_value=1000,
+                                   device=local)
+        args.client_warps, args.ctas, args.depth = best.client_warps, best.ctas, best.version_depth
+        tuned = {"client_warps": best.client_warps, "ctas": best.ctas,
+                 "version_depth": best.version_depth, "candidates": len(trials),
+                 "sample_txn": 1 << 16}
     barrier(world)
+    progress("plain arm")
     plain, info = run_plain(cg, dev, addr_dev, n_addr, args, local, warm, timed)
     barrier(world)
+    progress("learned arm")
     with ClockSampler(local) as clk:
         learned = run_learned(torch, cg, dev, addr_dev, n_addr, args, local, warm, timed)
     barrier(world)
+    progress("e2e")
     t_learned = reduce_max(learned["wall"], world)
     value = learned["commits"] * world / t_learned
     t_plain = reduce_max(plain["ms"] * 1e-3, world)
@@ -505,7 +617,7 @@ def main():
         "data": "synthetic (seeded generator with the configured shapes)",
         "config": {"workload": workload_name(args), "l2": "inputs larger than L2 (28 MB/batch)",
                    "ctas": info["ctas"], "threads_per_cta": info["threads_per_cta"],
-                   "version_depth": args.depth, "scheduler": SCHED,
+                   "version_depth": args.depth, "autotuned": tuned, "scheduler": SCHED,
                    "parallelism": f"replicas x{world}"},
         "abort_rate": l_abort,
         "learned": {"tx_s": value, "abort_rate": l_abort,
@@ -527,10 +639,18 @@ def main():
         "clocks": clk.summary(),
     }
     if not args.no_extras:
-        line["hotspot"] = hotspot_section(torch, cg, local)
-        line["uniform"] = uniform_section(torch, cg, args, local)
-        line["memcd"] = memcd_section(cg, local)
+        sections = [("hotspot", lambda: hotspot_section(torch, cg, local)),
+                    ("uniform", lambda: uniform_section(torch, cg, args, local)),
+                    ("memcd", lambda: memcd_section(cg, local)),
+                    ("serving", lambda: serve_section(cg, local))]
+        for name, fn in sections:
+            progress(name)
+            try:
+                line[name] = fn()
+            except Exception as e:  # a section's failure is reported, not fatal to the line
+                line[name] = {"error": f"{type(e).__name__}: {e}"}
     if not args.no_cpu_baseline:
+        progress("cpu baseline")
         line["cpu_baseline"] = cpu_baseline(host)
     print(json.dumps(line))
 

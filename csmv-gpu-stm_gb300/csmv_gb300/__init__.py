@@ -104,6 +104,15 @@ class MemcdConfig(C.Structure):
         "max_req", "spin_limit_log2")] + [("device", C.c_int32)]
 
 
+class TuneTrial(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in ("client_warps", "ctas", "version_depth", "runs")] + [
+        ("status", C.c_int32), ("tx_per_s", C.c_double), ("abort_rate", C.c_double)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("best", BankConfig), ("n_trials", C.c_uint32), ("trials", TuneTrial * 64)]
+
+
 class ServeConfig(C.Structure):
     _fields_ = [(n, C.c_uint32) for n in ("n_sets", "client_warps", "ctas", "arena_requests",
                                           "max_inflight_sets", "idle_timeout_ms")] + [
@@ -184,6 +193,8 @@ def lib() -> C.CDLL:
         "csmv_mlp_get_grads": (I32, [P, P]),
         "csmv_mlp_adam_step": (I32, [P, C.c_float]),
         "csmv_mlp_destroy": (None, [P]),
+        "csmv_bank_autotune": (I32, [C.POINTER(BankConfig), C.POINTER(BankStream), P, U32,
+                                     C.POINTER(TuneResult)]),
         "csmv_serve_config_default": (None, [C.POINTER(ServeConfig)]),
         "csmv_serve_create": (I32, [C.POINTER(ServeConfig), C.POINTER(P)]),
         "csmv_serve_start": (I32, [P]),
@@ -755,6 +766,22 @@ class Scheduler:
                "csmv_sched_read_plan")
         n1 = n - 32 * pr.value
         return perm[:n1], pr.value, sp.value
+
+
+def autotune(stream: Stream, repeats: int = 3, init: np.ndarray | None = None, **base):
+    """Pick the engine's launch shape for a workload (csmv_bank_autotune). Returns (best
+    BankConfig, list of trial dicts)."""
+    cfg = bank_config(**base)
+    res = TuneResult()
+    s = stream.c_struct()
+    init_p = None
+    if init is not None:
+        init = np.ascontiguousarray(init, dtype=np.int32)
+        init_p = _ptr(init)
+    _check(lib().csmv_bank_autotune(C.byref(cfg), C.byref(s), init_p, repeats, C.byref(res)),
+           "csmv_bank_autotune")
+    trials = [{n: getattr(t, n) for n, _ in TuneTrial._fields_} for t in res.trials[:res.n_trials]]
+    return res.best, trials
 
 
 def cuda_device_present() -> bool:

@@ -478,3 +478,104 @@ extern "C" void csmv_bank_destroy(csmv_bank_t* h) {
   free_all(h);
   delete h;
 }
+
+// ---------------------------------------------------------------------------------------------
+// Autotuner: picks the engine's launch shape for a workload by measurement. Candidates: client
+// warps per CTA 1, 2, 4, 8 (block size; each client warp owns one mailbox of its CTA's server),
+// CTAs per SM (1 or 2, as co-residency allows) and versions per account (4, 8). Every candidate
+// runs the caller's sample once from the same initial state; the best quarter runs `repeats`
+// more times and the fastest median wins (successive halving).
+// ---------------------------------------------------------------------------------------------
+#include <algorithm>
+
+namespace {
+struct Trial {
+  csmv_bank_config cfg;
+  double best_ms = 1e30;
+  std::vector<double> ms;
+  double abort_rate = 0;
+  csmv_status st = CSMV_OK;
+};
+
+csmv_status tune_run(const csmv_bank_config& cfg, const csmv_bank_stream* s, const int32_t* init,
+                     uint32_t times, Trial& t) {
+  csmv_bank_t* h = nullptr;
+  csmv_status st = csmv_bank_create(&cfg, &h);
+  if (st != CSMV_OK) return st;
+  for (uint32_t i = 0; i < times && st == CSMV_OK; i++) {
+    if ((st = csmv_bank_load(h, init)) != CSMV_OK) break;
+    csmv_stats out;
+    if ((st = csmv_bank_run(h, s, &out)) != CSMV_OK) break;
+    t.ms.push_back(out.kernel_ms);
+    const double c = (double)(out.commits_update + out.commits_readonly + out.commits_nowrite);
+    const double a = (double)(out.aborts_data_age + out.aborts_record_age + out.aborts_read_write +
+                              out.aborts_prevalid + out.aborts_write_write);
+    t.abort_rate = a / std::max(1.0, a + c);
+  }
+  csmv_bank_destroy(h);
+  return st;
+}
+}  // namespace
+
+extern "C" csmv_status csmv_bank_autotune(const csmv_bank_config* base,
+                                          const csmv_bank_stream* host_sample,
+                                          const int32_t* host_init, uint32_t repeats,
+                                          csmv_tune_result* out) {
+  if (!base || !host_sample || !out || repeats == 0) return CSMV_ERR_INVALID_ARG;
+  std::memset(out, 0, sizeof(*out));
+  int n_sms = 0;
+  csmv_status st = check_device(base->device, &n_sms);
+  if (st != CSMV_OK) return st;
+  std::vector<Trial> trials;
+  for (uint32_t depth : {4u, 8u})
+    for (uint32_t cw : {1u, 2u, 4u, 8u})
+      for (uint32_t per_sm : {1u, 2u}) {
+        Trial t;
+        t.cfg = *base;
+        t.cfg.version_depth = depth;
+        t.cfg.client_warps = cw;
+        t.cfg.ctas = per_sm * (uint32_t)n_sms;
+        t.cfg.max_txn = std::max(base->max_txn, host_sample->n_txn);
+        t.cfg.log_commits = 0;
+        trials.push_back(t);
+      }
+  for (auto& t : trials) {
+    t.st = tune_run(t.cfg, host_sample, host_init, 1, t);
+    if (t.st == CSMV_OK) t.best_ms = t.ms.back();
+  }
+  std::vector<size_t> order(trials.size());
+  for (size_t i = 0; i < order.size(); i++) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return trials[a].best_ms < trials[b].best_ms; });
+  const size_t keep = std::max<size_t>(1, trials.size() / 4);
+  for (size_t r = 0; r < keep; r++) {
+    Trial& t = trials[order[r]];
+    if (t.st != CSMV_OK) continue;
+    t.st = tune_run(t.cfg, host_sample, host_init, repeats, t);
+    std::vector<double> m = t.ms;
+    std::sort(m.begin(), m.end());
+    t.best_ms = m[m.size() / 2];  // median over every run
+  }
+  size_t best = order[0];
+  for (size_t r = 0; r < keep; r++)
+    if (trials[order[r]].st == CSMV_OK && trials[order[r]].best_ms < trials[best].best_ms) best = order[r];
+  if (trials[best].st != CSMV_OK) {
+    set_error("autotune: no candidate ran (%s)", csmv_status_str(trials[best].st));
+    return trials[best].st;
+  }
+  out->best = trials[best].cfg;
+  out->best.log_commits = base->log_commits;
+  out->best.max_txn = base->max_txn;
+  out->n_trials = (uint32_t)std::min<size_t>(trials.size(), CSMV_TUNE_MAX_TRIALS);
+  for (uint32_t i = 0; i < out->n_trials; i++) {
+    const Trial& t = trials[i];
+    csmv_tune_trial& o = out->trials[i];
+    o.client_warps = t.cfg.client_warps;
+    o.ctas = t.cfg.ctas;
+    o.version_depth = t.cfg.version_depth;
+    o.runs = (uint32_t)t.ms.size();
+    o.status = (int32_t)t.st;
+    o.tx_per_s = t.st == CSMV_OK ? host_sample->n_txn / (t.best_ms * 1e-3) : 0.0;
+    o.abort_rate = t.abort_rate;
+  }
+  return CSMV_OK;
+}

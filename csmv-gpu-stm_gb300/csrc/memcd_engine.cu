@@ -610,6 +610,10 @@ extern "C" csmv_status csmv_serve_submit(csmv_serve_t* h, const csmv_memcd_batch
     set_error("serve submit: no session running");
     return CSMV_ERR_STATE;
   }
+  if (const uint32_t err = *reinterpret_cast<volatile uint32_t*>(&h->ctl->error)) {
+    set_error("serving kernel stopped with device error %u", err);
+    return CSMV_ERR_TIMEOUT;
+  }
   const uint32_t A = h->cfg.arena_requests, n = b->n_req;
   if (n > A) {
     set_error("batch of %u requests exceeds the arena (%u)", n, A);
@@ -664,7 +668,14 @@ extern "C" csmv_status csmv_serve_poll(csmv_serve_t* h, uint64_t batch_id, uint3
     *done = 1;
     return CSMV_OK;
   }
-  if (!batch_done(h, batch_id)) return CSMV_OK;
+  if (!batch_done(h, batch_id)) {
+    const uint32_t err = *reinterpret_cast<volatile uint32_t*>(&h->ctl->error);
+    if (err) {  // the session stopped on a device error: this batch will not complete
+      set_error("serving kernel stopped with device error %u", err);
+      return CSMV_ERR_TIMEOUT;
+    }
+    return CSMV_OK;
+  }
   h->collected[batch_id % kServeSlots] = true;
   const ServeBatchDesc& d = h->desc[batch_id % kServeSlots];
   const uint32_t A = h->cfg.arena_requests, n = d.n_req, first = d.first;

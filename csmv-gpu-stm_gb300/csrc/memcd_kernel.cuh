@@ -142,54 +142,79 @@ __device__ bool memcd_round(const MemcdParams& p, MemcdShared& sm, MemcdMail& ms
       }
 
       if (!is_set) {
-        // GET: read-only at the snapshot
+        // GET: the latest committed version of each way, read through its commit word and
+        // re-checked afterwards (a double collect), serialised at the largest stamp read. The
+        // stamp's version is never a writer's victim (that is the older slot), so its record
+        // stays put while the stamp does. Locks: a holder with a timestamp above the snapshot
+        // commits after it and is ignored; one below it, or one still without a timestamp when
+        // the GET looks, may commit inside the snapshot, so the GET waits (bounded) or retries.
         bool found = false, aged = false;
+        uint32_t smax = 0;
         uint4 o0 = make_uint4(0, 0, 0, 0), o1 = o0;
         if (mine) {
+          unsigned long long w1[kWays];
+#pragma unroll
+          for (int wy = 0; wy < kWays; wy++) w1[wy] = ld_relaxed_gpu(&p.cw[e0 + wy]);
+#pragma unroll
+          for (int wy = 0; wy < kWays; wy++) {
+            for (uint32_t it = 0; it < 512u; it++) {
+              const uint32_t own = (uint32_t)(w1[wy] >> 32);
+              if (own == 0u || (own & kPendingFlag)) break;
+              __nanosleep(64);
+              w1[wy] = ld_relaxed_gpu(&p.cw[e0 + wy]);
+            }
+          }
+          fence_acq_rel_gpu();  // versions after the stamps
+          unsigned long long tg2[kWays * D];
+#pragma unroll
+          for (int i = 0; i < kWays * D; i += 2)
+            ld_relaxed_gpu_v2(p.tag + (size_t)e0 * D + i, tg2[i], tg2[i + 1]);
           int pick[kWays];
           unsigned long long ptag[kWays];
 #pragma unroll
           for (int wy = 0; wy < kWays; wy++) {
-            int best = -1;
-            uint32_t bts = 0;
-            unsigned long long bt = 0;
+            const uint32_t st = (uint32_t)w1[wy], own = (uint32_t)(w1[wy] >> 32);
+            if (own != 0u && !(own & kPendingFlag)) aged = true;  // still no timestamp: retry
+            smax = max(smax, st);
+            int j = -1;
+            unsigned long long t0 = 0;
 #pragma unroll
-            for (int j = 0; j < D; j++) {
-              const uint32_t t = tag_ts(tg[wy * D + j]);
-              if (t != kEmptyTs && t <= snap && (best < 0 || t > bts)) {
-                best = j;
-                bts = t;
-                bt = tg[wy * D + j];
+            for (int q = 0; q < D; q++)
+              if (tag_ts(tg2[wy * D + q]) == st) {
+                j = q;
+                t0 = tg2[wy * D + q];
               }
-            }
-            pick[wy] = best;
-            ptag[wy] = bt;
-            aged |= best < 0;
+            pick[wy] = j;
+            ptag[wy] = t0;
+            aged |= j < 0;
           }
-          bool fenced = false;
+#pragma unroll
+          for (int wy = 0; wy < kWays; wy++) {
+            const uint32_t own = (uint32_t)(w1[wy] >> 32);
+            if ((own & kPendingFlag) && (own & ~kPendingFlag) < smax) aged = true;
+          }
 #pragma unroll
           for (int wy = 0; wy < kWays; wy++) {
             const unsigned long long t0 = ptag[wy];
             // skip: decided, or not valid, or another key's hash
             if (aged || found || (uint32_t)t0 != th) continue;
-            if (!fenced) {  // the record loads stay behind the tag loads (sequence lock)
-              fence_acq_rel_gpu();
-              fenced = true;
-            }
             const size_t v = (size_t)(e0 + wy) * D + pick[wy];
             const uint4 kk = ld_relaxed_gpu_v4(p.rec + v * 4 + 1);
-            const uint4 a0 = ld_relaxed_gpu_v4(p.rec + v * 4 + 2);
-            const uint4 a1 = ld_relaxed_gpu_v4(p.rec + v * 4 + 3);
-            fence_acq_rel_gpu();
-            if (ld_relaxed_gpu(p.tag + v) != t0) {  // overwritten meanwhile: retry
-              aged = true;
-              continue;
-            }
             if (key_eq(kk, key)) {
               found = true;
-              o0 = a0;
-              o1 = a1;
+              o0 = ld_relaxed_gpu_v4(p.rec + v * 4 + 2);
+              o1 = ld_relaxed_gpu_v4(p.rec + v * 4 + 3);
             }
+          }
+          fence_acq_rel_gpu();
+#pragma unroll
+          for (int wy = 0; wy < kWays; wy++) {  // the second collect
+            const unsigned long long w2 = ld_relaxed_gpu(&p.cw[e0 + wy]);
+            const uint32_t own = (uint32_t)(w2 >> 32);
+            if ((uint32_t)w2 != (uint32_t)w1[wy]) aged = true;
+            if ((own & kPendingFlag) && (own & ~kPendingFlag) < smax) aged = true;
+            // a holder without a timestamp that locked after the first collect draws its
+            // timestamp after every stamp read here: it lands above the snapshot
           }
         }
         const bool done = mine && !aged;
@@ -197,7 +222,9 @@ __device__ bool memcd_round(const MemcdParams& p, MemcdShared& sm, MemcdMail& ms
           p.found[r] = found ? 1u : 0u;
           p.val_out[2 * r] = o0;
           p.val_out[2 * r + 1] = o1;
-          if (p.log) p.outcome[r] = snap | kSnapFlag;
+          // every commit up to the clock read before the first collect was visible to it, so
+          // the state read is also the state at that clock when it is the later of the two
+          if (p.log) p.outcome[r] = max(smax, snap) | kSnapFlag;
         }
         const uint32_t dm = __ballot_sync(0xFFFFFFFFu, done);
         const uint32_t am = __ballot_sync(0xFFFFFFFFu, mine && aged);
@@ -456,15 +483,16 @@ __global__ void __launch_bounds__(512, 1) memcd_kernel(MemcdParams p) {
 // rounds in order and run them with the cache's commit protocol, so rounds of different batches
 // overlap on the device. After a round, the warp makes its results visible to the host and
 // counts the round off its batch; the batch's last round stamps done_ns and sets done (release).
-// The kernel returns once ctl->stop is set and every published batch has completed, or after
-// idle_ns without work (error ERR_WAIT_REQUEST).
+// The kernel returns once ctl->stop is set and every published batch has completed, or when the
+// host has published nothing for idle_ns (error ERR_WAIT_REQUEST).
 // ---------------------------------------------------------------------------------------------
 constexpr uint32_t kServeSlots = 1024;  // batch descriptors in flight at most
 
-struct ServeHostCtl {     // mapped host memory, written by the host
-  uint32_t submitted;     // batches published
-  uint32_t stop;          // finish what is published, then return
-  uint32_t pad[14];
+struct ServeHostCtl {     // mapped host memory
+  uint32_t submitted;     // host: batches published
+  uint32_t stop;          // host: finish what is published, then return
+  uint32_t error;         // device: first device error of the session (0 = none)
+  uint32_t pad[13];
 };
 
 struct ServeBatchDesc {   // mapped host memory, one per in-flight batch (slot = batch % kServeSlots)
@@ -544,7 +572,8 @@ __device__ void serve_client(const MemcdParams& p, const ServeParams& s, MemcdSh
   const uint32_t lane = lane_id();
   const uint32_t me = blockIdx.x * p.nc + w + 1;
   uint32_t seq = 0;
-  unsigned long long idle_since = 0;
+  unsigned long long idle_since = 0;  // since when the host has published nothing new
+  uint32_t last_sub = 0xFFFFFFFFu;
   for (;;) {
     uint32_t got = 0u, first = 0u, slot = 0u;
     if (lane == 0) {
@@ -570,11 +599,19 @@ __device__ void serve_client(const MemcdParams& p, const ServeParams& s, MemcdSh
         const uint32_t sub = ld_acquire_sys(&s.ctl->submitted);
         const uint32_t adm = ld_relaxed_gpu(&s.dev->admitted);
         const unsigned long long now = globaltimer_ns();
-        if (idle_since == 0) idle_since = now;
-        if (ld_relaxed_gpu(&p.gs->error)) leave = 1;
-        else if (stop && adm == sub && h >= t) leave = 1;
-        else if (now - idle_since > s.idle_ns) {
+        if (sub != last_sub || h < t) {  // the host published, or work is queued: not idle
+          last_sub = sub;
+          idle_since = now;
+        }
+        const uint32_t err = ld_relaxed_gpu(&p.gs->error);
+        if (err) {
+          st_release_sys(&s.ctl->error, err);  // the host sees it without waiting for the end
+          leave = 1;
+        } else if (stop && adm == sub && h >= t) {
+          leave = 1;
+        } else if (now - idle_since > s.idle_ns) {
           raise_error(&p.gs->error, ERR_WAIT_REQUEST);
+          st_release_sys(&s.ctl->error, ERR_WAIT_REQUEST);
           leave = 1;
         }
       }
@@ -582,13 +619,15 @@ __device__ void serve_client(const MemcdParams& p, const ServeParams& s, MemcdSh
       __nanosleep(200);
       continue;
     }
-    idle_since = 0;
     first = __shfl_sync(0xFFFFFFFFu, first, 0);
     slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
     uint32_t tk = 0;
     if (lane == 0) tk = ld_relaxed_gpu(&s.tick[slot]);
     tk = __shfl_sync(0xFFFFFFFFu, tk, 0);
-    if (!memcd_round(p, sm, ms, me, (first + lane) & s.arena_mask, seq, tk)) break;
+    if (!memcd_round(p, sm, ms, me, (first + lane) & s.arena_mask, seq, tk)) {
+      if (lane == 0) st_release_sys(&s.ctl->error, max(1u, ld_relaxed_gpu(&p.gs->error)));
+      break;
+    }
     __syncwarp();
     if (lane == 0) {
       __threadfence_system();  // this round's results reach the host before its batch completes

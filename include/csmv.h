@@ -486,6 +486,29 @@ csmv_status csmv_sched_read_plan(csmv_sched_t* s, uint32_t* host_perm, uint32_t 
 csmv_mlp_t* csmv_sched_mlp(csmv_sched_t* s);
 void csmv_sched_destroy(csmv_sched_t* s);
 
+/* ------------------------------------------------------------------------------------------
+ * Autotuner (no counterpart in the reference, whose launch shape is fixed on the command line):
+ * measures the engine on a sample of the caller's stream over client warps per CTA (1, 2, 4,
+ * 8: the block size and the number of mailboxes per commit-server warp), CTAs per SM (1, 2)
+ * and versions per account (4, 8), with the rest of *base fixed; every candidate runs once from
+ * host_init (NULL: base->init_value), the best quarter `repeats` more times, and the fastest
+ * median wins. out->best is *base with the winning shape.
+ * ------------------------------------------------------------------------------------------ */
+#define CSMV_TUNE_MAX_TRIALS 64
+typedef struct csmv_tune_trial {
+  uint32_t client_warps, ctas, version_depth, runs;
+  int32_t status;             /* csmv_status of the candidate (e.g. does not fit)           */
+  double tx_per_s;            /* committed tx/s of the sample (median over runs)            */
+  double abort_rate;
+} csmv_tune_trial;
+typedef struct csmv_tune_result {
+  csmv_bank_config best;
+  uint32_t n_trials;
+  csmv_tune_trial trials[CSMV_TUNE_MAX_TRIALS];
+} csmv_tune_result;
+csmv_status csmv_bank_autotune(const csmv_bank_config* base, const csmv_bank_stream* host_sample,
+                               const int32_t* host_init, uint32_t repeats, csmv_tune_result* out);
+
 /* Page-locked host buffers for staging streams (the e2e path copies from pinned memory).
  * Replaces CUDA_DUAL_ALLOC's cudaMallocHost half (memcachedGPU/cuda_util.h:50-60). */
 csmv_status csmv_pinned_alloc(size_t bytes, void** out);
