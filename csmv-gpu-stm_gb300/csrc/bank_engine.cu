@@ -33,6 +33,16 @@ KernelFn pick_kernel(uint32_t depth) {
   }
 }
 
+KernelFn pick_cluster(uint32_t depth) {
+  switch (depth) {
+    case 2: return bank_cluster_kernel<2, kMaxR, kMaxW>;
+    case 4: return bank_cluster_kernel<4, kMaxR, kMaxW>;
+    case 8: return bank_cluster_kernel<8, kMaxR, kMaxW>;
+    case 16: return bank_cluster_kernel<16, kMaxR, kMaxW>;
+    default: return nullptr;
+  }
+}
+
 size_t serial_smem(uint32_t depth) {
   switch (depth) {
     case 2: return serial_smem_bytes<2, kMaxR>();
@@ -112,7 +122,14 @@ static csmv_status validate_config(const csmv_bank_config* c) {
   if (c->client_warps < 1 || c->client_warps > (uint32_t)kMaxClientWarps) return bad("client_warps");
   if (c->validate > CSMV_VALIDATE_RING_LANE) return bad("validate");
   if (c->writeback > CSMV_WRITEBACK_SERVER) return bad("writeback");
-  if (c->batch > CSMV_BATCH_CTA) return bad("batch (cluster batching is not built)");
+  if (c->batch > CSMV_BATCH_CLUSTER) return bad("batch");
+  if (c->batch == CSMV_BATCH_CLUSTER) {
+    if (c->validate != CSMV_VALIDATE_STAMP) return bad("cluster batching runs the stamp protocol");
+    if (c->cluster_size != 2 && c->cluster_size != 4 && c->cluster_size != 8)
+      return bad("cluster_size must be 2, 4 or 8");
+    if (c->client_warps * c->cluster_size > 32)
+      return bad("client_warps x cluster_size must be <= 32 (one server lane per mailbox)");
+  }
   if (c->validate != CSMV_VALIDATE_STAMP && c->batch == CSMV_BATCH_LANE &&
       c->writeback != CSMV_WRITEBACK_SERVER)
     return bad("per-transaction sections need server write-back");
@@ -157,9 +174,11 @@ extern "C" csmv_status csmv_bank_create(const csmv_bank_config* cfg, csmv_bank_t
   csmv_bank_t* h = new csmv_bank_t;
   h->cfg = *cfg;
   h->n_sms = n_sms;
-  h->kernel = pick_kernel(cfg->version_depth);
+  const bool cluster = cfg->batch == CSMV_BATCH_CLUSTER;
+  h->kernel = cluster ? pick_cluster(cfg->version_depth) : pick_kernel(cfg->version_depth);
   h->threads = (int)(cfg->client_warps + 1) * 32;
-  h->smem = cta_shared_bytes<kMaxR, kMaxW>(cfg->client_warps);
+  // cluster form: every CTA reserves the cluster's mailboxes; the leader's are used
+  h->smem = cta_shared_bytes<kMaxR, kMaxW>(cfg->client_warps * (cluster ? cfg->cluster_size : 1u));
   auto fail = [&](csmv_status s) {
     free_all(h);
     delete h;
@@ -174,12 +193,35 @@ extern "C" csmv_status csmv_bank_create(const csmv_bank_config* cfg, csmv_bank_t
                                              (int)serial_smem(cfg->version_depth)),
                         "cudaFuncSetAttribute")) != CSMV_OK)
     return fail(st);
-  int per_sm = 0;
-  if ((st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, h->kernel,
-                                                                       h->threads, h->smem),
-                        "occupancy")) != CSMV_OK)
-    return fail(st);
-  const int max_ctas = per_sm * n_sms;
+  int max_ctas = 0;
+  if (cluster) {
+    cudaLaunchConfig_t lc = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cfg->cluster_size;
+    at[0].val.clusterDim.y = at[0].val.clusterDim.z = 1;
+    lc.gridDim = dim3(cfg->cluster_size * (uint32_t)n_sms);
+    lc.blockDim = dim3(h->threads);
+    lc.dynamicSmemBytes = h->smem;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    int clusters = 0;
+    if ((st = cuda_status(cudaOccupancyMaxActiveClusters(&clusters, (const void*)h->kernel, &lc),
+                          "cluster occupancy")) != CSMV_OK)
+      return fail(st);
+    max_ctas = clusters * (int)cfg->cluster_size;
+    if (cfg->ctas && cfg->ctas % cfg->cluster_size) {
+      set_error("ctas must be a multiple of cluster_size");
+      return fail(CSMV_ERR_INVALID_ARG);
+    }
+  } else {
+    int per_sm = 0;
+    if ((st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, h->kernel,
+                                                                         h->threads, h->smem),
+                          "occupancy")) != CSMV_OK)
+      return fail(st);
+    max_ctas = per_sm * n_sms;
+  }
   if (max_ctas <= 0) {
     set_error("kernel does not fit on an SM (threads %d, smem %zu)", h->threads, h->smem);
     return fail(CSMV_ERR_INVALID_ARG);
@@ -294,6 +336,20 @@ static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* of
   if (serial) {
     pick_serial(c.version_depth)<<<1, 32, serial_smem(c.version_depth), h->stream>>>(p);
     CSMV_CUDA(cudaGetLastError());
+  } else if (c.batch == CSMV_BATCH_CLUSTER) {
+    // clusters of cluster_size CTAs; the grid never exceeds the co-resident clusters
+    cudaLaunchConfig_t lc = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = c.cluster_size;
+    at[0].val.clusterDim.y = at[0].val.clusterDim.z = 1;
+    lc.gridDim = dim3(h->ctas);
+    lc.blockDim = dim3(h->threads);
+    lc.dynamicSmemBytes = h->smem;
+    lc.stream = h->stream;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    CSMV_CUDA(cudaLaunchKernelExC(&lc, (const void*)h->kernel, args));
   } else {
     CSMV_CUDA(cudaLaunchCooperativeKernel((const void*)h->kernel, dim3(h->ctas), dim3(h->threads),
                                           args, h->smem, h->stream));

@@ -30,6 +30,8 @@
 
 #include "../../include/csmv.h"
 #include "../../include/csmv_tx.cuh"
+#include <cooperative_groups.h>
+
 #include "csmv_prims.cuh"
 
 namespace csmv {
@@ -279,9 +281,11 @@ __device__ __forceinline__ void batch_done(const BankParams& p, CtaShared<MAXR, 
 // ---------------------------------------------------------------------------------------------
 // client side
 // ---------------------------------------------------------------------------------------------
-template <int DEPTH, int MAXR, int MAXW>
-__device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint32_t w) {
-  MailSlot<MAXR, MAXW>& ms = sm.mail[w];
+// CLUSTER: the mailbox `ms` (and the finished-client counter) live in the shared memory of the
+// cluster's leader CTA, reached through distributed shared memory; else in this CTA's.
+template <int DEPTH, int MAXR, int MAXW, bool CLUSTER = false>
+__device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint32_t w,
+                            MailSlot<MAXR, MAXW>& ms, uint32_t* done_ctr) {
   const uint32_t lane = lane_id();
   const VersionStore vs{p.slots, p.n_items};
   const bool stamp = p.validate == CSMV_VALIDATE_STAMP;
@@ -521,18 +525,18 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
           if (lane == 0) {
             ms.snap = snap;
             ms.cand = cand;
-            st_release_cta(&ms.req, seq);
+            mail_release<CLUSTER>(&ms.req, seq);
           }
           bool ok_wait = true;
           if (lane == 0)
-            ok_wait = bounded_wait([&] { return ld_acquire_cta(&ms.rep) == seq; }, &p.gs->error,
+            ok_wait = bounded_wait([&] { return mail_acquire<CLUSTER>(&ms.rep) == seq; }, &p.gs->error,
                                    ERR_WAIT_REPLY, p.spin_log2);
           ok_wait = __shfl_sync(0xFFFFFFFFu, ok_wait, 0);
           if (!ok_wait) {
             failed = true;
             break;
           }
-          (void)ld_acquire_cta(&ms.rep);
+          (void)mail_acquire<CLUSTER>(&ms.rep);
           base = ms.base;
           my_ts = base + 1 + __popc(cand & lanemask_lt());
           fence_acq_rel_gpu();
@@ -736,18 +740,18 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
       if (lane == 0) {
         ms.snap = snap;
         ms.cand = cand;
-        st_release_cta(&ms.req, seq);
+        mail_release<CLUSTER>(&ms.req, seq);
       }
       bool ok_wait = true;
       if (lane == 0)
-        ok_wait = bounded_wait([&] { return ld_acquire_cta(&ms.rep) == seq; }, &p.gs->error,
+        ok_wait = bounded_wait([&] { return mail_acquire<CLUSTER>(&ms.rep) == seq; }, &p.gs->error,
                                ERR_WAIT_REPLY, p.spin_log2);
       ok_wait = __shfl_sync(0xFFFFFFFFu, ok_wait, 0);
       if (!ok_wait) {
         failed = true;
         break;
       }
-      (void)ld_acquire_cta(&ms.rep);
+      (void)mail_acquire<CLUSTER>(&ms.rep);
 
       uint32_t okm = 0, my_ts = 0;
       if (stamp) {
@@ -843,7 +847,7 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
     if (p.txn_aborts) p.txn_aborts[t] = tries - 1u;
   }
   __syncwarp();
-  if (lane == 0) atomicAdd(&sm.done_warps, 1u);
+  if (lane == 0) atomicAdd(done_ctr, 1u);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -853,18 +857,18 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
 // Polls the mailboxes of the CTA's client warps; returns the ready mask (0 = none), sets
 // *stop when every client finished or an error was raised. SM is any CTA layout with
 // mail[w].{req,rep,cand,base} slots and done_warps/stat fields.
-template <class SM>
+template <class SM, bool CLUSTER = false>
 __device__ __forceinline__ uint32_t poll_mailboxes(uint32_t nc, GlobalSync* gs, SM& sm,
                                                    uint32_t seen, uint32_t* req, bool* stop) {
   const uint32_t lane = lane_id();
   *req = 0;
-  if (lane < nc) *req = ld_acquire_cta(&sm.mail[lane].req);
+  if (lane < nc) *req = mail_acquire<CLUSTER>(&sm.mail[lane].req);
   const uint32_t ready = __ballot_sync(0xFFFFFFFFu, lane < nc && *req != seen);
   *stop = false;
   if (ready == 0) {
     uint32_t done = 0, err = 0;
     if (lane == 0) {
-      done = *(volatile uint32_t*)&sm.done_warps;
+      done = CLUSTER ? ld_acquire_cluster(&sm.done_warps) : *(volatile uint32_t*)&sm.done_warps;
       err = ld_relaxed_gpu(&gs->error);
     }
     done = __shfl_sync(0xFFFFFFFFu, done, 0);
@@ -877,14 +881,14 @@ __device__ __forceinline__ uint32_t poll_mailboxes(uint32_t nc, GlobalSync* gs, 
 // Stamp protocol server: one atomicAdd draws consecutive timestamps for every ready warp
 // (batched commit-timestamp assignment, batchedAtrInsert/csmv_sh/API.cu:331-361, here per CTA
 // batch instead of per warp); warp w gets (base_w, base_w + count_w].
-template <class SM>
+template <class SM, bool CLUSTER = false>
 __device__ void server_warp_stamp(uint32_t nc, uint32_t batch, GlobalSync* gs, SM& sm) {
   const uint32_t lane = lane_id();
   uint32_t seen = 0;
   for (;;) {
     uint32_t req;
     bool stop;
-    uint32_t ready = poll_mailboxes(nc, gs, sm, seen, &req, &stop);
+    uint32_t ready = poll_mailboxes<SM, CLUSTER>(nc, gs, sm, seen, &req, &stop);
     if (ready == 0) {
       if (stop) break;
       __nanosleep(64);
@@ -914,7 +918,7 @@ __device__ void server_warp_stamp(uint32_t nc, uint32_t batch, GlobalSync* gs, S
     t0 = __shfl_sync(0xFFFFFFFFu, t0, 0);
     if (mine) {
       sm.mail[lane].base = t0 + incl - cnt;
-      st_release_cta(&sm.mail[lane].rep, seen);
+      mail_release<CLUSTER>(&sm.mail[lane].rep, seen);
     }
     if (lane == 0) stat_add(sm.stat, ST_SECTIONS, 1);
   }
@@ -1649,9 +1653,43 @@ __global__ void __launch_bounds__(512, 1) bank_kernel(BankParams p) {
     else
       server_warp_ring<DEPTH, MAXR, MAXW>(p, sm);
   } else {
-    client_warp<DEPTH, MAXR, MAXW>(p, sm, warp - 1);
+    client_warp<DEPTH, MAXR, MAXW>(p, sm, warp - 1, sm.mail[warp - 1], &sm.done_warps);
   }
   __syncthreads();
+  for (uint32_t i = threadIdx.x; i < ST_COUNT; i += blockDim.x)
+    if (sm.stat[i]) atomicAdd(&p.stats[i], sm.stat[i]);
+}
+
+// The thread-block-cluster form (one commit server for several blocks; the reference has no
+// cluster code): the client warps of every CTA of a cluster post to the commit-server warp of
+// the cluster's leader CTA, through mailboxes in the leader's shared memory reached over
+// distributed shared memory. Stamp protocol only.
+template <int DEPTH, int MAXR, int MAXW>
+__global__ void __launch_bounds__(512, 1) bank_cluster_kernel(BankParams p) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  CtaShared<MAXR, MAXW>& sm = *reinterpret_cast<CtaShared<MAXR, MAXW>*>(smem_raw);
+  const uint32_t warp = threadIdx.x >> 5, rank = cluster.block_rank(), cs = cluster.num_blocks();
+  const uint32_t nct = p.nc * cs;  // mailboxes of the cluster (<= 32)
+  if (threadIdx.x == 0) {
+    sm.done_warps = 0;
+    sm.next_bid = 0;
+  }
+  for (uint32_t i = threadIdx.x; i < ST_COUNT; i += blockDim.x) sm.stat[i] = 0;
+  for (uint32_t i = threadIdx.x; i < nct; i += blockDim.x) {
+    sm.mail[i].req = 0;
+    sm.mail[i].rep = 0;
+  }
+  cluster.sync();  // the leader's mailboxes are set before any client posts
+  CtaShared<MAXR, MAXW>* lead = cluster.map_shared_rank(&sm, 0);
+  if (warp == 0) {
+    if (rank == 0) server_warp_stamp<CtaShared<MAXR, MAXW>, true>(nct, p.batch, p.gs, sm);
+  } else {
+    client_warp<DEPTH, MAXR, MAXW, true>(p, sm, warp - 1, lead->mail[rank * p.nc + warp - 1],
+                                         &lead->done_warps);
+  }
+  cluster.sync();  // no CTA leaves while its mailboxes in the leader may still be touched
   for (uint32_t i = threadIdx.x; i < ST_COUNT; i += blockDim.x)
     if (sm.stat[i]) atomicAdd(&p.stats[i], sm.stat[i]);
 }

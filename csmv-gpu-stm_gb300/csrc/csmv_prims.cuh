@@ -125,6 +125,29 @@ __device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) 
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;" ::: "memory");
 }
+// Cluster scope through generic addresses (the caller's shared memory or another CTA's of the
+// cluster, as mapped by cluster.map_shared_rank): mailboxes of a thread-block cluster.
+__device__ __forceinline__ uint32_t ld_acquire_cluster(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.cluster.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_cluster(uint32_t* p, uint32_t v) {
+  asm volatile("st.release.cluster.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// Mailbox handshakes at the scope the mailbox is shared at.
+template <bool CLUSTER>
+__device__ __forceinline__ uint32_t mail_acquire(const uint32_t* p) {
+  return CLUSTER ? ld_acquire_cluster(p) : ld_acquire_cta(p);
+}
+template <bool CLUSTER>
+__device__ __forceinline__ void mail_release(uint32_t* p, uint32_t v) {
+  if (CLUSTER)
+    st_release_cluster(p, v);
+  else
+    st_release_cta(p, v);
+}
+
 // System scope: words shared with the host through mapped (zero-copy) host memory.
 __device__ __forceinline__ uint32_t ld_acquire_sys(const uint32_t* p) {
   uint32_t v;

@@ -136,8 +136,11 @@ enum {
   CSMV_BATCH_LANE = 0,  /* one transaction per section (plain TXAddToRecord, API.cu:193-272)  */
   CSMV_BATCH_WARP = 1,  /* one client warp per section (batchedAtrInsert TXAddToRecord)        */
   CSMV_BATCH_CTA = 2,   /* every pending client warp of the CTA in one section                 */
-  CSMV_BATCH_CLUSTER = 3 /* client warps of a thread-block cluster post to one server warp
-                            through distributed shared memory                                  */
+  CSMV_BATCH_CLUSTER = 3 /* client warps of a thread-block cluster post to the server warp of
+                            the cluster's leader CTA through distributed shared memory (one
+                            server for several blocks; no counterpart in the reference);
+                            stamp protocol, client_warps x cluster_size <= 32, ctas a
+                            multiple of cluster_size                                           */
 };
 
 typedef struct csmv_bank_config {
@@ -147,7 +150,7 @@ typedef struct csmv_bank_config {
   uint32_t ring_size;          /* commit-record ring entries, power of two, >= 64             */
   uint32_t client_warps;       /* client warps per CTA (1..15)                                */
   uint32_t ctas;               /* CTAs; 0 = as many as fit co-resident on the GPU             */
-  uint32_t cluster_size;       /* CTAs per cluster for CSMV_BATCH_CLUSTER (2..8)               */
+  uint32_t cluster_size;       /* CTAs per cluster for CSMV_BATCH_CLUSTER (2, 4 or 8)          */
   uint32_t validate;           /* CSMV_VALIDATE_*                                             */
   uint32_t writeback;          /* CSMV_WRITEBACK_*                                            */
   uint32_t batch;              /* CSMV_BATCH_*                                                */

@@ -41,7 +41,9 @@ def test_library_loads_and_reports_version():
 def test_config_validation_is_a_status():
     for bad in (dict(version_depth=3), dict(ring_size=100), dict(client_warps=0),
                 dict(client_warps=16), dict(validate=1, batch=0, writeback=0), dict(max_txn=33),
-                dict(spin_limit_log2=2), dict(n_accounts=1), dict(batch=9)):
+                dict(spin_limit_log2=2), dict(n_accounts=1), dict(batch=9),
+                dict(batch=3, validate=1, writeback=1), dict(batch=3, cluster_size=3),
+                dict(batch=3, cluster_size=4, client_warps=15)):
         with pytest.raises(cg.CsmvError) as e:
             cg.Bank(cg.bank_config(**bad))
         assert e.value.status == 1, bad

@@ -50,6 +50,8 @@ VARIANTS = {
     "ringlane-warp-client": dict(validate=cg.VALIDATE_RING_LANE, batch=cg.BATCH_WARP),
     "stamp-cta-noprevalid": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CTA, prevalidate=0),
     "stamp-cta-chain": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CTA, prevalidate=2),
+    "stamp-cluster2": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CLUSTER, cluster_size=2),
+    "stamp-cluster8": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CLUSTER, cluster_size=8),
 }
 
 
