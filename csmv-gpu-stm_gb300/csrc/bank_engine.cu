@@ -12,16 +12,13 @@
 #include <cstring>
 #include <vector>
 
-#include "bank_kernel.cuh"
-#include "common.h"
+#include "bank_internal.h"
 
 using namespace csmv;
 
 namespace {
 constexpr int kMaxR = 8;
 constexpr int kMaxW = 2;
-constexpr uint32_t kDoneWords = 1u << 16;  // 2^21 timestamps in flight at most
-using KernelFn = void (*)(BankParams);
 
 KernelFn pick_kernel(uint32_t depth) {
   switch (depth) {
@@ -63,32 +60,6 @@ KernelFn pick_serial(uint32_t depth) {
   }
 }
 }  // namespace
-
-struct csmv_bank_t {
-  csmv_bank_config cfg{};
-  int n_sms = 0, ctas = 0, threads = 0;
-  size_t smem = 0, device_bytes = 0;
-  KernelFn kernel = nullptr;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  unsigned long long* slots = nullptr;
-  unsigned long long* cw = nullptr;
-  uint4* ring = nullptr;
-  uint32_t* done = nullptr;
-  uint32_t log_cap = 0;
-  GlobalSync* gs = nullptr;
-  uint32_t* log_txn = nullptr;
-  uint32_t* outcome = nullptr;
-  int32_t* result = nullptr;
-  unsigned long long* stats = nullptr;
-  uint32_t* d_op = nullptr;
-  uint32_t* d_off = nullptr;
-  uint32_t* d_addr = nullptr;
-  uint32_t* d_aborts = nullptr;
-  uint64_t addr_cap = 0;
-  bool loaded = false;
-  uint32_t last_final_ts = 0, last_n_txn = 0, run_base_ts = 0;
-};
 
 extern "C" void csmv_bank_config_default(csmv_bank_config* c) {
   if (!c) return;
@@ -152,6 +123,8 @@ static void free_all(csmv_bank_t* h) {
   cudaFree(h->d_off);
   cudaFree(h->d_addr);
   cudaFree(h->d_aborts);
+  flow_scratch_free(h->flow);
+  h->flow = nullptr;
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -269,6 +242,10 @@ extern "C" csmv_status csmv_bank_load(csmv_bank_t* h, const int32_t* host_values
   CSMV_CUDA(cudaMemsetAsync(h->ring, 0, (size_t)h->cfg.ring_size * 16, h->stream));
   CSMV_CUDA(cudaMemsetAsync(h->done, 0, (size_t)kDoneWords * 4, h->stream));
   CSMV_CUDA(cudaMemsetAsync(h->gs, 0, sizeof(GlobalSync), h->stream));
+  if (h->flow) {
+    csmv_status st = flow_scratch_reset(h->flow, h->stream);
+    if (st != CSMV_OK) return st;
+  }
   CSMV_CUDA(cudaStreamSynchronize(h->stream));
   h->loaded = true;
   h->last_final_ts = 0;
@@ -276,7 +253,7 @@ extern "C" csmv_status csmv_bank_load(csmv_bank_t* h, const int32_t* host_values
   return CSMV_OK;
 }
 
-static csmv_status check_stream(const csmv_bank_t* h, const csmv_bank_stream* s) {
+csmv_status csmv::check_stream(const csmv_bank_t* h, const csmv_bank_stream* s) {
   if (!s || !s->op || !s->off || !s->addr || s->n_txn == 0 || s->n_txn % 32) {
     set_error("stream: n_txn must be a positive multiple of 32 with op/off/addr set");
     return CSMV_ERR_INVALID_ARG;
@@ -292,10 +269,8 @@ static csmv_status check_stream(const csmv_bank_t* h, const csmv_bank_stream* s)
   return CSMV_OK;
 }
 
-static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* off,
-                          const uint32_t* addr, uint32_t n_txn, uint32_t* txn_aborts,
-                          uint32_t split_round, uint32_t deferred_warps, csmv_stats* out,
-                          bool serial = false) {
+BankParams csmv::bank_params(const csmv_bank_t* h, const uint32_t* op, const uint32_t* off,
+                             const uint32_t* addr, uint32_t n_txn, uint32_t* txn_aborts) {
   const csmv_bank_config& c = h->cfg;
   BankParams p{};
   p.op = op;
@@ -324,36 +299,21 @@ static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* of
   p.prevalidate = c.prevalidate;
   p.spin_log2 = c.spin_limit_log2;
   p.txn_aborts = txn_aborts;
-  p.split_round = split_round;
-  p.deferred_warps = deferred_warps;
+  return p;
+}
+
+csmv_status csmv::bank_begin_run(csmv_bank_t* h) {
   // the commit order carries on from the previous run: only the cursors and error reset
   CSMV_CUDA(cudaMemsetAsync(&h->gs->round_next, 0, 4, h->stream));
   CSMV_CUDA(cudaMemsetAsync(&h->gs->round_deferred, 0, 4, h->stream));
   CSMV_CUDA(cudaMemsetAsync(&h->gs->error, 0, 4, h->stream));
   CSMV_CUDA(cudaMemsetAsync(h->stats, 0, ST_COUNT * 8, h->stream));
-  void* args[] = {&p};
   CSMV_CUDA(cudaEventRecord(h->ev0, h->stream));
-  if (serial) {
-    pick_serial(c.version_depth)<<<1, 32, serial_smem(c.version_depth), h->stream>>>(p);
-    CSMV_CUDA(cudaGetLastError());
-  } else if (c.batch == CSMV_BATCH_CLUSTER) {
-    // clusters of cluster_size CTAs; the grid never exceeds the co-resident clusters
-    cudaLaunchConfig_t lc = {};
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = c.cluster_size;
-    at[0].val.clusterDim.y = at[0].val.clusterDim.z = 1;
-    lc.gridDim = dim3(h->ctas);
-    lc.blockDim = dim3(h->threads);
-    lc.dynamicSmemBytes = h->smem;
-    lc.stream = h->stream;
-    lc.attrs = at;
-    lc.numAttrs = 1;
-    CSMV_CUDA(cudaLaunchKernelExC(&lc, (const void*)h->kernel, args));
-  } else {
-    CSMV_CUDA(cudaLaunchCooperativeKernel((const void*)h->kernel, dim3(h->ctas), dim3(h->threads),
-                                          args, h->smem, h->stream));
-  }
+  return CSMV_OK;
+}
+
+csmv_status csmv::bank_end_run(csmv_bank_t* h, uint32_t n_txn, csmv_stats* out) {
+  const csmv_bank_config& c = h->cfg;
   CSMV_CUDA(cudaEventRecord(h->ev1, h->stream));
   unsigned long long st[ST_COUNT];
   GlobalSync gs;
@@ -382,11 +342,47 @@ static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* of
     out->kernel_ms = ms;
   }
   if (gs.error) {
-    set_error("device error %u (1 turn, 2 clock, 3 reply, 4 request, 5 capacity, 6 data, 7 livelock)",
+    set_error("device error %u (1 turn, 2 clock, 3 reply, 4 request, 5 capacity, 6 data, "
+              "7 livelock, 8 dataflow wait)",
               gs.error);
     return gs.error == ERR_DATA ? CSMV_ERR_INVALID_ARG : CSMV_ERR_TIMEOUT;
   }
   return CSMV_OK;
+}
+
+static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* off,
+                          const uint32_t* addr, uint32_t n_txn, uint32_t* txn_aborts,
+                          uint32_t split_round, uint32_t deferred_warps, csmv_stats* out,
+                          bool serial = false) {
+  const csmv_bank_config& c = h->cfg;
+  BankParams p = bank_params(h, op, off, addr, n_txn, txn_aborts);
+  p.split_round = split_round;
+  p.deferred_warps = deferred_warps;
+  csmv_status bst = bank_begin_run(h);
+  if (bst != CSMV_OK) return bst;
+  void* args[] = {&p};
+  if (serial) {
+    pick_serial(c.version_depth)<<<1, 32, serial_smem(c.version_depth), h->stream>>>(p);
+    CSMV_CUDA(cudaGetLastError());
+  } else if (c.batch == CSMV_BATCH_CLUSTER) {
+    // clusters of cluster_size CTAs; the grid never exceeds the co-resident clusters
+    cudaLaunchConfig_t lc = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = c.cluster_size;
+    at[0].val.clusterDim.y = at[0].val.clusterDim.z = 1;
+    lc.gridDim = dim3(h->ctas);
+    lc.blockDim = dim3(h->threads);
+    lc.dynamicSmemBytes = h->smem;
+    lc.stream = h->stream;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    CSMV_CUDA(cudaLaunchKernelExC(&lc, (const void*)h->kernel, args));
+  } else {
+    CSMV_CUDA(cudaLaunchCooperativeKernel((const void*)h->kernel, dim3(h->ctas), dim3(h->threads),
+                                          args, h->smem, h->stream));
+  }
+  return bank_end_run(h, n_txn, out);
 }
 
 extern "C" csmv_status csmv_bank_run_device(csmv_bank_t* h, const csmv_bank_stream* s,

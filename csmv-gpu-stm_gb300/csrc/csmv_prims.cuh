@@ -64,6 +64,17 @@ __device__ __forceinline__ void fence_acq_rel_gpu() {
 }
 
 
+// Global words shared only by the threads of one CTA (one SM): CTA scope lets the SM's L1 serve
+// them. Each 8-byte access is single-copy atomic.
+__device__ __forceinline__ unsigned long long ld_relaxed_cta_global(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.cta.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_cta_global(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.cta.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 // ---- shared (cta scope) -------------------------------------------------------------------
 __device__ __forceinline__ uint32_t ld_acquire_cta(const uint32_t* p) {
   uint32_t v;
@@ -88,7 +99,8 @@ enum : uint32_t {
   ERR_WAIT_REQUEST = 4,  // the server saw no progress from its clients
   ERR_CAPACITY = 5,      // read/write set or batch capacity exceeded
   ERR_DATA = 6,          // malformed transaction (bad size / address)
-  ERR_LIVELOCK = 7       // a round exhausted its attempt budget without committing
+  ERR_LIVELOCK = 7,      // a round exhausted its attempt budget without committing
+  ERR_WAIT_FLOW = 8      // a dataflow-lane transaction's inputs never arrived
 };
 
 __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t code) {

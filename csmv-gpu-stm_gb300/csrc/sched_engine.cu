@@ -81,7 +81,7 @@ extern "C" csmv_status csmv_sched_create(const csmv_sched_config* cfg, csmv_sche
   *out = nullptr;
   if (cfg->n_accounts < 2 || cfg->max_txn == 0 || cfg->max_txn % 32 || cfg->max_txn > (1u << 26) ||
       cfg->probe_rounds_pct > 100 || cfg->probe_every == 0 || !(cfg->lr > 0.f) ||
-      cfg->deferred_warps == 0) {
+      cfg->deferred_warps == 0 || cfg->serial_lane > 2) {
     set_error("invalid scheduler config");
     return CSMV_ERR_INVALID_ARG;
   }
@@ -330,7 +330,8 @@ extern "C" csmv_status csmv_sched_serial_run(csmv_sched_t* s, csmv_bank_t* bank,
   rs.txn_aborts = nullptr;
   rs.split_round = rs.deferred_warps = 0;
   csmv_stats bst;
-  csmv_status st = csmv_bank_run_serial_device(bank, &rs, &bst);
+  csmv_status st = s->cfg.serial_lane == 2 ? csmv_bank_run_flow_device(bank, &rs, &bst)
+                                            : csmv_bank_run_serial_device(bank, &rs, &bst);
   if (rep) {
     rep->serial = bst;
     rep->n_serial = n;

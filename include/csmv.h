@@ -210,6 +210,19 @@ csmv_status csmv_bank_run_device(csmv_bank_t* h, const csmv_bank_stream* dev_str
 csmv_status csmv_bank_run_serial_device(csmv_bank_t* h, const csmv_bank_stream* dev_stream,
                                         csmv_stats* out);
 
+/* Dataflow lane (no counterpart in the reference): the same contract and the same end state as
+ * csmv_bank_run_serial_device - timestamps, version slots, commit words, log, outcomes and
+ * results are identical - but every transaction whose inputs are known runs at once. Each read
+ * is matched to the last earlier write of its account in the stream by a device radix sort;
+ * one CTA then runs the transactions, each as soon as its producers have published, and the
+ * commit (timestamps, log, version installs) is written in parallel. Limits per call: 2^25
+ * transactions, 2^26 accesses (CSMV_ERR_CAPACITY). A malformed transaction (bad size, account
+ * or mixed round) fails the call with nothing applied (CSMV_ERR_INVALID_ARG). Device scratch
+ * of about 28 B per access and 40 B per transaction is kept by the handle after the first
+ * call. */
+csmv_status csmv_bank_run_flow_device(csmv_bank_t* h, const csmv_bank_stream* dev_stream,
+                                      csmv_stats* out);
+
 /* Replaces TXEnd (bank/csmv_sh/API.cu:335-359): latest value of every account. */
 csmv_status csmv_bank_read_values(csmv_bank_t* h, int32_t* host_values);
 
@@ -451,7 +464,8 @@ typedef struct csmv_sched_config {
   float threshold;            /* predicted abort probability above which a transfer is spaced */
   float defer_threshold;      /* above this it is deferred (> 1 = never)                      */
   uint32_t deferred_warps;    /* warps serving the deferred queue                             */
-  uint32_t serial_lane;       /* 1: deferred transfers run on the serial lane after the rest  */
+  uint32_t serial_lane;       /* deferred transfers run after the rest: 1 on the serial lane,
+                                 2 on the dataflow lane (csmv_bank_run_flow_device)           */
   uint64_t seed;
   int32_t device;
 } csmv_sched_config;
@@ -459,7 +473,7 @@ typedef struct csmv_sched_config {
 typedef struct csmv_sched_report {
   csmv_stats probe;           /* engine statistics of the probe run                          */
   csmv_stats planned;         /* ... of the planned run                                      */
-  csmv_stats serial;          /* ... and of the serial-lane run (serial_lane = 1)            */
+  csmv_stats serial;          /* ... and of the serial- or dataflow-lane run               */
   float loss;                 /* mean cross-entropy on the probe slice before this chunk's steps */
   uint32_t n_probe, n_planned, n_flagged, n_deferred_rounds, n_serial;
   double train_ms, plan_ms;   /* device time of training / of features, inference and planning */

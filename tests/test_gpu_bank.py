@@ -223,6 +223,113 @@ def test_serial_lane_equals_stream_order_execution(dist):
     assert (np.diff(writers) > 0).all() and (log_txn == writers).all()  # stream order
 
 
+FLOW_CASES = {
+    "zipf-depth4": dict(n_acc=2048, n=32 * 600, dist=cg.DIST_ZIPF, depth=4, up_reads=4, ro=20),
+    "uniform-depth8": dict(n_acc=1 << 16, n=1 << 15, dist=cg.DIST_UNIFORM, depth=8, up_reads=4,
+                           ro=20),
+    "hot16-depth2": dict(n_acc=16, n=32 * 200, dist=cg.DIST_UNIFORM, depth=2, up_reads=3, ro=30),
+    "zipf-depth16-transfers": dict(n_acc=1 << 14, n=1 << 14, dist=cg.DIST_ZIPF, depth=16,
+                                   up_reads=4, ro=0),
+    "two-accounts-always": dict(n_acc=2, n=32 * 40, dist=cg.DIST_UNIFORM, depth=4, up_reads=2,
+                                ro=0, kind=cg.KIND_TRANSFER_ALWAYS),
+    "zipf-self-transfers": dict(n_acc=512, n=32 * 300, dist=cg.DIST_ZIPF, depth=4, up_reads=3,
+                                ro=10, self_every=5),
+}
+
+
+@pytest.mark.parametrize("case", list(FLOW_CASES))
+def test_flow_lane_equals_serial_lane(case):
+    """The dataflow lane leaves exactly what the serial lane leaves - versions in the same slots,
+    commit log, outcomes, results, statistics - and its run replays exactly."""
+    torch = pytest.importorskip("torch")
+    c = FLOW_CASES[case]
+    n_acc, n, depth = c["n_acc"], c["n"], c["depth"]
+    w = c1_workload(n_txn=n, n_accounts=n_acc, dist=c["dist"], zipf_theta=0.99,
+                    up_reads=c["up_reads"], pr_read_pct=c["ro"], seed=21,
+                    kind=c.get("kind", cg.KIND_TRANSFER))
+    s = cg.generate(w)
+    if "self_every" in c:  # some transfers name one account twice: it is written once
+        t = np.flatnonzero((s.op & 3) != 0)[:: c["self_every"]]
+        s.addr[s.off[t] + 1] = s.addr[s.off[t]]
+    ds, keep = to_device(torch, s)
+    res = []
+    for lane in ("serial", "flow"):
+        with cg.Bank(n_accounts=n_acc, max_txn=n, version_depth=depth) as bank:
+            bank.load()
+            st = bank.run_serial_device(ds) if lane == "serial" else bank.run_flow_device(ds)
+            res.append((st, bank.log(n, st.final_ts), bank.versions(), bank.values()))
+    (s1, l1, v1, b1), (s2, l2, v2, b2) = res
+    assert s2.error == 0 and s2.commits == n and s2.aborts == 0
+    for f in ("commits_update", "commits_readonly", "commits_nowrite", "final_ts", "rounds",
+              "sections"):
+        assert getattr(s1, f) == getattr(s2, f), f
+    for a, b in zip(l1, l2):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(v1, v2)
+    np.testing.assert_array_equal(b1, b2)
+    init = np.full(n_acc, 1000, np.int32)
+    ref, _ = orc.serial(s.op, s.off, s.addr, n_acc, init)
+    np.testing.assert_array_equal(b2, ref)
+    if "self_every" not in c:  # a self-transfer keeps only its credit: the total is not invariant
+        err = orc.check(s.op, s.off, s.addr, n_acc, init, depth, s2.final_ts, *l2, v2)
+        assert err is None, err
+
+
+def test_flow_lane_interleaves_with_engine_and_serial_lane():
+    """Concurrent run, dataflow run, serial-lane run, dataflow run on one bank: the commit order
+    carries across them and the concatenated log replays exactly."""
+    torch = pytest.importorskip("torch")
+    n_acc, n = 4096, 32 * 512
+    w = c1_workload(n_txn=4 * n, n_accounts=n_acc, seed=17, dist=cg.DIST_ZIPF, zipf_theta=0.9,
+                    up_reads=4)
+    s = cg.generate(w)
+    parts = [sub_stream(s, i * n, (i + 1) * n) for i in range(4)]
+    logs, outs, ress = [], [], []
+    with cg.Bank(n_accounts=n_acc, max_txn=n, ctas=8, client_warps=4) as bank:
+        bank.load()
+        prev = 0
+        for i, part in enumerate(parts):
+            ds, keep = to_device(torch, part)
+            run = [bank.run_device, bank.run_flow_device, bank.run_serial_device,
+                   bank.run_flow_device][i]
+            st = run(ds)
+            lt, oc, rs = bank.log(n, st.final_ts - prev)
+            logs.append(np.where(lt != 0xFFFFFFFF, lt + i * n, lt).astype(np.uint32))
+            outs.append(oc)
+            ress.append(rs)
+            prev = st.final_ts
+        slots = bank.versions()
+    err = orc.check(s.op, s.off, s.addr, n_acc, np.full(n_acc, 1000, np.int32), 4, prev,
+                    np.concatenate(logs), np.concatenate(outs), np.concatenate(ress), slots)
+    assert err is None, err
+
+
+def test_flow_lane_rejects_a_bad_account_and_applies_nothing():
+    """An account id past the bank fails the call (CSMV_ERR_INVALID_ARG); the checks run before
+    any access, so the bank is left as it was and the next run is exact."""
+    torch = pytest.importorskip("torch")
+    n_acc, n = 1024, 32 * 64
+    w = c1_workload(n_txn=2 * n, n_accounts=n_acc, seed=23, pr_read_pct=0)
+    s = cg.generate(w)
+    bad = cg.Stream(s.op[:n].copy(), s.off[:n].copy(), s.addr.copy())
+    bad.addr[bad.off[n // 2] + 1] = n_acc + 5
+    with cg.Bank(n_accounts=n_acc, max_txn=n) as bank:
+        bank.load()
+        before = bank.versions()
+        dbad, keep = to_device(torch, bad)
+        with pytest.raises(cg.CsmvError):
+            bank.run_flow_device(dbad)
+        np.testing.assert_array_equal(bank.versions(), before)
+        ds, keep2 = to_device(torch, sub_stream(s, n, 2 * n))
+        st = bank.run_flow_device(ds)
+        log_txn, outcome, result = bank.log(n, st.final_ts)
+        slots = bank.versions()
+    tail = sub_stream(s, n, 2 * n)
+    err = orc.check(tail.op, tail.off, tail.addr, n_acc, np.full(n_acc, 1000, np.int32), 4,
+                    st.final_ts, log_txn, outcome, result, slots)
+    assert err is None, err
+
+
 def test_engine_and_serial_lane_runs_interleave_exactly():
     """Concurrent run, serial-lane run, concurrent run on one bank: the commit order carries
     across them and the concatenated log replays exactly."""

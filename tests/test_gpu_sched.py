@@ -95,9 +95,11 @@ def test_trained_scheduler_lowers_abort_rate_on_shifting_hotspot():
     assert res["learned"][0] <= 0.7 * res["plain"][0], res
 
 
-def test_serial_lane_plan_replays_exactly():
-    """With serial_lane set, transfers scored above defer_threshold run on the serial lane after
-    the concurrent part; probe, concurrent and serial runs replay exactly together."""
+@pytest.mark.parametrize("lane", [1, 2])
+def test_serial_lane_plan_replays_exactly(lane):
+    """With serial_lane set, transfers scored above defer_threshold run on the serial lane (1) or
+    the dataflow lane (2) after the concurrent part; probe, concurrent and deferred runs replay
+    exactly together."""
     torch = pytest.importorskip("torch")
     n_acc, n = 1 << 14, 1 << 15
     w = c1_workload(n_txn=n, n_accounts=n_acc, dist=cg.DIST_ZIPF, zipf_theta=0.99, seed=9,
@@ -106,7 +108,7 @@ def test_serial_lane_plan_replays_exactly():
     ds, keep = to_device(torch, s)
     with cg.Bank(n_accounts=n_acc, max_txn=n, ctas=16, client_warps=4) as bank, \
             cg.Scheduler(n_accounts=n_acc, max_txn=n, threshold=0.0, defer_threshold=0.0,
-                         serial_lane=1, train_steps=2) as sched:
+                         serial_lane=lane, train_steps=2) as sched:
         bank.load()
         r1 = sched.probe(bank, ds)
         f1, np_ = r1.probe.final_ts, r1.n_probe
