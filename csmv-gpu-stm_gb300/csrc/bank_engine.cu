@@ -106,6 +106,7 @@ static csmv_status validate_config(const csmv_bank_config* c) {
     return bad("per-transaction sections need server write-back");
   if (c->max_txn == 0 || c->max_txn % 32) return bad("max_txn must be a positive multiple of 32");
   if (c->spin_limit_log2 < 10 || c->spin_limit_log2 > 30) return bad("spin_limit_log2");
+  if (c->flow_warps > 16) return bad("flow_warps must be 0 (default) or 1..16");
   return CSMV_OK;
 }
 

@@ -86,6 +86,8 @@ csmv_status ensure_txn(csmv_bank_t* h, uint32_t n) {
         (st = grow(&f->agg, kScanMaxTiles + 1)) != CSMV_OK)
       return st;
     CSMV_CUDA(cudaMallocHost((void**)&f->host_total, 4));
+    CSMV_CUDA(cudaFuncSetAttribute((const void*)flow_exec_kernel,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FlowSmem)));
     CSMV_CUDA(cudaMemsetAsync(f->cnt, 0, (size_t)f->items * 4, h->stream));
   }
   FlowScratch* f = h->flow;
@@ -192,7 +194,8 @@ csmv_status flow_launch(csmv_bank_t* h, const csmv_bank_stream* s) {
     f->epoch = 1;
   }
   p.epoch = f->epoch;
-  flow_exec_kernel<<<1, kFlowExecThreads, 0, st>>>(p);
+  const uint32_t warps = h->cfg.flow_warps ? h->cfg.flow_warps : kFlowExecWarps;
+  flow_exec_kernel<<<1, 32 * warps, sizeof(FlowSmem), st>>>(p);
   CSMV_CUDA(cudaGetLastError());
   if ((rc = scan<false>(f->wflag, n, f->agg, st)) != CSMV_OK) return rc;
   flow_finalize_kernel<<<grid_of(n, 256), 256, 0, st>>>(p);

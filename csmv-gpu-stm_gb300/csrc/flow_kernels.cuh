@@ -15,12 +15,12 @@
 //              takes the account's latest committed version, looked up here
 //   tails      the last write of each account, where its installs start
 // Execution (one CTA, flow_exec_kernel): warp w runs the blocks of 32 consecutive transactions
-//   w, w + 32, w + 64, ...; each lane polls the output words (epoch << 32 | value) of its
-//   reads' producers until all have arrived, runs its transfer and publishes the value of each
-//   account it writes - new, or unchanged when the funds were short. Outputs are written and
-//   polled at CTA scope, so the SM's L1 carries the hand-offs. A transaction waits only on
-//   earlier ones and the earliest unfinished one has all its inputs, so the lane always makes
-//   progress; the polls are bounded all the same (ERR_WAIT_FLOW).
+//   w, w + 32, w + 64, ...; each lane polls its reads' producers' outputs until all have
+//   arrived, runs its transfer and publishes the value of each account it writes - new, or
+//   unchanged when the funds were short - to a shared-memory ring (the chain hand-offs) and to
+//   global memory. A transaction waits only on earlier ones and the earliest unfinished one has
+//   all its inputs, so the lane always makes progress; the polls are bounded all the same
+//   (ERR_WAIT_FLOW).
 // Commit (all SMs):
 //   ranks      exclusive scan of the has-write flags: the writers take consecutive timestamps in
 //              stream order, as in the serial lane
@@ -39,7 +39,8 @@ constexpr uint32_t kFlowWrite = 64;                      // element codes >= 64 
 constexpr uint32_t kFlowMaxTxn = 1u << 25;               // element values pack txn << 7 | code
 constexpr uint32_t kFlowMaxElem = 1u << 26;              // accesses per call
 constexpr unsigned long long kFlowValue = 1ull << 63;    // src word: a value, no producer
-constexpr uint32_t kFlowExecThreads = 1024;
+constexpr uint32_t kFlowExecThreads = 512;   // the execution CTA at most (16 warps)
+constexpr uint32_t kFlowExecWarps = 8;       // ... and by default
 
 struct FlowParams {
   BankParams b;              // stream, version store, commit words, log, sync words, statistics
@@ -319,79 +320,231 @@ __global__ void __launch_bounds__(256) flow_src_kernel(FlowParams f, const uint3
 }
 
 // ---------------------------------------------------------------------------------------------
-// Execution: one CTA of kFlowExecThreads threads.
+// Execution: one CTA of kFlowExecThreads threads (32 warps).
+//
+// Outputs go to a ring in shared memory (the hand-offs of a dependency chain take a shared-memory
+// round trip) and to `out` in global memory (read by consumers far behind their producer and by
+// the installs). Ring word of transaction j's slot s, at (2j + s) mod 2R: (j + 1) << 32 | value.
+// A warp starts block b only when every block <= b - G has finished (per-warp finished-block
+// counters). Then a consumer in block c reads producer block bj from the ring when c - bj < G -
+// the ring slot cannot have been reused yet, as its next writer, block bj + R/32, waits for c
+// (R/32 >= 2G - 1) - and from `out` otherwise, where the producer has certainly finished.
 // ---------------------------------------------------------------------------------------------
+constexpr uint32_t kFlowRing = 8192;  // transactions whose outputs the ring holds (R)
+constexpr uint32_t kFlowGate = 128;   // blocks a warp may run ahead of the oldest unfinished (G)
+static_assert(kFlowRing / 32 >= 2 * kFlowGate - 1, "ring reach");
+static_assert((kFlowRing & (kFlowRing - 1)) == 0, "ring size");
+constexpr uint32_t kFlowReadsInRegs = 8;  // a transfer's producers are held in registers
+
+struct FlowSmem {
+  unsigned long long ring[2 * kFlowRing];
+  uint32_t prog[32];  // blocks finished by each warp
+  uint32_t failed;
+};
+
+__device__ __forceinline__ unsigned long long ld_relaxed_cta_shared(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.cta.shared.u64 %0, [%1];"
+               : "=l"(v)
+               : "r"((uint32_t)__cvta_generic_to_shared(p))
+               : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_cta_shared(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.cta.shared.u64 [%0], %1;" ::"r"((uint32_t)__cvta_generic_to_shared(p)),
+               "l"(v)
+               : "memory");
+}
+
+// Value of a read with source word s, for a consumer in block c; false while it has not arrived.
+__device__ __forceinline__ bool flow_fetch(const FlowParams& f, FlowSmem& S, unsigned long long s,
+                                           uint32_t c, unsigned long long tag, uint32_t& x) {
+  if (s & kFlowValue) {
+    x = (uint32_t)s;
+    return true;
+  }
+  const uint32_t j = (uint32_t)s >> 1;
+  if (c - (j >> 5) < kFlowGate) {
+    const unsigned long long wv = ld_relaxed_cta_shared(&S.ring[(uint32_t)s & (2u * kFlowRing - 1u)]);
+    x = (uint32_t)wv;
+    return (uint32_t)(wv >> 32) == j + 1u;
+  }
+  const unsigned long long wv = ld_relaxed_cta_global(&f.out[s]);
+  x = (uint32_t)wv;
+  return (wv & 0xFFFFFFFF00000000ull) == tag;
+}
+
+// Entry k (< kFlowReadsInRegs) of a lane's register array, without local memory.
+template <class T>
+__device__ __forceinline__ T pick(const T (&a)[kFlowReadsInRegs], uint32_t k) {
+  T s = a[0];
+#pragma unroll
+  for (uint32_t q = 1; q < kFlowReadsInRegs; q++) s = k == q ? a[q] : s;
+  return s;
+}
+
+// A transfer's static inputs (producers, committed values, written accounts, divisor) are read
+// at the start of its block, and so are the outputs of producers at least G blocks older (they
+// have finished). What is left are producers in the ring, with their ring word and tag worked
+// out once: a lane polls them in read order and stops at the first that has not arrived, so a
+// pass costs a blocked lane one shared-memory load. A finished transfer publishes to the ring at
+// once and leaves its global outputs, flags and counts for the end of the block: the passes that
+// carry the dependency chain stay short.
 __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowParams f) {
-  __shared__ uint32_t failed;
+  extern __shared__ __align__(16) unsigned char flow_smem_raw[];
+  FlowSmem& S = *reinterpret_cast<FlowSmem*>(flow_smem_raw);
   const uint32_t lane = lane_id(), w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const uint32_t nb = f.n_txn / 32u;
   const unsigned long long tag = (unsigned long long)f.epoch << 32;
   uint32_t* err = &f.b.gs->error;
   const unsigned long long limit = 1ull << f.b.spin_log2;
-  if (threadIdx.x == 0) failed = ld_relaxed_gpu(err);
+  for (uint32_t k = threadIdx.x; k < 2u * kFlowRing; k += blockDim.x) S.ring[k] = 0ull;
+  if (threadIdx.x < 32) S.prog[threadIdx.x] = 0u;
+  if (threadIdx.x == 0) S.failed = ld_relaxed_gpu(err);
   __syncthreads();
-  if (failed) return;
+  if (S.failed) return;
+  // bounded poll bookkeeping: false when the warp must leave (budget spent or an error raised)
+  auto keep_polling = [&](unsigned long long it) {
+    if (it >= limit) {
+      if (lane == 0) raise_error(err, ERR_WAIT_FLOW);
+      return false;
+    }
+    if ((it & 1023ull) == 1023ull) {
+      uint32_t e = 0;
+      if (lane == 0) e = ld_relaxed_gpu(err);
+      if (__shfl_sync(0xFFFFFFFFu, e, 0)) return false;
+    }
+    return true;
+  };
+  uint32_t finished = 0;  // this warp's blocks
+  uint32_t op_n = 0, e0_n = 0;  // the next block's op and element offset, loaded ahead
+  if (w < nb) {
+    op_n = f.b.op[w * 32u + lane];
+    e0_n = f.eoff[w * 32u + lane];
+  }
   for (uint32_t b = w; b < nb; b += nw) {
     const uint32_t i = b * 32u + lane;
-    const uint32_t op = f.b.op[i], e0 = f.eoff[i];
+    const uint32_t op = op_n, e0 = e0_n;
+    if (b + nw < nb) {
+      op_n = f.b.op[i + 32u * nw];
+      e0_n = f.eoff[i + 32u * nw];
+    }
     const uint32_t nr = CSMV_OP_NREADS(op);
     const bool ro = CSMV_OP_KIND(op) == CSMV_KIND_READONLY;
-    unsigned long long pend = (1ull << nr) - 1ull;  // nr <= 63
+    unsigned long long sv[kFlowReadsInRegs];
+    uint32_t a0 = 0, a1 = 0;
+    if (!ro) {
+      const uint32_t off = f.b.off[i];
+#pragma unroll
+      for (uint32_t k = 0; k < kFlowReadsInRegs; k++) sv[k] = k < nr ? __ldg(&f.src[e0 + k]) : kFlowValue;
+      a0 = f.b.addr[off];
+      a1 = f.b.addr[off + 1];
+    }
+    if (b >= kFlowGate) {  // every block <= b - G finished
+      const uint32_t q = b - kFlowGate;
+      for (unsigned long long it = 0;; ++it) {
+        bool ok = true;
+        if (lane < nw) ok = ld_acquire_cta(&S.prog[lane]) >= (q >= lane ? (q - lane) / nw + 1u : 0u);
+        if (__all_sync(0xFFFFFFFFu, ok)) break;
+        if (!keep_polling(it)) return;
+      }
+      __syncwarp();
+    }
     int32_t v0 = 0, v1 = 0;
     uint32_t acc = 0;  // extra reads of a transfer; every read past the first two of a scan
-    bool done = false;
+    unsigned long long pend = 0, gpend = 0;  // reads waiting on the ring / on global memory
+    auto take = [&](uint32_t k, uint32_t x) {
+      if (k == 0)
+        v0 = (int32_t)x;
+      else if (k == 1)
+        v1 = (int32_t)x;
+      else
+        acc += x;
+    };
+    const ModMagic mm(ro ? 1u : CSMV_OP_AMOD(op));
+    uint32_t ridx[kFlowReadsInRegs], rtag[kFlowReadsInRegs];
+    if (!ro) {
+      // committed values, and outputs of producers that finished (all loads issued together)
+      unsigned long long gv[kFlowReadsInRegs];
+#pragma unroll
+      for (uint32_t k = 0; k < kFlowReadsInRegs; k++) {
+        const unsigned long long s = sv[k];
+        gv[k] = s;
+        if (k < nr && !(s & kFlowValue) && b - ((uint32_t)s >> 6) >= kFlowGate)
+          gv[k] = ld_relaxed_cta_global(&f.out[s]);
+        ridx[k] = (uint32_t)s & (2u * kFlowRing - 1u);
+        rtag[k] = ((uint32_t)s >> 1) + 1u;
+      }
+#pragma unroll
+      for (uint32_t k = 0; k < kFlowReadsInRegs; k++) {
+        if (k >= nr) continue;
+        const unsigned long long s = sv[k];
+        if (s & kFlowValue) {
+          take(k, (uint32_t)s);
+        } else if (b - ((uint32_t)s >> 6) >= kFlowGate) {
+          if ((gv[k] & 0xFFFFFFFF00000000ull) == tag)
+            take(k, (uint32_t)gv[k]);
+          else
+            gpend |= 1ull << k;
+        } else {
+          pend |= 1ull << k;
+        }
+      }
+    } else {
+      gpend = (1ull << nr) - 1ull;  // a scan: every read through flow_fetch (nr <= 63)
+    }
+    bool done = false, hw = false;
+    uint32_t o0 = 0, o1 = 0;
     for (unsigned long long it = 0;; ++it) {
       if (!done) {
-        for (unsigned long long m = pend; m; m &= m - 1ull) {
+        while (pend) {
+          const uint32_t k = (uint32_t)__ffsll((long long)pend) - 1u;
+          const unsigned long long wv = ld_relaxed_cta_shared(&S.ring[pick(ridx, k)]);
+          if ((uint32_t)(wv >> 32) != pick(rtag, k)) break;
+          take(k, (uint32_t)wv);
+          pend &= pend - 1ull;
+        }
+        for (unsigned long long m = gpend; m; m &= m - 1ull) {
           const uint32_t k = (uint32_t)__ffsll((long long)m) - 1u;
-          const unsigned long long s = __ldg(&f.src[e0 + k]);
-          const bool direct = (s & kFlowValue) != 0ull;
-          const unsigned long long wv = direct ? s : ld_relaxed_cta_global(&f.out[s]);
-          if (direct || (wv & 0xFFFFFFFF00000000ull) == tag) {
-            const uint32_t x = (uint32_t)wv;
-            if (k == 0)
-              v0 = (int32_t)x;
-            else if (k == 1)
-              v1 = (int32_t)x;
-            else
-              acc += x;
-            pend &= ~(1ull << k);
+          uint32_t x;
+          if (flow_fetch(f, S, ro ? __ldg(&f.src[e0 + k]) : pick(sv, k), b, tag, x)) {
+            take(k, x);
+            gpend &= ~(1ull << k);
           }
         }
-        if (pend == 0ull) {
+        if ((pend | gpend) == 0ull) {
           done = true;
-          if (ro) {
-            if (f.b.log) f.b.result[i] = (int32_t)((uint32_t)v0 + (uint32_t)v1 + acc);
-            f.wflag[i] = 0u;
-          } else {
-            const uint32_t off = f.b.off[i];
-            const uint32_t a0 = f.b.addr[off], a1 = f.b.addr[off + 1];
-            const uint32_t amt = 1u + (CSMV_OP_AMT0(op) - 1u + acc) % CSMV_OP_AMOD(op);
-            const bool hw = CSMV_OP_KIND(op) == CSMV_KIND_TRANSFER_ALWAYS || v0 >= (int32_t)amt;
-            const uint32_t o0 = hw ? (uint32_t)v0 - amt : (uint32_t)v0;
-            const uint32_t o1 = hw ? (uint32_t)v1 + amt : (uint32_t)v1;
-            if (a0 != a1) st_relaxed_cta_global(&f.out[2u * i], tag | o0);
-            st_relaxed_cta_global(&f.out[2u * i + 1u], tag | o1);
-            f.wflag[i] = hw ? 1u : 0u;
-            if (hw) {
-              atomicAdd(&f.cnt[a0], 1u);
-              if (a1 != a0) atomicAdd(&f.cnt[a1], 1u);
-            }
+          if (!ro) {
+            const uint32_t amt = 1u + mm.mod(CSMV_OP_AMT0(op) - 1u + acc);
+            hw = CSMV_OP_KIND(op) == CSMV_KIND_TRANSFER_ALWAYS || v0 >= (int32_t)amt;
+            o0 = hw ? (uint32_t)v0 - amt : (uint32_t)v0;
+            o1 = hw ? (uint32_t)v1 + amt : (uint32_t)v1;
+            const unsigned long long rt = (unsigned long long)(i + 1u) << 32;
+            const uint32_t r0 = (2u * i) & (2u * kFlowRing - 1u);
+            if (a0 != a1) st_relaxed_cta_shared(&S.ring[r0], rt | o0);
+            st_relaxed_cta_shared(&S.ring[r0 + 1u], rt | o1);
           }
         }
       }
       if (__all_sync(0xFFFFFFFFu, done)) break;
       __syncwarp();  // this pass's outputs before the next pass's polls
-      if (it >= limit) {
-        if (lane == 0) raise_error(err, ERR_WAIT_FLOW);
-        return;
-      }
-      if ((it & 1023ull) == 1023ull) {
-        uint32_t e = 0;
-        if (lane == 0) e = ld_relaxed_gpu(err);
-        if (__shfl_sync(0xFFFFFFFFu, e, 0)) return;
+      if (!keep_polling(it)) return;
+    }
+    // off the chain: global outputs, flags, counts, scan results
+    if (ro) {
+      if (f.b.log) f.b.result[i] = (int32_t)((uint32_t)v0 + (uint32_t)v1 + acc);
+      f.wflag[i] = 0u;
+    } else {
+      if (a0 != a1) st_relaxed_cta_global(&f.out[2u * i], tag | o0);
+      st_relaxed_cta_global(&f.out[2u * i + 1u], tag | o1);
+      f.wflag[i] = hw ? 1u : 0u;
+      if (hw) {
+        atomicAdd(&f.cnt[a0], 1u);
+        if (a1 != a0) atomicAdd(&f.cnt[a1], 1u);
       }
     }
+    __syncwarp();  // every lane's outputs before the block is announced
+    if (lane == 0) st_release_cta(&S.prog[w], ++finished);
   }
 }
 

@@ -157,8 +157,9 @@ typedef struct csmv_bank_config {
   uint32_t prevalidate;        /* 1 = intra-warp pre-validation (batchedAtrInsert)             */
   uint32_t log_commits;        /* 1 = keep the per-ts commit log and per-txn outcomes         */
   uint32_t max_txn;            /* largest stream a run may carry (sizes the logs)             */
-  uint32_t spin_limit_log2;    /* bounded waits give up after 2^this polls (default 26)       */
+  uint32_t spin_limit_log2;    /* bounded waits give up after 2^this polls (default 24)       */
   int32_t device;
+  uint32_t flow_warps;         /* warps of the dataflow lane's execution CTA, 1..16 (0 = 8)    */
 } csmv_bank_config;
 
 void csmv_bank_config_default(csmv_bank_config* cfg);

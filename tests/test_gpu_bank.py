@@ -234,6 +234,10 @@ FLOW_CASES = {
                                 ro=0, kind=cg.KIND_TRANSFER_ALWAYS),
     "zipf-self-transfers": dict(n_acc=512, n=32 * 300, dist=cg.DIST_ZIPF, depth=4, up_reads=3,
                                 ro=10, self_every=5),
+    "zipf-1-warp": dict(n_acc=1024, n=32 * 400, dist=cg.DIST_ZIPF, depth=4, up_reads=4, ro=20,
+                        flow_warps=1),
+    "zipf-16-warps": dict(n_acc=1 << 15, n=1 << 16, dist=cg.DIST_ZIPF, depth=8, up_reads=4,
+                          ro=20, flow_warps=16),
 }
 
 
@@ -254,7 +258,8 @@ def test_flow_lane_equals_serial_lane(case):
     ds, keep = to_device(torch, s)
     res = []
     for lane in ("serial", "flow"):
-        with cg.Bank(n_accounts=n_acc, max_txn=n, version_depth=depth) as bank:
+        with cg.Bank(n_accounts=n_acc, max_txn=n, version_depth=depth,
+                     flow_warps=c.get("flow_warps", 0)) as bank:
             bank.load()
             st = bank.run_serial_device(ds) if lane == "serial" else bank.run_flow_device(ds)
             res.append((st, bank.log(n, st.final_ts), bank.versions(), bank.values()))
