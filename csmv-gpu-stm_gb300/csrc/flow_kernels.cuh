@@ -452,14 +452,12 @@ __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowPara
     }
     int32_t v0 = 0, v1 = 0;
     uint32_t acc = 0;  // extra reads of a transfer; every read past the first two of a scan
-    unsigned long long pend = 0, gpend = 0;  // reads waiting on the ring / on global memory
+    uint32_t pm = 0;   // a transfer's reads waiting on the ring
+    unsigned long long gpend = 0;  // reads waiting on global memory (a scan: all of them)
     auto take = [&](uint32_t k, uint32_t x) {
-      if (k == 0)
-        v0 = (int32_t)x;
-      else if (k == 1)
-        v1 = (int32_t)x;
-      else
-        acc += x;
+      v0 = k == 0 ? (int32_t)x : v0;
+      v1 = k == 1 ? (int32_t)x : v1;
+      acc += k >= 2 ? x : 0u;
     };
     const ModMagic mm(ro ? 1u : CSMV_OP_AMOD(op));
     uint32_t ridx[kFlowReadsInRegs], rtag[kFlowReadsInRegs];
@@ -487,32 +485,42 @@ __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowPara
           else
             gpend |= 1ull << k;
         } else {
-          pend |= 1ull << k;
+          pm |= 1u << k;
         }
       }
     } else {
       gpend = (1ull << nr) - 1ull;  // a scan: every read through flow_fetch (nr <= 63)
     }
+    // the lowest read still waiting on the ring: its index, ring word and tag (k = 32: none)
+    uint32_t ck = 32u, cidx = 0u, ctag = 0u;
+    auto advance = [&]() {
+      ck = pm ? (uint32_t)__ffs(pm) - 1u : 32u;
+      cidx = pick(ridx, ck);
+      ctag = pick(rtag, ck);
+    };
+    advance();
     bool done = false, hw = false;
     uint32_t o0 = 0, o1 = 0;
     for (unsigned long long it = 0;; ++it) {
       if (!done) {
-        while (pend) {
-          const uint32_t k = (uint32_t)__ffsll((long long)pend) - 1u;
-          const unsigned long long wv = ld_relaxed_cta_shared(&S.ring[pick(ridx, k)]);
-          if ((uint32_t)(wv >> 32) != pick(rtag, k)) break;
-          take(k, (uint32_t)wv);
-          pend &= pend - 1ull;
+        while (ck < 32u) {
+          const unsigned long long wv = ld_relaxed_cta_shared(&S.ring[cidx]);
+          if ((uint32_t)(wv >> 32) != ctag) break;
+          take(ck, (uint32_t)wv);
+          pm &= pm - 1u;
+          advance();
         }
-        for (unsigned long long m = gpend; m; m &= m - 1ull) {
-          const uint32_t k = (uint32_t)__ffsll((long long)m) - 1u;
-          uint32_t x;
-          if (flow_fetch(f, S, ro ? __ldg(&f.src[e0 + k]) : pick(sv, k), b, tag, x)) {
-            take(k, x);
-            gpend &= ~(1ull << k);
+        if (gpend) {
+          for (unsigned long long m = gpend; m; m &= m - 1ull) {
+            const uint32_t k = (uint32_t)__ffsll((long long)m) - 1u;
+            uint32_t x;
+            if (flow_fetch(f, S, ro ? __ldg(&f.src[e0 + k]) : pick(sv, k), b, tag, x)) {
+              take(k, x);
+              gpend &= ~(1ull << k);
+            }
           }
         }
-        if ((pend | gpend) == 0ull) {
+        if (ck == 32u && gpend == 0ull) {
           done = true;
           if (!ro) {
             const uint32_t amt = 1u + mm.mod(CSMV_OP_AMT0(op) - 1u + acc);

@@ -109,7 +109,8 @@ struct AccountDraw {
 
 csmv_status check_workload(const csmv_bank_workload* w) {
   if (!w || w->n_txn == 0 || w->n_txn % 32 || w->n_accounts < 2 || w->up_reads < 2 ||
-      w->up_reads > 32 || w->ro_reads < 1 || w->ro_reads > 32 || w->amt_lo < 1 ||
+      w->up_reads > 32 || w->up_reads > w->n_accounts /* a transfer's accounts are distinct */ ||
+      w->ro_reads < 1 || w->ro_reads > 32 || w->amt_lo < 1 ||
       w->amt_hi < w->amt_lo || w->amt_hi > 4095 || w->pr_read_pct > 100 ||
       (w->kind != CSMV_KIND_TRANSFER && w->kind != CSMV_KIND_TRANSFER_ALWAYS) || w->dist > 2 ||
       (w->dist == CSMV_DIST_HOTSPOT && !(w->hot_frac > 0.0 && w->hot_frac <= 1.0))) {

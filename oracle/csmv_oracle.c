@@ -140,8 +140,8 @@ int orc_bank_stream_size(const orc_bank_workload* w, uint64_t* n_addr) {
 
 int orc_bank_generate(const orc_bank_workload* w, uint32_t* op, uint32_t* off, uint32_t* addr) {
   if (!w || w->n_txn % 32 || w->n_accounts == 0 || w->up_reads < 2 || w->up_reads > 32 ||
-      w->ro_reads < 1 || w->ro_reads > 32 || w->amt_lo < 1 || w->amt_hi < w->amt_lo ||
-      w->amt_hi > 4095)
+      w->up_reads > w->n_accounts || w->ro_reads < 1 || w->ro_reads > 32 || w->amt_lo < 1 ||
+      w->amt_hi < w->amt_lo || w->amt_hi > 4095)
     return 1;
   gen_t g;
   g.w = w;

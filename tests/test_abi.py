@@ -66,7 +66,8 @@ def test_memcd_config_validation_is_a_status():
 
 def test_workload_validation_is_a_status():
     for bad in (dict(n_txn=33), dict(up_reads=1), dict(amt_lo=0), dict(amt_hi=5000),
-                dict(pr_read_pct=101), dict(kind=0), dict(dist=7)):
+                dict(pr_read_pct=101), dict(kind=0), dict(dist=7),
+                dict(n_accounts=3, up_reads=4)):  # four distinct accounts out of three
         kw = dict(n_accounts=100, n_txn=64)
         kw.update(bad)
         with pytest.raises(cg.CsmvError) as e:
