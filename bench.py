@@ -13,7 +13,8 @@ Two arms run the same batches on separate banks:
            protocol, client warps + per-CTA commit server on every SM
   learned  the learned conflict scheduler in front of the same engine (csmv_sched_run): a probe
            slice in stream order trains the conflict predictor, the predictor routes likely-
-           conflicting transfers to the serial lane and spaces the rest
+           conflicting transfers to the dataflow lane (run after the rest, each transfer as
+           soon as the transfers it depends on have run) and spaces the rest
 value = the learned arm's committed tx/s (GPU time of the whole step, inputs resident in HBM);
 e2e = the same through host buffers (pinned -> device copies and the statistics read inside
 the timed region). Both arms' throughput and abort rate are in "plain" / "learned".
@@ -27,7 +28,7 @@ peak, batches of 1 K-64 K requests, 95 % GET rounds: achieved req/s and p50/p99 
 
 --impl reference runs the reference arm: the path's CPU execution (the oracle port, striped
 locks on every host core) on the same batches. --case NAME runs one small invocation of one
-kernel for profiling (engine, serial, mlp, memcd, sched). Multi-GPU: replicas only (no
+kernel for profiling (engine, serial, flow, mlp, memcd, sched). Multi-GPU: replicas only (no
 collective on the path); each rank runs its own instance on its own GPU, value sums the ranks'
 transactions over the slowest rank's time.
 """
@@ -54,7 +55,8 @@ WORKLOAD = dict(seed=2026, pr_read_pct=20, ro_reads=32, up_reads=4, amt_lo=1, am
                 zipf_theta=0.99)
 B_UPDATE = 16 * 4 + 12 * 2   # algorithmic bytes of a transfer: 4 versioned reads, 2 writes
 B_RO = 16 * 32               # a 32-account read-only scan
-SCHED = dict(serial_lane=1, defer_threshold=0.0, probe_every=3, probe_rounds_pct=2)
+SCHED = dict(serial_lane=2, defer_threshold=0.0, probe_every=3, probe_rounds_pct=2)
+FLOW_WARPS = 12  # warps of the dataflow lane's execution CTA
 
 
 def parse():
@@ -68,7 +70,8 @@ def parse():
     ap.add_argument("--client-warps", type=int, default=int(os.environ.get("CSMV_CLIENT_WARPS", 2)))
     ap.add_argument("--ctas", type=int, default=int(os.environ.get("CSMV_CTAS", 152)))
     ap.add_argument("--depth", type=int, default=int(os.environ.get("CSMV_DEPTH", 8)))
-    ap.add_argument("--case", default=None, choices=["engine", "serial", "mlp", "memcd", "sched"])
+    ap.add_argument("--case", default=None,
+                    choices=["engine", "serial", "flow", "mlp", "memcd", "sched"])
     ap.add_argument("--no-extras", action="store_true", help="skip hotspot/uniform/memcd sections")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (use the flags)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -190,13 +193,14 @@ def launches_learned(rep) -> int:
     if rep.n_planned:
         n += 6  # keys, buckets, scan, scatter, read-only list, emit
         n += 1 if rep.planned.commits else 0  # concurrent engine run
-        n += 1 if rep.n_serial else 0         # serial lane
+        if rep.n_serial:                      # dataflow lane: analysis, sort, run, commit
+            n += 17 + 5 * (((N_ACCOUNTS - 1).bit_length() + 7) // 8)
     return n
 
 
 def new_bank(cg, args, local, max_txn, **over):
     kw = dict(n_accounts=N_ACCOUNTS, version_depth=args.depth, client_warps=args.client_warps,
-              ctas=args.ctas, max_txn=max_txn, log_commits=0, device=local)
+              ctas=args.ctas, max_txn=max_txn, log_commits=0, device=local, flow_warps=FLOW_WARPS)
     kw.update(over)
     bank = cg.Bank(**kw)
     bank.load()
@@ -504,7 +508,7 @@ def run_case(args, local):
 
     import csmv_gb300 as cg
     torch.cuda.set_device(local)
-    if args.case in ("engine", "serial", "sched"):
+    if args.case in ("engine", "serial", "flow", "sched"):
         dist = "uniform" if args.case == "engine" else "zipf"
         n = (1 << 15) if args.case == "serial" else (1 << 18)
         s, bs = generate_batches(dist, n, 2, pinned=False)
@@ -518,7 +522,8 @@ def run_case(args, local):
             sched.close()
             out = {"case": "sched", "commits": r.commits}
         else:
-            run = bank.run_device if args.case == "engine" else bank.run_serial_device
+            run = {"engine": bank.run_device, "serial": bank.run_serial_device,
+                   "flow": bank.run_flow_device}[args.case]
             for d in dev:  # a warm-up launch, then the profiled one
                 st = run(d.stream(cg, addr, s.addr.shape[0]))
             out = {"case": args.case, "commits": st.commits, "kernel_ms": st.kernel_ms}
@@ -597,15 +602,16 @@ def main():
     if rank != 0:
         return
     pk, pk_kind = peaks()
-    # roofline of the dominant kernel of the learned step (the serial lane): algorithmic bytes
-    # of the transfers it committed over its device time
+    # roofline of the dominant part of the learned step, the dataflow lane (its execution
+    # kernel holds nearly all of the lane's device time): algorithmic bytes of the transfers it
+    # committed over the lane's device time
     s_ms = learned["serial_ms"]
     achieved = learned["serial_txn"] * B_UPDATE / (s_ms * 1e-3) / 1e9 if s_ms > 0 else 0.0
     traffic = None
     tr = ROOT / "profiles" / "traffic.json"
     if tr.exists():
         try:
-            traffic = json.loads(tr.read_text()).get("bank_serial_kernel_bytes_per_launch")
+            traffic = json.loads(tr.read_text()).get("flow_exec_kernel_bytes_per_launch")
         except Exception:
             traffic = None
     plain_gbs = (plain["upd"] * B_UPDATE + plain["ro"] * B_RO) / (plain["ms"] * 1e-3) / 1e9
@@ -621,7 +627,8 @@ def main():
                    "parallelism": f"replicas x{world}"},
         "abort_rate": l_abort,
         "learned": {"tx_s": value, "abort_rate": l_abort,
-                    "serial_lane_txn_per_step": learned["serial_txn"] // timed,
+                    "dataflow_lane_txn_per_step": learned["serial_txn"] // timed,
+                    "dataflow_lane_ms_per_step": learned["serial_ms"] / timed,
                     "plan_ms_per_step": learned["plan_ms"] / timed,
                     "train_ms_per_step": learned["train_ms"] / timed},
         "plain": {"tx_s": plain["commits"] * world / t_plain,
@@ -629,7 +636,7 @@ def main():
                   "roofline_frac_of_measured_hbm": plain_gbs / pk["hbm_gbs"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
-                     "kernel": "bank_serial_kernel", "peak_source": pk_kind,
+                     "kernel": "flow_exec_kernel (dataflow lane)", "peak_source": pk_kind,
                      "bytes_per_txn": B_UPDATE},
         "e2e": {"value": e2e, "unit": "committed tx/s", "h2d_bytes_per_step": h2d,
                 # per engine run: statistics (80 B) + commit-order words (768 B); up to three runs
