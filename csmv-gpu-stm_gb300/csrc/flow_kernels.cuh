@@ -385,11 +385,12 @@ __device__ __forceinline__ T pick(const T (&a)[kFlowReadsInRegs], uint32_t k) {
 
 // A transfer's static inputs (producers, committed values, written accounts, divisor) are read
 // at the start of its block, and so are the outputs of producers at least G blocks older (they
-// have finished). What is left are producers in the ring, with their ring word and tag worked
-// out once: a lane polls them in read order and stops at the first that has not arrived, so a
-// pass costs a blocked lane one shared-memory load. A finished transfer publishes to the ring at
-// once and leaves its global outputs, flags and counts for the end of the block: the passes that
-// carry the dependency chain stay short.
+// have finished); the amount is worked out as soon as its extra reads are in. What is left are
+// producers in the ring, with their ring word and tag worked out once: a pass loads all of them
+// at once (independent shared-memory loads) and takes them when all have arrived - a ring word
+// keeps its producer's value until the consumer's block is done. A finished transfer publishes
+// to the ring at once and leaves its global outputs, flags and counts for the end of the block:
+// the passes that carry the dependency chain stay short.
 __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowParams f) {
   extern __shared__ __align__(16) unsigned char flow_smem_raw[];
   FlowSmem& S = *reinterpret_cast<FlowSmem*>(flow_smem_raw);
@@ -397,19 +398,19 @@ __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowPara
   const uint32_t nb = f.n_txn / 32u;
   const unsigned long long tag = (unsigned long long)f.epoch << 32;
   uint32_t* err = &f.b.gs->error;
-  const unsigned long long limit = 1ull << f.b.spin_log2;
+  const uint32_t limit = 1u << f.b.spin_log2;  // spin_log2 <= 30
   for (uint32_t k = threadIdx.x; k < 2u * kFlowRing; k += blockDim.x) S.ring[k] = 0ull;
   if (threadIdx.x < 32) S.prog[threadIdx.x] = 0u;
   if (threadIdx.x == 0) S.failed = ld_relaxed_gpu(err);
   __syncthreads();
   if (S.failed) return;
   // bounded poll bookkeeping: false when the warp must leave (budget spent or an error raised)
-  auto keep_polling = [&](unsigned long long it) {
+  auto keep_polling = [&](uint32_t it) {
     if (it >= limit) {
       if (lane == 0) raise_error(err, ERR_WAIT_FLOW);
       return false;
     }
-    if ((it & 1023ull) == 1023ull) {
+    if ((it & 1023u) == 1023u) {
       uint32_t e = 0;
       if (lane == 0) e = ld_relaxed_gpu(err);
       if (__shfl_sync(0xFFFFFFFFu, e, 0)) return false;
@@ -442,7 +443,7 @@ __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowPara
     }
     if (b >= kFlowGate) {  // every block <= b - G finished
       const uint32_t q = b - kFlowGate;
-      for (unsigned long long it = 0;; ++it) {
+      for (uint32_t it = 0;; ++it) {
         bool ok = true;
         if (lane < nw) ok = ld_acquire_cta(&S.prog[lane]) >= (q >= lane ? (q - lane) / nw + 1u : 0u);
         if (__all_sync(0xFFFFFFFFu, ok)) break;
@@ -491,24 +492,37 @@ __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowPara
     } else {
       gpend = (1ull << nr) - 1ull;  // a scan: every read through flow_fetch (nr <= 63)
     }
-    // the lowest read still waiting on the ring: its index, ring word and tag (k = 32: none)
-    uint32_t ck = 32u, cidx = 0u, ctag = 0u;
-    auto advance = [&]() {
-      ck = pm ? (uint32_t)__ffs(pm) - 1u : 32u;
-      cidx = pick(ridx, ck);
-      ctag = pick(rtag, ck);
+    // the amount, as soon as every extra read is in (usually here, before any wait)
+    uint32_t amt = 0;
+    bool amt_known = false;
+    auto try_amount = [&]() {
+      if (!ro && !amt_known && ((pm | (uint32_t)gpend) & ~3u) == 0u) {
+        amt = 1u + mm.mod(CSMV_OP_AMT0(op) - 1u + acc);
+        amt_known = true;
+      }
     };
-    advance();
+    try_amount();
     bool done = false, hw = false;
     uint32_t o0 = 0, o1 = 0;
-    for (unsigned long long it = 0;; ++it) {
+    for (uint32_t it = 0;; ++it) {
       if (!done) {
-        while (ck < 32u) {
-          const unsigned long long wv = ld_relaxed_cta_shared(&S.ring[cidx]);
-          if ((uint32_t)(wv >> 32) != ctag) break;
-          take(ck, (uint32_t)wv);
-          pm &= pm - 1u;
-          advance();
+        if (pm) {  // every ring read polled at once; all are taken when all have arrived
+          uint32_t rdy = 0, xv[kFlowReadsInRegs];
+#pragma unroll
+          for (uint32_t k = 0; k < kFlowReadsInRegs; k++) {
+            xv[k] = 0u;
+            if ((pm >> k) & 1u) {
+              const unsigned long long wv = ld_relaxed_cta_shared(&S.ring[ridx[k]]);
+              xv[k] = (uint32_t)wv;
+              rdy |= (uint32_t)((uint32_t)(wv >> 32) == rtag[k]) << k;
+            }
+          }
+          if (rdy == pm) {
+#pragma unroll
+            for (uint32_t k = 0; k < kFlowReadsInRegs; k++)
+              if ((pm >> k) & 1u) take(k, xv[k]);
+            pm = 0u;
+          }
         }
         if (gpend) {
           for (unsigned long long m = gpend; m; m &= m - 1ull) {
@@ -520,10 +534,10 @@ __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowPara
             }
           }
         }
-        if (ck == 32u && gpend == 0ull) {
+        if (pm == 0u && gpend == 0ull) {
           done = true;
           if (!ro) {
-            const uint32_t amt = 1u + mm.mod(CSMV_OP_AMT0(op) - 1u + acc);
+            try_amount();
             hw = CSMV_OP_KIND(op) == CSMV_KIND_TRANSFER_ALWAYS || v0 >= (int32_t)amt;
             o0 = hw ? (uint32_t)v0 - amt : (uint32_t)v0;
             o1 = hw ? (uint32_t)v1 + amt : (uint32_t)v1;
@@ -532,6 +546,8 @@ __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowPara
             if (a0 != a1) st_relaxed_cta_shared(&S.ring[r0], rt | o0);
             st_relaxed_cta_shared(&S.ring[r0 + 1u], rt | o1);
           }
+        } else {
+          try_amount();
         }
       }
       if (__all_sync(0xFFFFFFFFu, done)) break;
