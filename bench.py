@@ -56,7 +56,7 @@ WORKLOAD = dict(seed=2026, pr_read_pct=20, ro_reads=32, up_reads=4, amt_lo=1, am
 B_UPDATE = 16 * 4 + 12 * 2   # algorithmic bytes of a transfer: 4 versioned reads, 2 writes
 B_RO = 16 * 32               # a 32-account read-only scan
 SCHED = dict(serial_lane=2, defer_threshold=0.0, probe_every=3, probe_rounds_pct=2)
-FLOW_WARPS = 12  # warps of the dataflow lane's execution CTA
+FLOW_WARPS = 8  # warps of the dataflow lane's execution CTA
 
 
 def parse():

@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowPara
       if (__shfl_sync(0xFFFFFFFFu, e, 0)) return false;
     }
     return true;
-  };
+  };  // (called with it = 255, 511, ... by the execution loop: limit >= 1024)
   uint32_t finished = 0;  // this warp's blocks
   uint32_t op_n = 0, e0_n = 0;  // the next block's op and element offset, loaded ahead
   if (w < nb) {
@@ -551,8 +551,8 @@ __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowPara
         }
       }
       if (__all_sync(0xFFFFFFFFu, done)) break;
-      __syncwarp();  // this pass's outputs before the next pass's polls
-      if (!keep_polling(it)) return;
+      // (no warp barrier between passes: a ring word read before its store is only "not yet")
+      if ((it & 255u) == 255u && !keep_polling(it)) return;
     }
     // off the chain: global outputs, flags, counts, scan results
     if (ro) {
