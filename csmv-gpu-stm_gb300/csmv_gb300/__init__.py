@@ -9,6 +9,7 @@ with statistics named after the reference's Statistics struct (bank/csmv_sh/API.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass
 from pathlib import Path
 
@@ -19,7 +20,7 @@ LIB_PATH = PKG_ROOT / "lib" / "libcsmv.so"
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory",
           4: "bounded device wait timed out", 5: "capacity exceeded", 6: "no sm_103 device",
-          7: "call out of order"}
+          7: "call out of order", 8: "file error"}
 
 KIND_READONLY, KIND_TRANSFER, KIND_TRANSFER_ALWAYS = 0, 1, 2
 DIST_UNIFORM, DIST_ZIPF, DIST_HOTSPOT = 0, 1, 2
@@ -164,6 +165,12 @@ def lib() -> C.CDLL:
         "csmv_bank_config_default": (None, [C.POINTER(BankConfig)]),
         "csmv_bank_stream_size": (I32, [C.POINTER(BankWorkload), C.POINTER(C.c_uint64)]),
         "csmv_bank_generate": (I32, [C.POINTER(BankWorkload), P, P, P]),
+        "csmv_stream_save": (I32, [C.c_char_p, C.POINTER(BankStream)]),
+        "csmv_stream_info": (I32, [C.c_char_p, C.POINTER(U32), C.POINTER(C.c_uint64)]),
+        "csmv_stream_load": (I32, [C.c_char_p, P, P, P, U32, C.c_uint64]),
+        "csmv_log_save": (I32, [C.c_char_p, U32, P, U32, P, P, U32]),
+        "csmv_log_info": (I32, [C.c_char_p, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
+        "csmv_log_load": (I32, [C.c_char_p, P, U32, P, P, U32]),
         "csmv_bank_create": (I32, [C.POINTER(BankConfig), C.POINTER(P)]),
         "csmv_bank_load": (I32, [P, P]),
         "csmv_bank_run": (I32, [P, C.POINTER(BankStream), C.POINTER(Stats)]),
@@ -302,6 +309,49 @@ def generate(w: BankWorkload, pinned: bool = False) -> Stream:
     s = Stream(op, off, addr)
     s._holders = holders  # keep pinned memory alive
     return s
+
+
+def save_stream(path, s: Stream) -> None:
+    """Write a host stream to a stream file (csmv_stream_save)."""
+    op, off, addr = (np.ascontiguousarray(a, np.uint32) for a in (s.op, s.off, s.addr))
+    bs = BankStream(int(op.shape[0]), _ptr(op), _ptr(off), _ptr(addr), int(addr.shape[0]))
+    _check(lib().csmv_stream_save(os.fsencode(path), C.byref(bs)), "csmv_stream_save")
+
+
+def load_stream(path) -> Stream:
+    """Read a stream file (csmv_stream_info + csmv_stream_load)."""
+    n_txn, n_addr = C.c_uint32(), C.c_uint64()
+    _check(lib().csmv_stream_info(os.fsencode(path), C.byref(n_txn), C.byref(n_addr)),
+           "csmv_stream_info")
+    op = np.empty(n_txn.value, np.uint32)
+    off = np.empty(n_txn.value, np.uint32)
+    addr = np.empty(n_addr.value, np.uint32)
+    _check(lib().csmv_stream_load(os.fsencode(path), _ptr(op), _ptr(off), _ptr(addr),
+                                  n_txn.value, n_addr.value), "csmv_stream_load")
+    return Stream(op, off, addr)
+
+
+def save_log(path, base_ts: int, log_txn, outcome, result) -> None:
+    """Write a run's commit log (csmv_log_save)."""
+    lt = np.ascontiguousarray(log_txn, np.uint32)
+    oc = np.ascontiguousarray(outcome, np.uint32)
+    rs = np.ascontiguousarray(result, np.int32)
+    assert oc.shape == rs.shape
+    _check(lib().csmv_log_save(os.fsencode(path), base_ts, _ptr(lt), int(lt.shape[0]), _ptr(oc),
+                               _ptr(rs), int(oc.shape[0])), "csmv_log_save")
+
+
+def load_log(path):
+    """Read a commit-log file: (base_ts, log_txn, outcome, result)."""
+    n_txn, n_log, base = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    _check(lib().csmv_log_info(os.fsencode(path), C.byref(n_txn), C.byref(n_log), C.byref(base)),
+           "csmv_log_info")
+    lt = np.empty(n_log.value, np.uint32)
+    oc = np.empty(n_txn.value, np.uint32)
+    rs = np.empty(n_txn.value, np.int32)
+    _check(lib().csmv_log_load(os.fsencode(path), _ptr(lt), n_log.value, _ptr(oc), _ptr(rs),
+                               n_txn.value), "csmv_log_load")
+    return base.value, lt, oc, rs
 
 
 # ---------------------------------------------------------------------------------------------

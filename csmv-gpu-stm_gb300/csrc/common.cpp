@@ -50,6 +50,7 @@ extern "C" const char* csmv_status_str(csmv_status s) {
     case CSMV_ERR_CAPACITY: return "capacity exceeded";
     case CSMV_ERR_NO_DEVICE: return "no sm_103 device";
     case CSMV_ERR_STATE: return "call out of order";
+    case CSMV_ERR_IO: return "file error";
   }
   return "unknown status";
 }

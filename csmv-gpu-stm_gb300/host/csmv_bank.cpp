@@ -14,7 +14,10 @@
 // transfer that reads 2k accounts and writes two (the reference writes all 2k).
 // Engine options come from the environment: CSMV_VALIDATE (stamp|ring|ring_lane),
 // CSMV_BATCH (lane|warp|cta), CSMV_WRITEBACK (client|server), CSMV_PREVALIDATE (0|1),
-// CSMV_DEPTH (2|4|8|16), CSMV_SEED.
+// CSMV_DEPTH (2|4|8|16), CSMV_SEED. Traces: CSMV_TRACE_IN=<file> runs the stream of a stream
+// file (csmv_stream_save) instead of generating one; CSMV_TRACE_OUT=<prefix> writes the run's
+// stream to <prefix>.stream and its commit log to <prefix>.log (csmv_log_save), so the same run
+// can be replayed and checked on the CPU.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -111,6 +114,27 @@ int main(int argc, char** argv) {
   }
   std::vector<uint32_t> op(n_txn), off(n_txn), addr(n_addr);
   csmv_bank_generate(&w, op.data(), off.data(), addr.data());
+  uint32_t run_txn = n_txn;
+  if (const char* in = std::getenv("CSMV_TRACE_IN")) {
+    uint32_t t = 0;
+    uint64_t a = 0;
+    if ((st = csmv_stream_info(in, &t, &a)) != CSMV_OK) {
+      std::fprintf(stderr, "CSMV_TRACE_IN: %s\n", csmv_last_error());
+      return 1;
+    }
+    op.assign(t, 0);
+    off.assign(t, 0);
+    addr.assign(a, 0);
+    if ((st = csmv_stream_load(in, op.data(), off.data(), addr.data(), t, a)) != CSMV_OK) {
+      std::fprintf(stderr, "CSMV_TRACE_IN: %s\n", csmv_last_error());
+      return 1;
+    }
+    run_txn = t;
+    n_addr = a;
+    cfg.max_txn = t > 0 ? t : 32;
+  }
+  const char* trace_out = std::getenv("CSMV_TRACE_OUT");
+  if (trace_out) cfg.log_commits = 1;
 
   csmv_bank_t* h = nullptr;
   if ((st = csmv_bank_create(&cfg, &h)) != CSMV_OK) {
@@ -121,13 +145,34 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "csmv_bank_load: %s\n", csmv_last_error());
     return 1;
   }
-  csmv_bank_stream s{n_txn, op.data(), off.data(), addr.data(), n_addr};
+  csmv_bank_stream s{run_txn, op.data(), off.data(), addr.data(), n_addr};
+  if (trace_out) {
+    const std::string path = std::string(trace_out) + ".stream";
+    if ((st = csmv_stream_save(path.c_str(), &s)) != CSMV_OK) {
+      std::fprintf(stderr, "CSMV_TRACE_OUT: %s\n", csmv_last_error());
+      csmv_bank_destroy(h);
+      return 1;
+    }
+  }
   csmv_stats stats;
   st = csmv_bank_run(h, &s, &stats);
   if (st != CSMV_OK) {
     std::fprintf(stderr, "csmv_bank_run: %s: %s\n", csmv_status_str(st), csmv_last_error());
     csmv_bank_destroy(h);
     return 1;
+  }
+  if (trace_out) {  // timestamps 1..final_ts of this (first) run, holes included
+    std::vector<uint32_t> log_txn(stats.final_ts > 0 ? stats.final_ts : 1), outcome(run_txn);
+    std::vector<int32_t> result(run_txn);
+    const std::string path = std::string(trace_out) + ".log";
+    if ((st = csmv_bank_read_log(h, log_txn.data(), stats.final_ts, outcome.data(), result.data(),
+                                 run_txn)) != CSMV_OK ||
+        (st = csmv_log_save(path.c_str(), 0, log_txn.data(), stats.final_ts, outcome.data(),
+                            result.data(), run_txn)) != CSMV_OK) {
+      std::fprintf(stderr, "CSMV_TRACE_OUT: %s\n", csmv_last_error());
+      csmv_bank_destroy(h);
+      return 1;
+    }
   }
   // TXEnd's invariant (bank/csmv_sh/API.cu:339-350)
   std::vector<int32_t> vals(n_accounts);

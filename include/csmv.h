@@ -33,7 +33,9 @@ typedef enum csmv_status {
   CSMV_ERR_TIMEOUT = 4,      /* a bounded device wait ran out; the kernel returned early     */
   CSMV_ERR_CAPACITY = 5,     /* commit log / result buffers too small for the run           */
   CSMV_ERR_NO_DEVICE = 6,    /* no CUDA device, or the device is not sm_103                  */
-  CSMV_ERR_STATE = 7         /* call order violated (e.g. run before load)                  */
+  CSMV_ERR_STATE = 7,        /* call order violated (e.g. run before load)                  */
+  CSMV_ERR_IO = 8            /* a file could not be opened, read or written, or is not a valid
+                                stream / commit-log file (magic, version, size, checksum)     */
 } csmv_status;
 
 /* ------------------------------------------------------------------------------------------
@@ -223,6 +225,27 @@ csmv_status csmv_bank_run_serial_device(csmv_bank_t* h, const csmv_bank_stream* 
  * call. */
 csmv_status csmv_bank_run_flow_device(csmv_bank_t* h, const csmv_bank_stream* dev_stream,
                                       csmv_stats* out);
+
+/* ------------------------------------------------------------------------------------------
+ * On-disk streams and commit logs, so CPU and GPU runs replay identical inputs and a run's
+ * commit order can be kept (the reference stores raw arrays without a header,
+ * memcachedGPU/keyGenAndCacheStore.cpp:151-182). Little-endian files with a header (magic,
+ * version, sizes) and an FNV-1a checksum of the payload; a mismatch returns CSMV_ERR_IO.
+ * All buffers are host memory.
+ * ---------------------------------------------------------------------------------------- */
+csmv_status csmv_stream_save(const char* path, const csmv_bank_stream* host_stream);
+csmv_status csmv_stream_info(const char* path, uint32_t* n_txn, uint64_t* n_addr);
+/* CSMV_ERR_CAPACITY when the file holds more than the caps. */
+csmv_status csmv_stream_load(const char* path, uint32_t* host_op, uint32_t* host_off,
+                             uint32_t* host_addr, uint32_t n_txn_cap, uint64_t n_addr_cap);
+/* A run's commit log as csmv_bank_read_log returns it: log_txn[k] = transaction of timestamp
+ * base_ts + k + 1 (0xFFFFFFFF = hole), outcome and result per transaction. */
+csmv_status csmv_log_save(const char* path, uint32_t base_ts, const uint32_t* host_log_txn,
+                          uint32_t n_log, const uint32_t* host_outcome,
+                          const int32_t* host_result, uint32_t n_txn);
+csmv_status csmv_log_info(const char* path, uint32_t* n_txn, uint32_t* n_log, uint32_t* base_ts);
+csmv_status csmv_log_load(const char* path, uint32_t* host_log_txn, uint32_t n_log_cap,
+                          uint32_t* host_outcome, int32_t* host_result, uint32_t n_txn_cap);
 
 /* Replaces TXEnd (bank/csmv_sh/API.cu:335-359): latest value of every account. */
 csmv_status csmv_bank_read_values(csmv_bank_t* h, int32_t* host_values);

@@ -173,6 +173,46 @@ def test_driver_reference_command_line():
     assert float(fields[1]) > 0 and 0.0 <= float(fields[0]) < 100.0
 
 
+def test_driver_trace_files_replay_exactly(tmp_path):
+    """CSMV_TRACE_OUT writes the driver's stream and commit log; the files replay exactly in
+    the oracle, and CSMV_TRACE_IN runs the same stream again from its file."""
+    from csmv_gb300 import build as b
+
+    prefix = tmp_path / "run"
+    env = {"CSMV_TX_PER_THREAD": "32", "PATH": "/usr/bin:/bin", "CSMV_TRACE_OUT": str(prefix)}
+    args = [str(b.BIN / "csmv_bank"), "2048", "128", "4", "128", "10", "8", "2", "0"]
+    out = subprocess.run(args, capture_output=True, text=True, timeout=300, env=env)
+    assert out.returncode == 0, out.stderr
+    s = cg.load_stream(f"{prefix}.stream")
+    base, log_txn, outcome, result = cg.load_log(f"{prefix}.log")
+    assert base == 0 and s.n_txn == 128 * 4 * 32 and outcome.shape[0] == s.n_txn
+    err = orc.check(s.op, s.off, s.addr, 2048, np.full(2048, 100, np.int32), 4, log_txn.shape[0],
+                    log_txn, outcome, result)
+    assert err is None, err
+    env2 = {"PATH": "/usr/bin:/bin", "CSMV_TRACE_IN": f"{prefix}.stream"}
+    out2 = subprocess.run(args, capture_output=True, text=True, timeout=300, env=env2)
+    assert out2.returncode == 0, out2.stderr
+    assert "Consistency fail" not in out2.stdout
+
+
+def test_bank_run_from_a_stream_file_and_log_file(tmp_path):
+    """A stream saved and loaded back runs on the GPU; its commit log, saved and loaded back,
+    replays exactly."""
+    w = c1_workload(n_txn=32 * 512, n_accounts=1024, dist=cg.DIST_ZIPF, up_reads=4, seed=31)
+    cg.save_stream(tmp_path / "s.stream", cg.generate(w))
+    s = cg.load_stream(tmp_path / "s.stream")
+    with cg.Bank(n_accounts=1024, max_txn=s.n_txn) as bank:
+        bank.load()
+        st = bank.run(s)
+        lt, oc, rs = bank.log(s.n_txn, st.final_ts)
+        slots = bank.versions()
+    cg.save_log(tmp_path / "s.log", 0, lt, oc, rs)
+    base, lt2, oc2, rs2 = cg.load_log(tmp_path / "s.log")
+    err = orc.check(s.op, s.off, s.addr, 1024, np.full(1024, 1000, np.int32), 4, st.final_ts,
+                    lt2, oc2, rs2, slots)
+    assert err is None, err
+
+
 @pytest.mark.parametrize("deferred_warps", [1, 7, 64])
 def test_deferred_queue_and_per_transaction_aborts_exact(deferred_warps):
     """A stream whose hot-account transfers sit in a deferred queue served by a few warps runs
