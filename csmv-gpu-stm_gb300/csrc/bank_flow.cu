@@ -68,7 +68,7 @@ InstallKernel pick_install(uint32_t depth) {
   }
 }
 
-// (Re)allocates *p for n elements of `bytes` each when the capacity is short.
+// Replaces *p by a fresh device array of n elements of T.
 template <class T>
 csmv_status grow(T** p, size_t n) {
   cudaFree(*p);
