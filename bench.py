@@ -364,7 +364,9 @@ def serve_section(cg, local, loads=(0.1, 0.25, 0.5, 0.75, 1.0), per_load_s=1.5):
     """Serving loop under open-loop Poisson arrivals: 2^20 sets x 8 ways, batches of U[1K, 64K]
     requests (multiples of 32), 95 % GET rounds, Zipf(0.99) keys over 4 M. The peak is the
     closed-loop throughput (submit as fast as admission allows); each offered load is a fraction
-    of it. Latency of a batch = completion seen by the host - its scheduled arrival."""
+    of it. Latency of a batch = completion seen by the host - its scheduled arrival. The same
+    arrivals then go through the plain form - one synchronous batch call at a time - for the
+    p50/p99 at equal offered load ("plain_*" in each row)."""
     rng = np.random.default_rng(7)
     pool_n = 1 << 21
     pool = cg.memcd_generate(cg.memcd_workload(1 << 22, pool_n, seed=77, get_pct=95))
@@ -409,7 +411,7 @@ def serve_section(cg, local, loads=(0.1, 0.25, 0.5, 0.75, 1.0), per_load_s=1.5):
         progress(f"serving: closed-loop peak {peak:.3g} req/s")
         out["peak_req_s"] = peak
         mean_n = (1024 + 65536) / 2
-        rows = []
+        rows, replay = [], []
         for load in loads:
             rate = load * peak / mean_n  # batches per second
             n_b = max(20, int(rate * per_load_s))
@@ -441,10 +443,35 @@ def serve_section(cg, local, loads=(0.1, 0.25, 0.5, 0.75, 1.0), per_load_s=1.5):
             rows.append({"offered_frac": load, "offered_req_s": load * peak,
                          "achieved_req_s": served / span, "p50_ms": float(np.percentile(lat, 50)),
                          "p99_ms": float(np.percentile(lat, 99)), "batches": n_b})
+            replay.append((arrivals, reqs))
             progress(f"serving: load {load}: p50 {rows[-1]['p50_ms']:.3f} ms")
         st = srv.stop()
         out["loads"] = rows
         out["abort_rate"] = st.aborts / max(1, st.aborts + st.commits)
+    # the plain form at equal offered load: the same arrivals, one batch call at a time
+    # (csmv_memcd_run with host buffers); a batch that arrives while another runs waits
+    with cg.Memcd(n_sets=1 << 20, client_warps=4, max_req=1 << 16, log_commits=0,
+                  device=local) as cache:
+        for _ in range(8):
+            cache.run(fill)
+        for row, (arrivals, reqs) in zip(rows, replay):
+            lat, served, t0 = [], 0, time.perf_counter()
+            t_end = t0 + per_load_s * 4 + 10
+            for arr, req in zip(arrivals, reqs):
+                if time.perf_counter() > t_end:
+                    row["plain_saturated"] = True
+                    break
+                while time.perf_counter() - t0 < arr:
+                    pass
+                cache.run(req)
+                lat.append(time.perf_counter() - t0 - arr)
+                served += req.n_req
+            lat = np.array(lat) * 1e3
+            row["plain_p50_ms"] = float(np.percentile(lat, 50))
+            row["plain_p99_ms"] = float(np.percentile(lat, 99))
+            row["plain_achieved_req_s"] = served / (time.perf_counter() - t0)
+            progress(f"serving: plain form at load {row['offered_frac']}: "
+                     f"p99 {row['plain_p99_ms']:.3f} ms")
     return out
 
 
