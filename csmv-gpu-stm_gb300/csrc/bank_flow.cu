@@ -23,7 +23,7 @@ struct FlowScratch {
   uint32_t *counts = nullptr, *wpos = nullptr, *key[2] = {nullptr, nullptr}, *val[2] = {nullptr, nullptr};
   unsigned long long *out = nullptr, *src = nullptr;
   uint2* tails = nullptr;
-  uint32_t* host_total = nullptr;  // pinned
+  uint32_t* host_total = nullptr;  // pinned: accesses, most reads of a transfer
 };
 
 void flow_scratch_free(FlowScratch* f) {
@@ -82,11 +82,13 @@ csmv_status ensure_txn(csmv_bank_t* h, uint32_t n) {
     FlowScratch* f = h->flow;
     f->items = h->cfg.n_accounts;
     csmv_status st;
-    if ((st = grow(&f->cnt, f->items)) != CSMV_OK || (st = grow(&f->n_tails, 1)) != CSMV_OK ||
+    if ((st = grow(&f->cnt, f->items)) != CSMV_OK || (st = grow(&f->n_tails, 2)) != CSMV_OK ||
         (st = grow(&f->agg, kScanMaxTiles + 1)) != CSMV_OK)
       return st;
-    CSMV_CUDA(cudaMallocHost((void**)&f->host_total, 4));
-    CSMV_CUDA(cudaFuncSetAttribute((const void*)flow_exec_kernel,
+    CSMV_CUDA(cudaMallocHost((void**)&f->host_total, 8));
+    CSMV_CUDA(cudaFuncSetAttribute((const void*)flow_exec_kernel<4>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FlowSmem)));
+    CSMV_CUDA(cudaFuncSetAttribute((const void*)flow_exec_kernel<8>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FlowSmem)));
     CSMV_CUDA(cudaMemsetAsync(f->cnt, 0, (size_t)f->items * 4, h->stream));
   }
@@ -150,12 +152,13 @@ csmv_status flow_launch(csmv_bank_t* h, const csmv_bank_stream* s) {
   p.cnt = f->cnt;
   p.tails = f->tails;
   p.n_tails = f->n_tails;
-  CSMV_CUDA(cudaMemsetAsync(f->n_tails, 0, 4, st));
+  CSMV_CUDA(cudaMemsetAsync(f->n_tails, 0, 8, st));  // tail count, most reads of a transfer
   flow_count_kernel<<<grid_of(n, 256), 256, 0, st>>>(p, 8u);
   CSMV_CUDA(cudaGetLastError());
   csmv_status rc = scan<false>(f->eoff, n, f->agg, st);
   if (rc != CSMV_OK) return rc;
   CSMV_CUDA(cudaMemcpyAsync(f->host_total, f->eoff + n, 4, cudaMemcpyDeviceToHost, st));
+  CSMV_CUDA(cudaMemcpyAsync(f->host_total + 1, f->n_tails + 1, 4, cudaMemcpyDeviceToHost, st));
   CSMV_CUDA(cudaStreamSynchronize(st));
   const uint32_t E = *f->host_total;
   if (E > kFlowMaxElem) {
@@ -195,7 +198,10 @@ csmv_status flow_launch(csmv_bank_t* h, const csmv_bank_stream* s) {
   }
   p.epoch = f->epoch;
   const uint32_t warps = h->cfg.flow_warps ? h->cfg.flow_warps : kFlowExecWarps;
-  flow_exec_kernel<<<1, 32 * warps, sizeof(FlowSmem), st>>>(p);
+  if (f->host_total[1] <= 4u)  // the most accounts a transfer of the stream reads
+    flow_exec_kernel<4><<<1, 32 * warps, sizeof(FlowSmem), st>>>(p);
+  else
+    flow_exec_kernel<8><<<1, 32 * warps, sizeof(FlowSmem), st>>>(p);
   CSMV_CUDA(cudaGetLastError());
   if ((rc = scan<false>(f->wflag, n, f->agg, st)) != CSMV_OK) return rc;
   flow_finalize_kernel<<<grid_of(n, 256), 256, 0, st>>>(p);

@@ -51,7 +51,7 @@ struct FlowParams {
   uint32_t* wflag;           // [n_txn + 1] has-write flags, scanned to writer ranks
   uint32_t* cnt;             // [n_items] actual writes per account in this run (zero between runs)
   uint2* tails;              // [2 n_txn] (account, producer code of its last write)
-  uint32_t* n_tails;
+  uint32_t* n_tails;         // [2]: tails written; the most accounts a transfer reads
   uint32_t epoch;
 };
 
@@ -250,6 +250,7 @@ __global__ void __launch_bounds__(256) flow_count_kernel(FlowParams f, uint32_t 
   f.eoff[i] = bad ? 0u : nr + nw;
   if (bad) raise_error(&f.b.gs->error, ERR_DATA);
   if (!bad && all_ro && lane_id() == 0) atomicAdd(&f.b.stats[ST_COMMIT_RO], 32ull);
+  if (!bad && !ro) atomicMax(&f.n_tails[1], nr);
 }
 
 __global__ void __launch_bounds__(256) flow_elements_kernel(FlowParams f, uint32_t* key, uint32_t* val) {
@@ -334,7 +335,8 @@ constexpr uint32_t kFlowRing = 8192;  // transactions whose outputs the ring hol
 constexpr uint32_t kFlowGate = 128;   // blocks a warp may run ahead of the oldest unfinished (G)
 static_assert(kFlowRing / 32 >= 2 * kFlowGate - 1, "ring reach");
 static_assert((kFlowRing & (kFlowRing - 1)) == 0, "ring size");
-constexpr uint32_t kFlowReadsInRegs = 8;  // a transfer's producers are held in registers
+// A transfer's producers are held in registers: NR of them, NR = 4 when no transfer of the
+// stream reads more than 4 accounts, else 8 (the most a transfer may read).
 
 struct FlowSmem {
   unsigned long long ring[2 * kFlowRing];
@@ -374,12 +376,12 @@ __device__ __forceinline__ bool flow_fetch(const FlowParams& f, FlowSmem& S, uns
   return (wv & 0xFFFFFFFF00000000ull) == tag;
 }
 
-// Entry k (< kFlowReadsInRegs) of a lane's register array, without local memory.
-template <class T>
-__device__ __forceinline__ T pick(const T (&a)[kFlowReadsInRegs], uint32_t k) {
+// Entry k (< NR) of a lane's register array, without local memory.
+template <uint32_t NR, class T>
+__device__ __forceinline__ T pick(const T (&a)[NR], uint32_t k) {
   T s = a[0];
 #pragma unroll
-  for (uint32_t q = 1; q < kFlowReadsInRegs; q++) s = k == q ? a[q] : s;
+  for (uint32_t q = 1; q < NR; q++) s = k == q ? a[q] : s;
   return s;
 }
 
@@ -391,6 +393,7 @@ __device__ __forceinline__ T pick(const T (&a)[kFlowReadsInRegs], uint32_t k) {
 // keeps its producer's value until the consumer's block is done. A finished transfer publishes
 // to the ring at once and leaves its global outputs, flags and counts for the end of the block:
 // the passes that carry the dependency chain stay short.
+template <uint32_t NR>
 __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowParams f) {
   extern __shared__ __align__(16) unsigned char flow_smem_raw[];
   FlowSmem& S = *reinterpret_cast<FlowSmem*>(flow_smem_raw);
@@ -432,12 +435,12 @@ __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowPara
     }
     const uint32_t nr = CSMV_OP_NREADS(op);
     const bool ro = CSMV_OP_KIND(op) == CSMV_KIND_READONLY;
-    unsigned long long sv[kFlowReadsInRegs];
+    unsigned long long sv[NR];
     uint32_t a0 = 0, a1 = 0;
     if (!ro) {
       const uint32_t off = f.b.off[i];
 #pragma unroll
-      for (uint32_t k = 0; k < kFlowReadsInRegs; k++) sv[k] = k < nr ? __ldg(&f.src[e0 + k]) : kFlowValue;
+      for (uint32_t k = 0; k < NR; k++) sv[k] = k < nr ? __ldg(&f.src[e0 + k]) : kFlowValue;
       a0 = f.b.addr[off];
       a1 = f.b.addr[off + 1];
     }
@@ -461,12 +464,12 @@ __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowPara
       acc += k >= 2 ? x : 0u;
     };
     const ModMagic mm(ro ? 1u : CSMV_OP_AMOD(op));
-    uint32_t ridx[kFlowReadsInRegs], rtag[kFlowReadsInRegs];
+    uint32_t ridx[NR], rtag[NR];
     if (!ro) {
       // committed values, and outputs of producers that finished (all loads issued together)
-      unsigned long long gv[kFlowReadsInRegs];
+      unsigned long long gv[NR];
 #pragma unroll
-      for (uint32_t k = 0; k < kFlowReadsInRegs; k++) {
+      for (uint32_t k = 0; k < NR; k++) {
         const unsigned long long s = sv[k];
         gv[k] = s;
         if (k < nr && !(s & kFlowValue) && b - ((uint32_t)s >> 6) >= kFlowGate)
@@ -475,7 +478,7 @@ __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowPara
         rtag[k] = ((uint32_t)s >> 1) + 1u;
       }
 #pragma unroll
-      for (uint32_t k = 0; k < kFlowReadsInRegs; k++) {
+      for (uint32_t k = 0; k < NR; k++) {
         if (k >= nr) continue;
         const unsigned long long s = sv[k];
         if (s & kFlowValue) {
@@ -507,9 +510,9 @@ __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowPara
     for (uint32_t it = 0;; ++it) {
       if (!done) {
         if (pm) {  // every ring read polled at once; all are taken when all have arrived
-          uint32_t rdy = 0, xv[kFlowReadsInRegs];
+          uint32_t rdy = 0, xv[NR];
 #pragma unroll
-          for (uint32_t k = 0; k < kFlowReadsInRegs; k++) {
+          for (uint32_t k = 0; k < NR; k++) {
             xv[k] = 0u;
             if ((pm >> k) & 1u) {
               const unsigned long long wv = ld_relaxed_cta_shared(&S.ring[ridx[k]]);
@@ -519,7 +522,7 @@ __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowPara
           }
           if (rdy == pm) {
 #pragma unroll
-            for (uint32_t k = 0; k < kFlowReadsInRegs; k++)
+            for (uint32_t k = 0; k < NR; k++)
               if ((pm >> k) & 1u) take(k, xv[k]);
             pm = 0u;
           }
@@ -528,7 +531,7 @@ __global__ void __launch_bounds__(kFlowExecThreads, 1) flow_exec_kernel(FlowPara
           for (unsigned long long m = gpend; m; m &= m - 1ull) {
             const uint32_t k = (uint32_t)__ffsll((long long)m) - 1u;
             uint32_t x;
-            if (flow_fetch(f, S, ro ? __ldg(&f.src[e0 + k]) : pick(sv, k), b, tag, x)) {
+            if (flow_fetch(f, S, ro ? __ldg(&f.src[e0 + k]) : pick<NR>(sv, k), b, tag, x)) {
               take(k, x);
               gpend &= ~(1ull << k);
             }

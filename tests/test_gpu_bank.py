@@ -278,6 +278,8 @@ FLOW_CASES = {
                         flow_warps=1),
     "zipf-16-warps": dict(n_acc=1 << 15, n=1 << 16, dist=cg.DIST_ZIPF, depth=8, up_reads=4,
                           ro=20, flow_warps=16),
+    "zipf-eight-reads": dict(n_acc=4096, n=32 * 300, dist=cg.DIST_ZIPF, depth=4, up_reads=8,
+                             ro=10),
 }
 
 
