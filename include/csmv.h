@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define CSMV_ABI_VERSION 1
+#define CSMV_ABI_VERSION 2 /* 2: csmv_bank_config.flow_warps, CSMV_ERR_IO, lanes and trace files */
 
 typedef enum csmv_status {
   CSMV_OK = 0,
