@@ -666,9 +666,10 @@ def main():
                      "kernel": "flow_exec_kernel (dataflow lane)", "peak_source": pk_kind,
                      "bytes_per_txn": B_UPDATE},
         "e2e": {"value": e2e, "unit": "committed tx/s", "h2d_bytes_per_step": h2d,
-                # per engine run: statistics (80 B) + commit-order words (768 B); up to three runs
-                # per step, plus the scheduler's 16 B of plan sizes and loss
-                "d2h_bytes_per_step": 3 * (80 + 768) + 16},
+                # per engine or lane run: statistics (80 B) + commit-order words (768 B); up to
+                # three runs per step, the scheduler's 16 B of plan sizes and loss, and the
+                # dataflow lane's 8 B of access count and widest transfer
+                "d2h_bytes_per_step": 3 * (80 + 768) + 16 + 8},
         "gpu_launches": learned["launches"],
         "clocks": clk.summary(),
     }
