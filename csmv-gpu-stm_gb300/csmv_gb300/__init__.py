@@ -50,7 +50,8 @@ class BankWorkload(C.Structure):
 class BankStream(C.Structure):
     _fields_ = [("n_txn", C.c_uint32), ("op", C.c_void_p), ("off", C.c_void_p),
                 ("addr", C.c_void_p), ("n_addr", C.c_uint64), ("txn_aborts", C.c_void_p),
-                ("split_round", C.c_uint32), ("deferred_warps", C.c_uint32)]
+                ("split_round", C.c_uint32), ("deferred_warps", C.c_uint32),
+                ("backoff", C.c_void_p), ("txn_waits", C.c_void_p)]
 
 
 class BankConfig(C.Structure):
@@ -126,7 +127,8 @@ class SchedConfig(C.Structure):
                 ("train_steps", C.c_uint32),
                 ("lr", C.c_float), ("threshold", C.c_float), ("defer_threshold", C.c_float),
                 ("deferred_warps", C.c_uint32), ("serial_lane", C.c_uint32),
-                ("seed", C.c_uint64), ("device", C.c_int32)]
+                ("seed", C.c_uint64), ("device", C.c_int32), ("plan", C.c_uint32),
+                ("hot_count", C.c_uint32), ("score", C.c_uint32), ("backoff_ns", C.c_uint32)]
 
 
 class SchedReport(C.Structure):
@@ -178,6 +180,7 @@ def lib() -> C.CDLL:
         "csmv_bank_read_values": (I32, [P, P]),
         "csmv_bank_read_versions": (I32, [P, P]),
         "csmv_bank_read_log": (I32, [P, P, U32, P, P, U32]),
+        "csmv_bank_read_groups": (I32, [P, P, U32]),
         "csmv_bank_device_info": (I32, [P, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                         C.POINTER(C.c_int), C.POINTER(C.c_size_t)]),
         "csmv_bank_destroy": (None, [P]),
@@ -403,15 +406,23 @@ class Bank:
                "csmv_bank_load")
 
     def run(self, stream: Stream, txn_aborts: np.ndarray | None = None, split_round: int = 0,
-            deferred_warps: int = 0) -> Stats:
+            deferred_warps: int = 0, backoff: np.ndarray | None = None,
+            txn_waits: np.ndarray | None = None) -> Stats:
         """Host buffers in: copies the stream to the device inside the call. txn_aborts (uint32
         [n_txn]) receives each transaction's failed attempts; split_round/deferred_warps set
-        up the deferred queue (csmv_bank_stream)."""
+        up the deferred queue; backoff (uint32 [n_txn], ns) bounds each transaction's pause
+        before a retry (csmv_bank_stream)."""
         st = Stats()
         s = stream.c_struct()
         if txn_aborts is not None:
             assert txn_aborts.dtype == np.uint32 and txn_aborts.shape[0] >= stream.n_txn
             s.txn_aborts = _ptr(txn_aborts)
+        if backoff is not None:
+            assert backoff.dtype == np.uint32 and backoff.shape[0] >= stream.n_txn
+            s.backoff = _ptr(backoff)
+        if txn_waits is not None:
+            assert txn_waits.dtype == np.uint32 and txn_waits.shape[0] >= stream.n_txn
+            s.txn_waits = _ptr(txn_waits)
         s.split_round, s.deferred_warps = split_round, deferred_warps
         rc = lib().csmv_bank_run(self._h, C.byref(s), C.byref(st))
         self.last_stats = st
@@ -459,6 +470,13 @@ class Bank:
         _check(lib().csmv_bank_read_log(self._h, _ptr(log_txn), max(1, n_commits), _ptr(outcome),
                                         _ptr(result), n_txn), "csmv_bank_read_log")
         return log_txn[:n_commits], outcome, result
+
+    def groups(self, n_commits: int) -> np.ndarray:
+        """Bitmap (uint32 words) of the last run's timestamps that end a commit group."""
+        out = np.empty(max(1, (n_commits + 31) // 32), np.uint32)
+        _check(lib().csmv_bank_read_groups(self._h, _ptr(out), max(1, n_commits)),
+               "csmv_bank_read_groups")
+        return out
 
     def device_info(self) -> dict:
         a, b, c_, d = C.c_int(), C.c_int(), C.c_int(), C.c_size_t()

@@ -101,6 +101,9 @@ static csmv_status validate_config(const csmv_bank_config* c) {
     if (c->client_warps * c->cluster_size > 32)
       return bad("client_warps x cluster_size must be <= 32 (one server lane per mailbox)");
   }
+  if (c->prevalidate > 3) return bad("prevalidate must be 0, 1, 2 or 3");
+  if (c->prevalidate >= 2 && c->validate != CSMV_VALIDATE_STAMP)
+    return bad("intra-warp chaining and group commit run the stamp protocol");
   if (c->validate != CSMV_VALIDATE_STAMP && c->batch == CSMV_BATCH_LANE &&
       c->writeback != CSMV_WRITEBACK_SERVER)
     return bad("per-transaction sections need server write-back");
@@ -124,6 +127,9 @@ static void free_all(csmv_bank_t* h) {
   cudaFree(h->d_off);
   cudaFree(h->d_addr);
   cudaFree(h->d_aborts);
+  cudaFree(h->d_backoff);
+  cudaFree(h->d_waits);
+  cudaFree(h->grp);
   flow_scratch_free(h->flow);
   h->flow = nullptr;
   if (h->ev0) cudaEventDestroy(h->ev0);
@@ -153,6 +159,8 @@ extern "C" csmv_status csmv_bank_create(const csmv_bank_config* cfg, csmv_bank_t
   h->threads = (int)(cfg->client_warps + 1) * 32;
   // cluster form: every CTA reserves the cluster's mailboxes; the leader's are used
   h->smem = cta_shared_bytes<kMaxR, kMaxW>(cfg->client_warps * (cluster ? cfg->cluster_size : 1u));
+  if (cfg->prevalidate == 3)  // one group-commit table per client warp of the CTA
+    h->smem = group_scratch_offset(h->smem) + cfg->client_warps * sizeof(GroupScratch);
   auto fail = [&](csmv_status s) {
     free_all(h);
     delete h;
@@ -218,7 +226,11 @@ extern "C" csmv_status csmv_bank_create(const csmv_bank_config* cfg, csmv_bank_t
       {(void**)&h->result, (size_t)cfg->max_txn * 4},  {(void**)&h->stats, ST_COUNT * 8},
       {(void**)&h->d_op, (size_t)cfg->max_txn * 4},    {(void**)&h->d_off, (size_t)cfg->max_txn * 4},
       {(void**)&h->d_aborts, (size_t)cfg->max_txn * 4},
+      {(void**)&h->d_backoff, (size_t)cfg->max_txn * 4},
+      {(void**)&h->d_waits, (size_t)cfg->max_txn * 4},
+      {(void**)&h->grp, (size_t)((h->log_cap + 31u) / 32u) * 4},
   };
+  h->grp_words = (h->log_cap + 31u) / 32u;
   for (auto& a : allocs) {
     if ((st = cuda_status(cudaMalloc(a.p, a.bytes), "cudaMalloc")) != CSMV_OK) return fail(st);
     h->device_bytes += a.bytes;
@@ -300,6 +312,7 @@ BankParams csmv::bank_params(const csmv_bank_t* h, const uint32_t* op, const uin
   p.prevalidate = c.prevalidate;
   p.spin_log2 = c.spin_limit_log2;
   p.txn_aborts = txn_aborts;
+  p.grp = (c.log_commits && c.prevalidate == 3 && c.validate == CSMV_VALIDATE_STAMP) ? h->grp : nullptr;
   return p;
 }
 
@@ -343,6 +356,11 @@ csmv_status csmv::bank_end_run(csmv_bank_t* h, uint32_t n_txn, csmv_stats* out) 
     out->kernel_ms = ms;
   }
   if (gs.error) {
+    if (gs.error == ERR_CAPACITY) {
+      set_error("device error 5: the run used more timestamps than the commit log holds "
+                "(8 x max_txn; aborted attempts take timestamps too)");
+      return CSMV_ERR_CAPACITY;
+    }
     set_error("device error %u (1 turn, 2 clock, 3 reply, 4 request, 5 capacity, 6 data, "
               "7 livelock, 8 dataflow wait)",
               gs.error);
@@ -353,12 +371,19 @@ csmv_status csmv::bank_end_run(csmv_bank_t* h, uint32_t n_txn, csmv_stats* out) 
 
 static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* off,
                           const uint32_t* addr, uint32_t n_txn, uint32_t* txn_aborts,
-                          uint32_t split_round, uint32_t deferred_warps, csmv_stats* out,
-                          bool serial = false) {
+                          uint32_t split_round, uint32_t deferred_warps, const uint32_t* backoff,
+                          uint32_t* txn_waits, csmv_stats* out, bool serial = false) {
   const csmv_bank_config& c = h->cfg;
   BankParams p = bank_params(h, op, off, addr, n_txn, txn_aborts);
   p.split_round = split_round;
   p.deferred_warps = deferred_warps;
+  p.backoff = backoff;
+  p.txn_waits = txn_waits;
+  if (txn_waits && (serial || c.prevalidate != 3))  // only group commit waits on locks
+    CSMV_CUDA(cudaMemsetAsync(txn_waits, 0, (size_t)n_txn * 4, h->stream));
+  if (serial) p.grp = nullptr;
+  if (p.grp) CSMV_CUDA(cudaMemsetAsync(h->grp, 0, (size_t)h->grp_words * 4, h->stream));
+  h->last_grouped = p.grp != nullptr;
   csmv_status bst = bank_begin_run(h);
   if (bst != CSMV_OK) return bst;
   void* args[] = {&p};
@@ -398,7 +423,7 @@ extern "C" csmv_status csmv_bank_run_device(csmv_bank_t* h, const csmv_bank_stre
   CSMV_CUDA(cudaSetDevice(h->cfg.device));
   auto t0 = std::chrono::steady_clock::now();
   st = launch(h, s->op, s->off, s->addr, s->n_txn, s->txn_aborts, s->split_round,
-              s->deferred_warps, out);
+              s->deferred_warps, s->backoff, s->txn_waits, out);
   if (out)
     out->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return st;
@@ -419,7 +444,8 @@ extern "C" csmv_status csmv_bank_run_serial_device(csmv_bank_t* h, const csmv_ba
   }
   CSMV_CUDA(cudaSetDevice(h->cfg.device));
   auto t0 = std::chrono::steady_clock::now();
-  st = launch(h, s->op, s->off, s->addr, s->n_txn, s->txn_aborts, 0, 0, out, true);
+  st = launch(h, s->op, s->off, s->addr, s->n_txn, s->txn_aborts, 0, 0, nullptr, s->txn_waits,
+              out, true);
   if (out)
     out->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return st;
@@ -445,11 +471,19 @@ extern "C" csmv_status csmv_bank_run(csmv_bank_t* h, const csmv_bank_stream* s, 
   CSMV_CUDA(cudaMemcpyAsync(h->d_op, s->op, (size_t)s->n_txn * 4, cudaMemcpyHostToDevice, h->stream));
   CSMV_CUDA(cudaMemcpyAsync(h->d_off, s->off, (size_t)s->n_txn * 4, cudaMemcpyHostToDevice, h->stream));
   CSMV_CUDA(cudaMemcpyAsync(h->d_addr, s->addr, s->n_addr * 4, cudaMemcpyHostToDevice, h->stream));
+  if (s->backoff)
+    CSMV_CUDA(cudaMemcpyAsync(h->d_backoff, s->backoff, (size_t)s->n_txn * 4,
+                              cudaMemcpyHostToDevice, h->stream));
   st = launch(h, h->d_op, h->d_off, h->d_addr, s->n_txn, s->txn_aborts ? h->d_aborts : nullptr,
-              s->split_round, s->deferred_warps, out);
-  if (st == CSMV_OK && s->txn_aborts) {
-    CSMV_CUDA(cudaMemcpyAsync(s->txn_aborts, h->d_aborts, (size_t)s->n_txn * 4,
-                              cudaMemcpyDeviceToHost, h->stream));
+              s->split_round, s->deferred_warps, s->backoff ? h->d_backoff : nullptr,
+              s->txn_waits ? h->d_waits : nullptr, out);
+  if (st == CSMV_OK && (s->txn_aborts || s->txn_waits)) {
+    if (s->txn_aborts)
+      CSMV_CUDA(cudaMemcpyAsync(s->txn_aborts, h->d_aborts, (size_t)s->n_txn * 4,
+                                cudaMemcpyDeviceToHost, h->stream));
+    if (s->txn_waits)
+      CSMV_CUDA(cudaMemcpyAsync(s->txn_waits, h->d_waits, (size_t)s->n_txn * 4,
+                                cudaMemcpyDeviceToHost, h->stream));
     CSMV_CUDA(cudaStreamSynchronize(h->stream));
   }
   if (out)
@@ -512,6 +546,28 @@ extern "C" csmv_status csmv_bank_read_log(csmv_bank_t* h, uint32_t* host_log_txn
   if (n_txn > h->last_n_txn) n_txn = h->last_n_txn;
   if (host_outcome) CSMV_CUDA(cudaMemcpy(host_outcome, h->outcome, (size_t)n_txn * 4, cudaMemcpyDeviceToHost));
   if (host_result) CSMV_CUDA(cudaMemcpy(host_result, h->result, (size_t)n_txn * 4, cudaMemcpyDeviceToHost));
+  return CSMV_OK;
+}
+
+extern "C" csmv_status csmv_bank_read_groups(csmv_bank_t* h, uint32_t* host_bits, uint32_t n_log) {
+  if (!h || !host_bits) return CSMV_ERR_INVALID_ARG;
+  if (!h->cfg.log_commits) {
+    set_error("handle was created with log_commits = 0");
+    return CSMV_ERR_STATE;
+  }
+  const uint32_t used = h->last_final_ts - h->run_base_ts;
+  if (n_log < used) {
+    set_error("group buffer covers %u timestamps, run used %u", n_log, used);
+    return CSMV_ERR_CAPACITY;
+  }
+  const uint32_t words = (used + 31u) / 32u;
+  if (!h->last_grouped) {  // every timestamp is its own group
+    for (uint32_t i = 0; i < (n_log + 31u) / 32u; i++) host_bits[i] = 0xFFFFFFFFu;
+    return CSMV_OK;
+  }
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  if (words) CSMV_CUDA(cudaMemcpy(host_bits, h->grp, (size_t)words * 4, cudaMemcpyDeviceToHost));
+  for (uint32_t i = words; i < (n_log + 31u) / 32u; i++) host_bits[i] = 0u;
   return CSMV_OK;
 }
 

@@ -235,6 +235,7 @@ extern "C" csmv_status csmv_bank_run_flow_device(csmv_bank_t* h, const csmv_bank
   CSMV_CUDA(cudaSetDevice(h->cfg.device));
   auto t0 = std::chrono::steady_clock::now();
   if ((st = ensure_txn(h, s->n_txn)) != CSMV_OK) return st;
+  h->last_grouped = false;  // the lane installs every write
   if ((st = bank_begin_run(h)) != CSMV_OK) return st;
   csmv_status lst = flow_launch(h, s);
   st = bank_end_run(h, s->n_txn, out);  // waits for the stream whatever happened

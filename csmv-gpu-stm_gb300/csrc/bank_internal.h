@@ -39,6 +39,11 @@ struct csmv_bank_t {
   uint32_t* d_off = nullptr;
   uint32_t* d_addr = nullptr;
   uint32_t* d_aborts = nullptr;
+  uint32_t* d_backoff = nullptr;  // host-buffer runs: the stream's backoff array, copied in
+  uint32_t* d_waits = nullptr;    // host-buffer runs: per-transaction lock waits, copied out
+  uint32_t* grp = nullptr;        // group-end bitmap of the last run (log_commits)
+  uint32_t grp_words = 0;
+  bool last_grouped = false;      // the last run was a group-commit run of the engine
   uint64_t addr_cap = 0;
   bool loaded = false;
   uint32_t last_final_ts = 0, last_n_txn = 0, run_base_ts = 0;

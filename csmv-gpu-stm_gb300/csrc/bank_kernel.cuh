@@ -39,6 +39,10 @@ namespace csmv {
 constexpr uint32_t kSnapFlag = 0x80000000u;
 constexpr uint32_t kHole = 0xFFFFFFFFu;  // log entry of a timestamp whose transaction aborted
 constexpr uint32_t kPendingFlag = 0x80000000u;  // lock word: holder's commit timestamp is known
+// Group commit: lock word of a holder that holds every lock of its group and is drawing its
+// timestamps (bit 31 clear). A holder without it is still acquiring, so its timestamps will be
+// drawn after any validator that sees it - that validator may ignore its lock.
+constexpr uint32_t kReadyFlag = 0x40000000u;
 constexpr int kMaxClientWarps = 15;
 constexpr int kHashSize = 4096;  // shared-memory hash entries (power of two)
 constexpr int kBatchDescs = 32;
@@ -95,6 +99,11 @@ struct BankParams {
   uint32_t* txn_aborts;     // optional [n_rounds*32]: failed attempts of each transaction
   uint32_t split_round;     // rounds [split_round, n_rounds) form the deferred queue (0 = none)
   uint32_t deferred_warps;  // client warps (lowest global ids) that serve the deferred queue
+  uint32_t* grp;            // group commit with log: bit (ts-1-log_base) = ts ends a commit group
+  uint32_t* txn_waits;      // optional [n_rounds*32]: 1 when the transaction's group waited for a
+                            // lock another warp held (group commit)
+  const uint32_t* backoff;  // optional [n_rounds*32]: longest pause (ns) before a retry of each
+                            // transaction (a scheduler's per-transaction backoff)
 };
 
 template <int MAXR, int MAXW>
@@ -136,6 +145,48 @@ static_assert(offsetof(CtaShared8x2, hkey) % 16 == 0, "hash table must be 16-byt
 template <int MAXR, int MAXW>
 __host__ __device__ constexpr size_t cta_shared_bytes(uint32_t nc) {
   return sizeof(CtaShared<MAXR, MAXW>) + (nc - 1) * sizeof(MailSlot<MAXR, MAXW>);
+}
+
+// Group commit (prevalidate == 3): per-client-warp table of the accounts the warp's round may
+// write (at most 64: two per lane), their writer lanes, lock state and latest committed value,
+// plus each lane's chain outputs. Lives in dynamic shared memory after the mailboxes.
+constexpr int kGrpSlots = 128;  // power of two, >= 2 x 64
+constexpr uint32_t kGrpEmpty = 0xFFFFFFFFu;
+struct GroupScratch {
+  uint32_t key[kGrpSlots];    // account (kGrpEmpty = free)
+  uint32_t wmask[kGrpSlots];  // lanes whose transfer may write it
+  uint32_t busy[kGrpSlots];   // 1 when its lock was held by another warp at the first try
+  int32_t base[kGrpSlots];    // its latest committed value, read under the warp's lock
+  int32_t out0[32], out1[32]; // per lane: value written to its debit / credit account
+  uint32_t wa0[32], wa1[32];  // per lane: its debit / credit account
+};
+
+__host__ __device__ constexpr size_t group_scratch_offset(size_t cta_bytes) {
+  return (cta_bytes + 15u) & ~size_t(15u);
+}
+
+__device__ __forceinline__ uint32_t grp_hash(uint32_t a) { return (a * 0x9E3779B1u) >> 25; }
+
+// Slot of account x in the warp's table, inserting it (lanes of one warp insert concurrently).
+__device__ __forceinline__ int grp_insert(GroupScratch& gx, uint32_t x) {
+  uint32_t h = grp_hash(x);
+  for (uint32_t probe = 0; probe < (uint32_t)kGrpSlots; probe++) {
+    const uint32_t prev = atomicCAS(&gx.key[h], kGrpEmpty, x);
+    if (prev == kGrpEmpty || prev == x) return (int)h;
+    h = (h + 1u) & (kGrpSlots - 1u);
+  }
+  return -1;  // unreachable: at most 64 keys
+}
+
+__device__ __forceinline__ int grp_find(const GroupScratch& gx, uint32_t x) {
+  uint32_t h = grp_hash(x);
+  for (uint32_t probe = 0; probe < (uint32_t)kGrpSlots; probe++) {
+    const uint32_t k = gx.key[h];
+    if (k == x) return (int)h;
+    if (k == kGrpEmpty) return -1;
+    h = (h + 1u) & (kGrpSlots - 1u);
+  }
+  return -1;
 }
 
 __device__ __forceinline__ uint32_t hash_addr(uint32_t a) {
@@ -218,6 +269,17 @@ struct SlotEditor {
 #pragma unroll
     for (int d = 0; d < DEPTH; d++) st_relaxed_gpu(item + d, s[d]);
   }
+  // value of the version with timestamp ts (false when the slots do not hold it)
+  __device__ __forceinline__ bool find(uint32_t ts, int32_t& v) const {
+    bool f = false;
+#pragma unroll
+    for (int d = 0; d < DEPTH; d++)
+      if (version_ts(s[d]) == ts) {
+        v = version_val(s[d]);
+        f = true;
+      }
+    return f;
+  }
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -227,14 +289,20 @@ struct SlotEditor {
 // Mark timestamps [lo, hi] complete (their write-back is visible), then move the clock over the
 // longest complete prefix. Any warp may advance: a CAS keeps the clock monotonic, and the warp
 // that passes the end of a bitmap word clears it for the next lap. Called by one lane.
+// A range is published atomically for the clock: its bitmap words are set from the highest down,
+// fenced, and the scan below reads words with acquire loads in ascending order, so a scan that
+// sees the range's lowest bits sees all of them - the clock never stops inside a range (a group
+// commit's intermediate versions are never installed, and no snapshot may fall between them).
 static __device__ void complete_range(uint32_t* done, uint32_t done_mask, GlobalSync* gs, uint32_t lo,
                                uint32_t hi) {
   __threadfence();
-  for (uint32_t t = lo; t <= hi;) {
-    const uint32_t bit = t & 31u, span = min(32u - bit, hi - t + 1);
+  for (uint32_t w = hi >> 5;; w--) {
+    const uint32_t t0 = max(lo, w << 5), t1 = min(hi, (w << 5) + 31u);
+    const uint32_t span = t1 - t0 + 1u, bit = t0 & 31u;
     const uint32_t m = (span == 32u ? 0xFFFFFFFFu : ((1u << span) - 1u)) << bit;
-    atomicOr(&done[(t >> 5) & done_mask], m);
-    t += span;
+    atomicOr(&done[w & done_mask], m);
+    if (w == (lo >> 5)) break;
+    __threadfence();
   }
   // store-buffering pattern with the warp completing the range below ours: with SC fences on
   // both sides at least one of us sees the other's bits, so the clock never stalls
@@ -244,7 +312,7 @@ static __device__ void complete_range(uint32_t* done, uint32_t done_mask, Global
     uint32_t n = c;
     for (uint32_t words = 0; words < 64; words++) {  // bounded scan per attempt
       const uint32_t t = n + 1, bit = t & 31u;
-      const uint32_t w = ld_relaxed_gpu(&done[(t >> 5) & done_mask]) >> bit;
+      const uint32_t w = ld_acquire_gpu(&done[(t >> 5) & done_mask]) >> bit;
       const uint32_t ones = (w == 0xFFFFFFFFu) ? 32u : (uint32_t)(__ffs(~w) - 1);
       const uint32_t run = min(ones, 32u - bit);
       n += run;
@@ -279,13 +347,350 @@ __device__ __forceinline__ void batch_done(const BankParams& p, CtaShared<MAXR, 
 }
 
 // ---------------------------------------------------------------------------------------------
+// group commit (prevalidate == 3, stamp protocol)
+// ---------------------------------------------------------------------------------------------
+
+// Lock of account x by a 64-bit CAS of its commit word from (stamp, free) to (stamp, owner):
+// the lock and, in the same atomic, a check that `stamp` (the version the caller read) is still
+// the latest. When only the stamp moved, the lock is taken at the new stamp and *stale is set
+// (the caller re-reads the value under the lock). False when another warp holds the lock.
+__device__ __forceinline__ unsigned long long lock_word(uint32_t stamp, uint32_t owner) {
+  return ((unsigned long long)owner << 32) | stamp;
+}
+
+__device__ __forceinline__ bool group_cas_lock(unsigned long long* cw, uint32_t x, uint32_t me,
+                                               uint32_t& stamp, bool& stale) {
+  for (int r = 0; r < 8; r++) {
+    const unsigned long long exp = stamp;
+    const unsigned long long old = atomicCAS(cw + x, exp, exp | ((unsigned long long)me << 32));
+    if (old == exp) return true;
+    if ((old >> 32) != 0ull) return false;
+    stamp = (uint32_t)old;
+    stale = true;
+  }
+  return false;
+}
+
+// Waits for account x's lock and takes it, with the account's version slots (ed) and latest value
+// (v) read as the lock is taken: the poll that finds the lock free is an acquire load, so the
+// slots loaded after it hold the version of the stamp it saw, and a CAS that succeeds at that
+// stamp proves them current (*stale stays false). Every waiter polls at the same short interval
+// (a back-off that grows with the wait would hand a contended lock to the newest waiters and
+// starve the oldest). Bounded: false after 2^18 polls (about 100 ms), or once another warp
+// raised a device error.
+template <int DEPTH>
+__device__ __forceinline__ bool group_wait_lock(const BankParams& p, uint32_t x, uint32_t me,
+                                                uint32_t& stamp, bool& stale,
+                                                SlotEditor<DEPTH>& ed, int32_t& v) {
+  for (uint32_t it = 0; it < (1u << 18); it++) {
+    const unsigned long long w = ld_acquire_gpu(&p.cw[x]);
+    if ((w >> 32) == 0ull) {
+      ed.load(p.slots + (size_t)x * DEPTH);
+      if (atomicCAS(&p.cw[x], w, w | ((unsigned long long)me << 32)) == w) {
+        stamp = (uint32_t)w;
+        stale = !ed.find(stamp, v);
+        return true;
+      }
+      continue;  // another waiter took it: poll again
+    }
+    if ((it & 63u) == 63u && ld_relaxed_gpu(&p.gs->error) != 0u) return false;
+    __nanosleep(64);
+  }
+  return false;
+}
+
+// One attempt of a transfer round as a commit group, warp-collective. Every active lane's
+// transfer may write its two accounts; the warp locks each such account once (its lowest writer
+// lane does), in ascending account order, waiting for a lock held elsewhere while it holds only
+// locks on smaller accounts (no cycle of waits is possible; a warp queued for a hot account
+// holds nothing, so the locks it needs next are free when its turn comes). Every access of this
+// mode to a commit word is a full 8-byte access. The locked accounts' latest values
+// are read under the locks; the commit server then gives the group consecutive timestamps in
+// lane order; every read of an account the group does not lock (a foreign read) is validated
+// against its commit word, as the stamp protocol validates any transaction; the lanes that pass
+// run in lane order as a chain through the locked accounts (each reads the value left by the
+// nearest lower lane that wrote it, else the locked value), so a dependent transfer never
+// aborts for a lower lane of its own group; and each locked account gets ONE new version, the
+// last group member's write. Intermediate versions of a group are never observable: snapshots
+// come from the clock, which passes a group's timestamps at once (complete_range), and latest
+// reads follow the stamp, which is published with the last version. A lane that fails
+// validation leaves a hole at its timestamp and is retried; when a lock wait runs out the whole
+// attempt is dropped before any timestamp is drawn (*gave_up). Returns the committed lanes.
+template <int DEPTH, int MAXR, int MAXW, bool CLUSTER>
+__device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm,
+                                  MailSlot<MAXR, MAXW>& ms, GroupScratch& gx, uint32_t me,
+                                  uint32_t t, uint32_t op, uint32_t nr,
+                                  const uint32_t (&a)[MAXR], bool act, uint32_t& seq,
+                                  bool& gave_up, bool& failed, bool& waited) {
+  constexpr uint32_t FULL = 0xFFFFFFFFu;
+  const uint32_t lane = lane_id();
+  const VersionStore vs{p.slots, p.n_items};
+  gave_up = false;
+  // 1. the accounts the round may write, with their writer lanes
+  for (uint32_t i = lane; i < (uint32_t)kGrpSlots; i += 32) {
+    gx.key[i] = kGrpEmpty;
+    gx.wmask[i] = 0u;
+    gx.busy[i] = 0u;
+  }
+  __syncwarp();
+  int s0 = -1, s1 = -1;
+  if (act) {
+    s0 = grp_insert(gx, a[0]);
+    s1 = a[1] == a[0] ? s0 : grp_insert(gx, a[1]);
+    atomicOr(&gx.wmask[s0], 1u << lane);
+    if (s1 != s0) atomicOr(&gx.wmask[s1], 1u << lane);
+    gx.wa0[lane] = a[0];
+    gx.wa1[lane] = a[1];
+  }
+  __syncwarp();
+  int rsl[MAXR];  // table slot of each read, -1 for a foreign read
+#pragma unroll
+  for (int k = 0; k < MAXR; k++)
+    rsl[k] = (!act || k >= (int)nr) ? -1 : k == 0 ? s0 : k == 1 ? s1 : grp_find(gx, a[k]);
+  const bool lead0 = act && (uint32_t)(__ffs(gx.wmask[s0]) - 1) == lane;
+  const bool lead1 = act && s1 != s0 && (uint32_t)(__ffs(gx.wmask[s1]) - 1) == lane;
+
+  // 2. locks, ascending account order, waiting (bounded) for locks held elsewhere. A leader
+  //    keeps the account's version slots from its read: the write-back edits them in registers.
+  uint32_t st0 = 0, st1 = 0;
+  int32_t bv0 = 0, bv1 = 0;
+  SlotEditor<DEPTH> ed0, ed1;
+  bool stale0 = false, stale1 = false, h0 = false, h1 = false;
+  if (lead0) {
+    st0 = (uint32_t)ld_acquire_gpu(&p.cw[a[0]]);
+    ed0.load(p.slots + (size_t)a[0] * DEPTH);
+  }
+  if (lead1) {
+    st1 = (uint32_t)ld_acquire_gpu(&p.cw[a[1]]);
+    ed1.load(p.slots + (size_t)a[1] * DEPTH);
+  }
+  if (lead0) stale0 = !ed0.find(st0, bv0);
+  if (lead1) stale1 = !ed1.find(st1, bv1);
+  if (lead0) h0 = group_cas_lock(p.cw, a[0], me, st0, stale0);
+  if (lead1) h1 = group_cas_lock(p.cw, a[1], me, st1, stale1);
+  if (lead0 && !h0) gx.busy[s0] = 1u;
+  if (lead1 && !h1) gx.busy[s1] = 1u;
+  __syncwarp();
+  waited = act && (gx.busy[s0] | gx.busy[s1]) != 0u;
+  bool all = false;
+  for (uint32_t it = 0; it <= 64u; it++) {  // each pass settles the smallest account still missing
+    const uint32_t m0 = (lead0 && !h0) ? a[0] : kGrpEmpty, m1 = (lead1 && !h1) ? a[1] : kGrpEmpty;
+    const uint32_t f = __reduce_min_sync(FULL, min(m0, m1));
+    if (f == kGrpEmpty) {
+      all = true;
+      break;
+    }
+    if (h0 && a[0] > f) {  // hold nothing above the lock being waited for
+      st_relaxed_gpu(&p.cw[a[0]], (unsigned long long)st0);
+      h0 = false;
+    }
+    if (h1 && a[1] > f) {
+      st_relaxed_gpu(&p.cw[a[1]], (unsigned long long)st1);
+      h1 = false;
+    }
+    bool ok = true;
+    if (lead0 && !h0 && a[0] == f)
+      ok = h0 = group_wait_lock<DEPTH>(p, a[0], me, st0, stale0, ed0, bv0);
+    else if (lead1 && !h1 && a[1] == f)
+      ok = h1 = group_wait_lock<DEPTH>(p, a[1], me, st1, stale1, ed1, bv1);
+    if (__any_sync(FULL, !ok)) break;
+    if (lead0 && !h0 && a[0] > f) h0 = group_cas_lock(p.cw, a[0], me, st0, stale0);
+    if (lead1 && !h1 && a[1] > f) h1 = group_cas_lock(p.cw, a[1], me, st1, stale1);
+  }
+  if (!all) {  // a wait ran out: release everything, the round retries later
+    if (h0) st_relaxed_gpu(&p.cw[a[0]], (unsigned long long)st0);
+    if (h1) st_relaxed_gpu(&p.cw[a[1]], (unsigned long long)st1);
+    gave_up = true;
+    return 0u;
+  }
+  // 3. latest values of the locked accounts whose slots were read before their stamp moved (the
+  //    stamp cannot move while the lock is held), then the ready marks: every lock of the group
+  //    is held and its timestamps are drawn next (the server's fence orders these marks before
+  //    its draw: the mailbox hand-off carries them to it)
+  if (__any_sync(FULL, (lead0 && stale0) || (lead1 && stale1))) {
+    fence_acq_rel_gpu();  // the previous holders' versions are visible before they are read
+    bool lost = false;
+    if (lead0 && stale0) {
+      ed0.load(p.slots + (size_t)a[0] * DEPTH);
+      lost |= !ed0.find(st0, bv0);
+    }
+    if (lead1 && stale1) {
+      ed1.load(p.slots + (size_t)a[1] * DEPTH);
+      lost |= !ed1.find(st1, bv1);
+    }
+    if (lost) raise_error(&p.gs->error, ERR_DATA);  // the latest version must be present
+  }
+  if (lead0) {
+    gx.base[s0] = bv0;
+    st_relaxed_gpu(&p.cw[a[0]], lock_word(st0, me | kReadyFlag));
+  }
+  if (lead1) {
+    gx.base[s1] = bv1;
+    st_relaxed_gpu(&p.cw[a[1]], lock_word(st1, me | kReadyFlag));
+  }
+  const uint32_t inc = __ballot_sync(FULL, act);
+  __syncwarp();
+
+  // 4. post the group to the commit server; the foreign reads run while it draws
+  seq++;
+  if (lane == 0) {
+    ms.snap = 0u;
+    ms.cand = inc;
+    mail_release<CLUSTER>(&ms.req, seq);
+  }
+  int32_t fv[MAXR];
+  uint32_t fst[MAXR];
+  bool fok = true;
+#pragma unroll
+  for (int k = 0; k < MAXR; k++) {
+    fv[k] = 0;
+    fst[k] = 0u;
+    if (act && k < (int)nr && rsl[k] < 0) fok &= read_latest<DEPTH>(vs, p.cw, a[k], fst[k], fv[k]);
+  }
+  bool ok_wait = true;
+  if (lane == 0)
+    ok_wait = bounded_wait([&] { return mail_acquire<CLUSTER>(&ms.rep) == seq; }, &p.gs->error,
+                           ERR_WAIT_REPLY, p.spin_log2);
+  ok_wait = __shfl_sync(FULL, ok_wait, 0);
+  if (!ok_wait) {
+    failed = true;
+    return 0u;
+  }
+  (void)mail_acquire<CLUSTER>(&ms.rep);
+  const uint32_t base = ms.base, n_ts = __popc(inc);
+  const uint32_t my_ts = base + 1u + __popc(inc & lanemask_lt());
+  fence_acq_rel_gpu();
+
+  // 5. the group's first timestamp in its locks, then validation of the foreign reads: the stamp
+  //    read must still be the latest, and a lock of a holder ordered before us (or whose
+  //    timestamps are being drawn) must be resolved first. Waits point only to earlier
+  //    timestamps or to holders already drawing: no cycles.
+  if (lead0) st_relaxed_gpu(&p.cw[a[0]], lock_word(st0, kPendingFlag | (base + 1u)));
+  if (lead1) st_relaxed_gpu(&p.cw[a[1]], lock_word(st1, kPendingFlag | (base + 1u)));
+  bool valid = act && fok;
+  if (valid) {
+    unsigned long long word[MAXR];
+#pragma unroll
+    for (int k = 0; k < MAXR; k++)
+      word[k] = (k < (int)nr && rsl[k] < 0) ? ld_relaxed_gpu(&p.cw[a[k]]) : 0ull;
+#pragma unroll
+    for (int k = 0; k < MAXR; k++) {
+      if (k >= (int)nr || rsl[k] >= 0 || !valid) continue;
+      unsigned long long wd = word[k];
+      bool settled = false;
+      for (uint32_t it = 0; it < 4096u; it++) {
+        const uint32_t own = (uint32_t)(wd >> 32);
+        bool clear;
+        if (own == 0u)
+          clear = true;
+        else if (own & kPendingFlag)
+          clear = (own & ~kPendingFlag) >= my_ts;  // its group is ordered after ours
+        else
+          clear = !(own & kReadyFlag);  // still acquiring: its timestamps follow ours
+        if (clear) {
+          settled = true;
+          break;
+        }
+        __nanosleep(32);
+        wd = ld_relaxed_gpu(&p.cw[a[k]]);
+      }
+      valid = settled && (uint32_t)wd == fst[k];
+    }
+  }
+  const uint32_t fin = __ballot_sync(FULL, valid);
+
+  // 6. the chain, in lane order through the locked accounts
+  uint32_t dep = 0u;
+#pragma unroll
+  for (int k = 0; k < MAXR; k++)
+    if (valid && rsl[k] >= 0) dep |= gx.wmask[rsl[k]];
+  dep &= fin & lanemask_lt();
+  uint32_t done = ~fin, hw = 0u;
+  bool computed = !valid, has_w = false;
+  for (uint32_t it = 0; it < 33u && done != FULL; it++) {
+    const bool ready = !computed && (dep & ~done) == 0u;
+    if (ready) {
+      int32_t v[MAXR];
+#pragma unroll
+      for (int k = 0; k < MAXR; k++) {
+        v[k] = 0;
+        if (k >= (int)nr) continue;
+        if (rsl[k] < 0) {
+          v[k] = fv[k];
+        } else {
+          const uint32_t wr = gx.wmask[rsl[k]] & hw & lanemask_lt();
+          if (wr) {
+            const uint32_t j = 31u - __clz(wr);
+            v[k] = gx.wa1[j] == a[k] ? gx.out1[j] : gx.out0[j];  // a transfer writes a1 last
+          } else {
+            v[k] = gx.base[rsl[k]];
+          }
+        }
+      }
+      int32_t w0 = 0, w1 = 0;
+      has_w = transfer_writes<MAXR>(op, nr, v, w0, w1);
+      gx.out0[lane] = w0;
+      gx.out1[lane] = w1;
+      computed = true;
+    }
+    done |= __ballot_sync(FULL, ready);
+    hw |= __ballot_sync(FULL, ready && has_w);
+    __syncwarp();
+  }
+
+  // 7. one version per locked account (its last writer's), then the stamp (a release store: the
+  //    version is visible first) and the unlock
+  auto install = [&](int s, uint32_t x, SlotEditor<DEPTH>& ed) -> uint32_t {
+    const uint32_t wr = gx.wmask[s] & hw;
+    if (!wr) return 0u;
+    const uint32_t j = 31u - __clz(wr);
+    const int32_t val = gx.wa1[j] == x ? gx.out1[j] : gx.out0[j];
+    const uint32_t ts = base + 1u + __popc(inc & ((1u << j) - 1u));
+    ed.insert(ts, val);
+    ed.store(p.slots + (size_t)x * DEPTH);
+    return ts;
+  };
+  uint32_t pub0 = 0u, pub1 = 0u;
+  if (lead0) pub0 = install(s0, a[0], ed0);
+  if (lead1) pub1 = install(s1, a[1], ed1);
+  if (lead0) st_release_gpu(&p.cw[a[0]], (unsigned long long)(pub0 ? pub0 : st0));
+  if (lead1) st_release_gpu(&p.cw[a[1]], (unsigned long long)(pub1 ? pub1 : st1));
+
+  // 8. log, outcomes, the group's end, completion
+  if (p.log && act) {
+    const uint32_t li = my_ts - 1u - p.log_base;
+    if (li < p.log_cap)
+      p.log_txn[li] = valid ? t : kHole;
+    else
+      raise_error(&p.gs->error, ERR_CAPACITY);
+    if (valid) {
+      p.outcome[t] = my_ts;
+      p.result[t] = 0;
+    }
+  }
+  __syncwarp();
+  if (lane == 0) {
+    if (p.log && p.grp) {
+      const uint32_t li = base + n_ts - 1u - p.log_base;
+      if (li < p.log_cap) atomicOr(&p.grp[li >> 5], 1u << (li & 31u));
+    }
+    complete_range(p.done, p.done_mask, p.gs, base + 1u, base + n_ts);
+    stat_add(sm.stat, ST_COMMIT_UPDATE, __popc(hw));
+    stat_add(sm.stat, ST_COMMIT_NOWRITE, __popc(fin & ~hw));
+    stat_add(sm.stat, ST_ABORT_READ_WRITE, __popc(inc & ~fin));
+  }
+  return fin;
+}
+
+// ---------------------------------------------------------------------------------------------
 // client side
 // ---------------------------------------------------------------------------------------------
 // CLUSTER: the mailbox `ms` (and the finished-client counter) live in the shared memory of the
 // cluster's leader CTA, reached through distributed shared memory; else in this CTA's.
+// gx: this warp's group-commit table (prevalidate == 3), in this CTA's shared memory.
 template <int DEPTH, int MAXR, int MAXW, bool CLUSTER = false>
 __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint32_t w,
-                            MailSlot<MAXR, MAXW>& ms, uint32_t* done_ctr) {
+                            MailSlot<MAXR, MAXW>& ms, uint32_t* done_ctr, GroupScratch* gx) {
   const uint32_t lane = lane_id();
   const VersionStore vs{p.slots, p.n_items};
   const bool stamp = p.validate == CSMV_VALIDATE_STAMP;
@@ -338,13 +743,18 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
     }
 
     uint32_t pending = 0xFFFFFFFFu;
-    uint32_t attempts = 0, lock_fails = 0, tries = 0;
+    uint32_t attempts = 0, lock_fails = 0, tries = 0, stuck = 0;
+    if (p.txn_waits) p.txn_waits[t] = 0u;
     while (pending) {
       if (lane == 0) atomicAdd(&sm.stat[ST_ROUNDS], 1ull);
       tries += (pending >> lane) & 1u;
       if (lock_fails) {  // randomized, growing back-off after a lost lock: breaks lock-step retries
         const uint32_t h = (me * 0x9E3779B1u) ^ (attempts * 0x85EBCA6Bu);
         __nanosleep((h >> 16) & ((64u << lock_fails) - 1u));
+      }
+      if (p.backoff && attempts > 0) {  // a scheduler's per-transaction pause before a retry
+        const uint32_t bo = __reduce_max_sync(0xFFFFFFFFu, ((pending >> lane) & 1u) ? p.backoff[t] : 0u);
+        if (bo) __nanosleep(((me * 0x85EBCA6Bu) ^ (attempts * 0x9E3779B1u)) % bo);
       }
       if (++attempts > (1u << 20)) {  // no round may retry forever: report and leave
         if (lane == 0) raise_error(&p.gs->error, ERR_LIVELOCK);
@@ -384,6 +794,31 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
           stat_add(sm.stat, ST_ABORT_DATA_AGE, __popc(am));
         }
         pending &= ~dm;
+        continue;
+      }
+
+      if (stamp && p.prevalidate == 3) {  // group commit of the round's transfers
+        bool gave_up = false, waited = false;
+        const uint32_t fin = group_attempt<DEPTH, MAXR, MAXW, CLUSTER>(
+            p, sm, ms, *gx, me, t, op, nr, a, mine, seq, gave_up, failed, waited);
+        if (failed) break;
+        if (p.txn_waits && waited) p.txn_waits[t] = 1u;
+        if (lane == 0 && gave_up) stat_add(sm.stat, ST_ABORT_WRITE_WRITE, __popc(pending));
+        lock_fails = gave_up ? min(lock_fails + 1, 6u) : 0u;
+        // a lock that stays held across 64 bounded waits (about 3 s) is reported, not retried on
+        if (gave_up && lock_fails == 6u && ++stuck > 64u) {
+          if (lane == 0) raise_error(&p.gs->error, ERR_LIVELOCK);
+          failed = true;
+          break;
+        }
+        if (!gave_up) stuck = 0;
+        pending &= ~fin;
+        uint32_t err = 0;
+        if (lane == 0) err = ld_relaxed_gpu(&p.gs->error);
+        if (__shfl_sync(0xFFFFFFFFu, err, 0) != 0) {
+          failed = true;
+          break;
+        }
         continue;
       }
 
@@ -884,16 +1319,17 @@ __device__ __forceinline__ uint32_t poll_mailboxes(uint32_t nc, GlobalSync* gs, 
 template <class SM, bool CLUSTER = false>
 __device__ void server_warp_stamp(uint32_t nc, uint32_t batch, GlobalSync* gs, SM& sm) {
   const uint32_t lane = lane_id();
-  uint32_t seen = 0;
+  uint32_t seen = 0, idle = 0;
   for (;;) {
     uint32_t req;
     bool stop;
     uint32_t ready = poll_mailboxes<SM, CLUSTER>(nc, gs, sm, seen, &req, &stop);
     if (ready == 0) {
       if (stop) break;
-      __nanosleep(64);
+      if (++idle > 256u) __nanosleep(64);  // spin a while first: the reply is latency-critical
       continue;
     }
+    idle = 0;
     if (batch != CSMV_BATCH_CTA) ready &= (0u - ready);  // one warp per assignment
     const bool mine = lane < nc && ((ready >> lane) & 1u);
     uint32_t cnt = 0;
@@ -1653,7 +2089,10 @@ __global__ void __launch_bounds__(512, 1) bank_kernel(BankParams p) {
     else
       server_warp_ring<DEPTH, MAXR, MAXW>(p, sm);
   } else {
-    client_warp<DEPTH, MAXR, MAXW>(p, sm, warp - 1, sm.mail[warp - 1], &sm.done_warps);
+    GroupScratch* gx = reinterpret_cast<GroupScratch*>(
+        smem_raw + group_scratch_offset(cta_shared_bytes<MAXR, MAXW>(p.nc)));
+    client_warp<DEPTH, MAXR, MAXW>(p, sm, warp - 1, sm.mail[warp - 1], &sm.done_warps,
+                                   gx + (warp - 1));
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < ST_COUNT; i += blockDim.x)
@@ -1686,8 +2125,10 @@ __global__ void __launch_bounds__(512, 1) bank_cluster_kernel(BankParams p) {
   if (warp == 0) {
     if (rank == 0) server_warp_stamp<CtaShared<MAXR, MAXW>, true>(nct, p.batch, p.gs, sm);
   } else {
+    GroupScratch* gx = reinterpret_cast<GroupScratch*>(
+        smem_raw + group_scratch_offset(cta_shared_bytes<MAXR, MAXW>(nct)));
     client_warp<DEPTH, MAXR, MAXW, true>(p, sm, warp - 1, lead->mail[rank * p.nc + warp - 1],
-                                         &lead->done_warps);
+                                         &lead->done_warps, gx + (warp - 1));
   }
   cluster.sync();  // no CTA leaves while its mailboxes in the leader may still be touched
   for (uint32_t i = threadIdx.x; i < ST_COUNT; i += blockDim.x)

@@ -10,6 +10,7 @@
 // train_steps Adam steps, and their per-bin abort rates refresh the recent-abort features;
 // (2) plan - the network scores the rest, flagged transfers are spread out by key
 // (sched_kernels.cuh), and the planned stream runs.
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 
@@ -41,6 +42,11 @@ struct csmv_sched_t {
            *bucket_fill = nullptr;
   uint32_t *order = nullptr, *perm = nullptr, *op2 = nullptr, *off2 = nullptr;
   uint32_t *ro_flag = nullptr, *ro_scan = nullptr, *ro_list = nullptr, *n_flagged = nullptr;
+  uint32_t* waits = nullptr;  // probe: per-transaction lock waits of the engine
+  // grouped plan (plan 1)
+  uint32_t *hidx = nullptr, *key_start = nullptr, *tile_sum = nullptr, *tile_off = nullptr;
+  uint32_t *rank = nullptr, *cold_pos = nullptr, *sorted = nullptr, *rbucket = nullptr;
+  uint32_t *round_order = nullptr, *bo = nullptr, *bo2 = nullptr, *max_count = nullptr;
   uint64_t chunks = 0;
   // the current chunk
   uint32_t n = 0, probe_rounds = 0, split_round = 0, planned = 0, serial_rounds = 0;
@@ -62,13 +68,19 @@ extern "C" void csmv_sched_config_default(csmv_sched_config* c) {
   c->serial_lane = 0;
   c->seed = 1;
   c->device = 0;
+  c->plan = 1;
+  c->hot_count = 0;
+  c->score = 0;
+  c->backoff_ns = 2048;
 }
 
 static void free_all(csmv_sched_t* s) {
   void* bufs[] = {s->sketch, s->key_count, s->key_rank, s->x, s->y, s->p, s->rates, s->aborts,
                   s->bin_stats, s->key, s->bucket, s->bucket_count, s->bucket_start,
                   s->bucket_fill, s->order, s->perm, s->op2, s->off2, s->ro_flag, s->ro_scan,
-                  s->ro_list, s->n_flagged};
+                  s->ro_list, s->n_flagged, s->waits, s->hidx, s->key_start, s->tile_sum,
+                  s->tile_off, s->rank, s->cold_pos, s->sorted, s->rbucket, s->round_order,
+                  s->bo, s->bo2, s->max_count};
   for (void* b : bufs) cudaFree(b);
   for (auto& e : s->ev)
     if (e) cudaEventDestroy(e);
@@ -81,7 +93,7 @@ extern "C" csmv_status csmv_sched_create(const csmv_sched_config* cfg, csmv_sche
   *out = nullptr;
   if (cfg->n_accounts < 2 || cfg->max_txn == 0 || cfg->max_txn % 32 || cfg->max_txn > (1u << 26) ||
       cfg->probe_rounds_pct > 100 || cfg->probe_every == 0 || !(cfg->lr > 0.f) ||
-      cfg->deferred_warps == 0 || cfg->serial_lane > 2) {
+      cfg->deferred_warps == 0 || cfg->serial_lane > 2 || cfg->plan > 1 || cfg->score > 1) {
     set_error("invalid scheduler config");
     return CSMV_ERR_INVALID_ARG;
   }
@@ -114,6 +126,13 @@ extern "C" csmv_status csmv_sched_create(const csmv_sched_config* cfg, csmv_sche
       {(void**)&s->op2, n * 4},          {(void**)&s->off2, n * 4},
       {(void**)&s->ro_flag, R * 4},      {(void**)&s->ro_scan, R * 4},
       {(void**)&s->ro_list, R * 4},      {(void**)&s->n_flagged, 4},
+      {(void**)&s->waits, n * 4},
+      {(void**)&s->hidx, (SK + 1) * 4},  {(void**)&s->key_start, (SK + 1) * 4},
+      {(void**)&s->tile_sum, 65537 * 4}, {(void**)&s->tile_off, 65537 * 4},
+      {(void**)&s->rank, n * 4},         {(void**)&s->cold_pos, (n + 1) * 4},
+      {(void**)&s->sorted, n * 4},       {(void**)&s->rbucket, R * 4},
+      {(void**)&s->round_order, R * 4},  {(void**)&s->bo, n * 4},
+      {(void**)&s->bo2, n * 4},          {(void**)&s->max_count, 4},
   };
   for (auto& a : allocs)
     if ((st = cuda_status(cudaMalloc(a.p, a.bytes), "cudaMalloc")) != CSMV_OK) return fail(st);
@@ -148,6 +167,18 @@ static uint32_t grid_for(const csmv_sched_t* s, uint32_t n) {
 
 #define SCHED_LAUNCH_CHECK(what) CSMV_CUDA(cudaGetLastError())
 
+// Exclusive scan of n counters into out[0..n] (out[n] = total), any n <= 2^28.
+static csmv_status scan_multi(csmv_sched_t* s, const uint32_t* in, uint32_t n, uint32_t* out) {
+  const uint32_t tiles = (n + kScanTile - 1u) / kScanTile;
+  sched_scan_tiles_kernel<<<tiles ? tiles : 1u, 1024, 0, s->stream>>>(in, n, out, s->tile_sum);
+  SCHED_LAUNCH_CHECK("scan tiles");
+  sched_scan_kernel<<<1, 1024, 0, s->stream>>>(s->tile_sum, tiles, s->tile_off);
+  SCHED_LAUNCH_CHECK("scan tile sums");
+  sched_scan_add_kernel<<<grid_for(s, n + 1u), 256, 0, s->stream>>>(out, n, s->tile_off, tiles);
+  SCHED_LAUNCH_CHECK("scan add");
+  return CSMV_OK;
+}
+
 extern "C" csmv_status csmv_sched_probe(csmv_sched_t* s, csmv_bank_t* bank,
                                         const csmv_bank_stream* d, csmv_sched_report* rep) {
   if (!s || !bank) return CSMV_ERR_INVALID_ARG;
@@ -179,6 +210,8 @@ extern "C" csmv_status csmv_sched_probe(csmv_sched_t* s, csmv_bank_t* bank,
   csmv_bank_stream ps = *d;
   ps.n_txn = np;
   ps.txn_aborts = s->aborts;
+  ps.txn_waits = s->waits;
+  ps.backoff = nullptr;
   ps.split_round = 0;
   ps.deferred_warps = 0;
   csmv_stats bst;
@@ -188,7 +221,7 @@ extern "C" csmv_status csmv_sched_probe(csmv_sched_t* s, csmv_bank_t* bank,
   // labels, recent abort rates, training
   CSMV_CUDA(cudaEventRecord(s->ev[0], s->stream));
   sched_labels_kernel<<<grid_for(s, np), 256, 0, s->stream>>>(
-      d->op, d->off, d->addr, np, s->cfg.n_accounts, s->aborts, s->y, s->bin_stats);
+      d->op, d->off, d->addr, np, s->cfg.n_accounts, s->aborts, s->waits, s->y, s->bin_stats);
   SCHED_LAUNCH_CHECK("labels");
   sched_rates_kernel<<<1, kRateBins, 0, s->stream>>>(s->bin_stats, s->rates);
   SCHED_LAUNCH_CHECK("rates");
@@ -242,7 +275,66 @@ extern "C" csmv_status csmv_sched_plan_run(csmv_sched_t* s, csmv_bank_t* bank,
   uint32_t flagged = 0, deferred_rounds = 0;
   const uint32_t* run_op = d->op + t0;
   const uint32_t* run_off = d->off + t0;
-  if (U > 0) {
+  bool with_backoff = false;
+  if (U > 0 && s->cfg.plan == 1) {
+    // grouped plan: hot accounts, keys by the two hottest accounts touched, counting sort,
+    // rounds of 32 consecutive sorted transfers spread by hot account
+    const uint32_t SK = 1u << kSketchLog2;
+    uint32_t hot = s->cfg.hot_count;
+    if (!hot) hot = std::max(2u, (U * 32u) >> 14);
+    const uint64_t seed = s->cfg.seed * 0x9E3779B97F4A7C15ull + s->chunks;
+    sched_hot_flags_kernel<<<grid_for(s, SK), 256, 0, s->stream>>>(s->sketch, hot, s->key_rank);
+    SCHED_LAUNCH_CHECK("hot flags");
+    if ((st = scan_multi(s, s->key_rank, SK, s->hidx)) != CSMV_OK) return st;
+    CSMV_CUDA(cudaMemsetAsync(s->key_count, 0, (size_t)SK * 4, s->stream));
+    CSMV_CUDA(cudaMemsetAsync(s->n_flagged, 0, 4, s->stream));
+    CSMV_CUDA(cudaMemsetAsync(s->max_count, 0, 4, s->stream));
+    if (s->cfg.score == 1) {
+      sched_max_kernel<<<grid_for(s, SK), 256, 0, s->stream>>>(s->sketch, SK, s->max_count);
+      SCHED_LAUNCH_CHECK("max");
+    }
+    sched_group_keys_kernel<<<grid_for(s, n1), 256, 0, s->stream>>>(
+        d->op, d->off, d->addr, t0, n, s->p, s->cfg.threshold, s->cfg.score, s->sketch,
+        s->max_count, hot, s->hidx, s->key, s->rank, s->key_count, s->n_flagged, s->bo,
+        s->cfg.backoff_ns);
+    SCHED_LAUNCH_CHECK("group keys");
+    if ((st = scan_multi(s, s->key_count, SK, s->key_start)) != CSMV_OK) return st;
+    sched_cold_flags_kernel<<<grid_for(s, n1), 256, 0, s->stream>>>(n1, s->key, s->bucket);
+    SCHED_LAUNCH_CHECK("cold flags");
+    if ((st = scan_multi(s, s->bucket, n1, s->cold_pos)) != CSMV_OK) return st;
+    sched_group_scatter_kernel<<<grid_for(s, n1), 256, 0, s->stream>>>(
+        t0, n, s->key, s->rank, s->key_start, s->cold_pos, s->sorted);
+    SCHED_LAUNCH_CHECK("group scatter");
+    CSMV_CUDA(cudaMemsetAsync(s->bucket_count, 0, (size_t)(U + 1) * 4, s->stream));
+    CSMV_CUDA(cudaMemsetAsync(s->bucket_fill, 0, (size_t)(U + 1) * 4, s->stream));
+    sched_round_bucket_kernel<<<grid_for(s, U), 256, 0, s->stream>>>(
+        t0, U, s->sorted, s->key, s->key_start, seed, s->rbucket, s->bucket_count);
+    SCHED_LAUNCH_CHECK("round buckets");
+    if ((st = scan_multi(s, s->bucket_count, U, s->bucket_start)) != CSMV_OK) return st;
+    sched_round_scatter_kernel<<<grid_for(s, U), 256, 0, s->stream>>>(
+        U, s->rbucket, s->bucket_start, s->bucket_fill, s->round_order);
+    SCHED_LAUNCH_CHECK("round scatter");
+    sched_expand_rounds_kernel<<<grid_for(s, U * 32u), 256, 0, s->stream>>>(
+        U, s->round_order, s->sorted, s->order);
+    SCHED_LAUNCH_CHECK("expand");
+    sched_ro_list_kernel<<<grid_for(s, Rp), 256, 0, s->stream>>>(P, Rp, s->ro_flag, s->ro_scan,
+                                                                s->ro_list);
+    SCHED_LAUNCH_CHECK("ro_list");
+    sched_emit_kernel<<<grid_for(s, n1), 256, 0, s->stream>>>(d->op, d->off, Rp, r_ro, Rp,
+                                                             s->ro_list, s->order, s->perm,
+                                                             s->op2, s->off2);
+    SCHED_LAUNCH_CHECK("emit");
+    if (s->cfg.backoff_ns) {
+      sched_plan_backoff_kernel<<<grid_for(s, n1), 256, 0, s->stream>>>(n1, t0, s->perm, s->bo,
+                                                                       s->bo2);
+      SCHED_LAUNCH_CHECK("backoff");
+      with_backoff = true;
+    }
+    CSMV_CUDA(cudaMemcpyAsync(&flagged, s->n_flagged, 4, cudaMemcpyDeviceToHost, s->stream));
+    s->split_round = 0;
+    run_op = s->op2;
+    run_off = s->off2;
+  } else if (U > 0) {
     const size_t SK = (size_t)1 << kSketchLog2;
     CSMV_CUDA(cudaMemsetAsync(s->key_count, 0, SK * 4, s->stream));
     CSMV_CUDA(cudaMemsetAsync(s->key_rank, 0, SK * 4, s->stream));
@@ -290,6 +382,8 @@ extern "C" csmv_status csmv_sched_plan_run(csmv_sched_t* s, csmv_bank_t* bank,
   rs.op = run_op;
   rs.off = run_off;
   rs.txn_aborts = nullptr;
+  rs.txn_waits = nullptr;
+  rs.backoff = with_backoff ? s->bo2 : nullptr;
   rs.split_round = s->split_round;
   rs.deferred_warps = s->split_round ? s->cfg.deferred_warps : 0;
   if (s->cfg.serial_lane && s->split_round) {  // the deferred rounds wait for the serial lane
@@ -328,6 +422,8 @@ extern "C" csmv_status csmv_sched_serial_run(csmv_sched_t* s, csmv_bank_t* bank,
   rs.op = s->op2 + first;
   rs.off = s->off2 + first;
   rs.txn_aborts = nullptr;
+  rs.txn_waits = nullptr;
+  rs.backoff = nullptr;
   rs.split_round = rs.deferred_warps = 0;
   csmv_stats bst;
   csmv_status st = s->cfg.serial_lane == 2 ? csmv_bank_run_flow_device(bank, &rs, &bst)

@@ -103,14 +103,16 @@ __global__ void sched_features_kernel(const uint32_t* op, const uint32_t* off, c
   }
 }
 
-// Labels of the probe slice and the per-bin access / abort counts of its transfers.
+// Labels of the probe slice (1: the transfer aborted or, under group commit, waited for a lock
+// another warp held - a conflict either way) and the per-bin access / conflict counts.
 __global__ void sched_labels_kernel(const uint32_t* op, const uint32_t* off, const uint32_t* addr,
                                     uint32_t n, uint32_t n_accounts, const uint32_t* aborts,
-                                    float* y, unsigned long long* bin_stats) {
+                                    const uint32_t* waits, float* y,
+                                    unsigned long long* bin_stats) {
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const uint32_t o = op[t];
     const bool upd = CSMV_OP_KIND(o) != CSMV_KIND_READONLY;
-    const bool ab = upd && aborts[t] > 0;
+    const bool ab = upd && (aborts[t] > 0 || waits[t] != 0u);
     y[t] = ab ? 1.f : 0.f;
     if (!upd) continue;
     const uint32_t base = off[t];
@@ -248,6 +250,185 @@ __global__ void sched_emit_kernel(const uint32_t* op, const uint32_t* off, uint3
     op2[s] = op[src];
     off2[s] = off[src];
   }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Multi-block exclusive scan of n counters (any n up to 2^28): tiles of 4096 scanned by one CTA
+// each, the tile totals by sched_scan_kernel, then the tile offsets added.
+// ---------------------------------------------------------------------------------------------
+constexpr uint32_t kScanTile = 4096;
+
+__global__ void __launch_bounds__(1024) sched_scan_tiles_kernel(const uint32_t* in, uint32_t n,
+                                                                uint32_t* out, uint32_t* tile_sum) {
+  __shared__ uint32_t part[1024];
+  const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * 4u;
+  uint32_t v[4], s = 0;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    v[i] = base + i < n ? in[base + i] : 0u;
+    s += v[i];
+  }
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (uint32_t d = 1; d < 1024; d <<= 1) {
+    const uint32_t x = threadIdx.x >= d ? part[threadIdx.x - d] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += x;
+    __syncthreads();
+  }
+  uint32_t run = part[threadIdx.x] - s;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    if (base + i < n) out[base + i] = run;
+    run += v[i];
+  }
+  if (threadIdx.x == 1023) tile_sum[blockIdx.x] = part[1023];
+}
+
+// out[i] += tile_off[i / kScanTile]; out[n] = the total
+__global__ void sched_scan_add_kernel(uint32_t* out, uint32_t n, const uint32_t* tile_off,
+                                      uint32_t tiles) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x)
+    out[i] = i < n ? out[i] + tile_off[i / kScanTile] : tile_off[tiles];
+}
+
+// ---------------------------------------------------------------------------------------------
+// Grouped plan: transfers likely to conflict are sorted by the two hottest accounts they touch
+// (read or write), so the 32 transfers of a round share their hot accounts and the engine's
+// group commit locks each hot account once for all of them; the rounds of one hot account are
+// then spread evenly over the plan, so warps queue for many different hot accounts at once.
+//   hot account: sketch count >= hot_count; hot index = its rank among hot sketch slots
+//   key = hidx(h1) << 6 | hidx(h2) mod 63 (63 when the transfer touches one hot account);
+//   transfers not flagged, or touching no hot account (or a hot index >= 65535), take the cold
+//   key (2^22 - 1) and keep stream order among themselves
+// ---------------------------------------------------------------------------------------------
+constexpr uint32_t kGroupKeys = 1u << 22;
+constexpr uint32_t kColdKey = kGroupKeys - 1u;
+constexpr uint32_t kHotNone = 0xFFFFu;
+
+__global__ void sched_hot_flags_kernel(const uint32_t* sketch, uint32_t hot_count, uint32_t* flag) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= kSketchMask; i += gridDim.x * blockDim.x)
+    flag[i] = sketch[i] >= hot_count ? 1u : 0u;
+}
+
+// score: 0 = the network's predicted probability p[t - t0]; 1 = the raw sketch-count score
+// (count of the transfer's most-accessed account / the chunk's largest count, no network).
+// backoff (ns) per transaction: 0 below a score of 1/4, else score x backoff_ns.
+__global__ void sched_group_keys_kernel(const uint32_t* op, const uint32_t* off,
+                                        const uint32_t* addr, uint32_t t0, uint32_t t1,
+                                        const float* p, float threshold, uint32_t score_mode,
+                                        const uint32_t* sketch, const uint32_t* max_count,
+                                        uint32_t hot_count, const uint32_t* hidx, uint32_t* key,
+                                        uint32_t* rank, uint32_t* key_count, uint32_t* n_flagged,
+                                        uint32_t* backoff, uint32_t backoff_ns) {
+  uint32_t flagged = 0;
+  for (uint32_t t = t0 + blockIdx.x * blockDim.x + threadIdx.x; t < t1; t += gridDim.x * blockDim.x) {
+    const uint32_t i = t - t0, o = op[t];
+    if (CSMV_OP_KIND(o) == CSMV_KIND_READONLY) {
+      key[i] = 0xFFFFFFFFu;
+      backoff[i] = 0u;
+      continue;
+    }
+    const uint32_t nr = CSMV_OP_NREADS(o), base = off[t];
+    uint32_t c1 = 0, c2 = 0, x1 = kHotNone, x2 = kHotNone, cmax = 0;
+    for (uint32_t k = 0; k < nr; k++) {
+      const uint32_t sl = sketch_slot(addr[base + k]), c = sketch[sl];
+      cmax = max(cmax, c);
+      if (c < hot_count) continue;
+      const uint32_t h = min(hidx[sl], kHotNone);
+      if (h == x1 || h == x2) continue;  // two accounts hashed to one slot
+      if (c > c1 || (c == c1 && h < x1)) {
+        c2 = c1;
+        x2 = x1;
+        c1 = c;
+        x1 = h;
+      } else if (c > c2 || (c == c2 && h < x2)) {
+        c2 = c;
+        x2 = h;
+      }
+    }
+    const float sc = score_mode ? (float)cmax / (float)max(1u, *max_count) : p[i];
+    const bool hot = sc > threshold && x1 != kHotNone;
+    const uint32_t k = hot ? (x1 << 6) | (x2 == kHotNone ? 63u : x2 % 63u) : kColdKey;
+    key[i] = k;
+    rank[i] = atomicAdd(&key_count[k], 1u);
+    backoff[i] = sc >= 0.25f ? (uint32_t)(fminf(sc, 1.f) * (float)backoff_ns) : 0u;
+    flagged += hot ? 1u : 0u;
+  }
+  if (flagged) atomicAdd(n_flagged, flagged);
+}
+
+__global__ void sched_max_kernel(const uint32_t* in, uint32_t n, uint32_t* out) {
+  uint32_t m = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    m = max(m, in[i]);
+  m = __reduce_max_sync(0xFFFFFFFFu, m);
+  if ((threadIdx.x & 31u) == 0 && m) atomicMax(out, m);
+}
+
+// sorted[key_start[key] + rank] = transaction (transfers of [t0, t1) only); the cold key's
+// transfers keep stream order (their rank is replaced by their position among cold transfers,
+// computed from a scan of cold flags)
+__global__ void sched_group_scatter_kernel(uint32_t t0, uint32_t t1, const uint32_t* key,
+                                           const uint32_t* rank, const uint32_t* key_start,
+                                           const uint32_t* cold_pos, uint32_t* sorted) {
+  for (uint32_t t = t0 + blockIdx.x * blockDim.x + threadIdx.x; t < t1; t += gridDim.x * blockDim.x) {
+    const uint32_t i = t - t0, k = key[i];
+    if (k == 0xFFFFFFFFu) continue;
+    sorted[key_start[k] + (k == kColdKey ? cold_pos[i] : rank[i])] = t;
+  }
+}
+
+__global__ void sched_cold_flags_kernel(uint32_t n, const uint32_t* key, uint32_t* flag) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    flag[i] = key[i] == kColdKey ? 1u : 0u;
+}
+
+// Position bucket of every transfer round of the sorted list: the j-th of the n rounds that start
+// within one hot account's keys goes to (j + u) / n of the plan (u a hash of the account in
+// [0, 1)), a cold round to a hash of its index.
+__global__ void sched_round_bucket_kernel(uint32_t t0, uint32_t U, const uint32_t* sorted,
+                                          const uint32_t* key, const uint32_t* key_start,
+                                          uint64_t seed, uint32_t* rbucket, uint32_t* bcount) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < U; j += gridDim.x * blockDim.x) {
+    const uint32_t k = key[sorted[32u * j] - t0], h1 = k >> 6;
+    float pos;
+    if (k == kColdKey || h1 >= kHotNone) {
+      pos = unit_hash(seed, j);
+    } else {
+      const uint32_t S = key_start[h1 << 6], E = key_start[(h1 + 1u) << 6];
+      const uint32_t first = (S + 31u) / 32u, last = (E - 1u) / 32u;  // rounds starting in [S, E)
+      const uint32_t n = last >= first ? last - first + 1u : 1u;
+      const uint32_t idx = j >= first ? j - first : 0u;
+      pos = ((float)min(idx, n - 1u) + unit_hash(seed ^ 0xA5A5A5A5ull, h1)) / (float)n;
+    }
+    const uint32_t b = min((uint32_t)(pos * (float)U), U - 1u);
+    rbucket[j] = b;
+    atomicAdd(&bcount[b], 1u);
+  }
+}
+
+__global__ void sched_round_scatter_kernel(uint32_t U, const uint32_t* rbucket,
+                                           const uint32_t* bstart, uint32_t* bfill,
+                                           uint32_t* round_order) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < U; j += gridDim.x * blockDim.x) {
+    const uint32_t b = rbucket[j];
+    round_order[bstart[b] + atomicAdd(&bfill[b], 1u)] = j;
+  }
+}
+
+// order[32 i + lane] = sorted[32 round_order[i] + lane]
+__global__ void sched_expand_rounds_kernel(uint32_t U, const uint32_t* round_order,
+                                           const uint32_t* sorted, uint32_t* order) {
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < U * 32u; s += gridDim.x * blockDim.x)
+    order[s] = sorted[32u * round_order[s / 32u] + (s & 31u)];
+}
+
+// backoff of the planned stream: bo2[s] = backoff of the transaction at planned slot s
+__global__ void sched_plan_backoff_kernel(uint32_t n, uint32_t t0, const uint32_t* perm,
+                                          const uint32_t* bo, uint32_t* bo2) {
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+    bo2[s] = bo[perm[s] - t0];
 }
 
 }  // namespace csmv

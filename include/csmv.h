@@ -23,7 +23,9 @@
 extern "C" {
 #endif
 
-#define CSMV_ABI_VERSION 2 /* 2: csmv_bank_config.flow_warps, CSMV_ERR_IO, lanes and trace files */
+#define CSMV_ABI_VERSION 3 /* 2: csmv_bank_config.flow_warps, CSMV_ERR_IO, lanes and trace files;
+                              3: group commit (prevalidate 3), csmv_bank_stream.backoff,
+                              csmv_bank_read_groups, scheduler grouping and backoff fields */
 
 typedef enum csmv_status {
   CSMV_OK = 0,
@@ -86,6 +88,14 @@ typedef struct csmv_bank_stream {
                               likely-conflicting transactions); they serve the main queue
                               [0, split_round) once it is empty                              */
   uint32_t deferred_warps;
+  const uint32_t* backoff; /* optional [n_txn] (same memory kind as op): before a round retries,
+                              its warp pauses a random time below the largest backoff[i] (ns)
+                              of its uncommitted transactions (a scheduler's backoff; the
+                              reference retries at once, bank/csmv_sh/exe.cu:142-269)      */
+  uint32_t* txn_waits;     /* optional out [n_txn] (same memory kind as op): 1 when the
+                              transaction's commit group found one of its write locks held by
+                              another warp and waited for it (group commit), else 0 - a
+                              conflict the engine resolved by waiting instead of aborting   */
 } csmv_bank_stream;
 
 /* Account-choice distributions for the workload generator. */
@@ -156,7 +166,16 @@ typedef struct csmv_bank_config {
   uint32_t validate;           /* CSMV_VALIDATE_*                                             */
   uint32_t writeback;          /* CSMV_WRITEBACK_*                                            */
   uint32_t batch;              /* CSMV_BATCH_*                                                */
-  uint32_t prevalidate;        /* 1 = intra-warp pre-validation (batchedAtrInsert)             */
+  uint32_t prevalidate;        /* 0 = none; 1 = intra-warp pre-validation (batchedAtrInsert,
+                                  API.cu:94-191); 2 = intra-warp chaining (stamp protocol);
+                                  3 = group commit (stamp protocol): a warp's round locks every
+                                  account it may write once, waiting in descending account
+                                  order, reads them under the locks, draws the round's
+                                  timestamps from its server, validates every read of an
+                                  account it does not lock, runs the transfers that pass as a
+                                  chain in lane order and installs ONE version per account
+                                  (the last writer's); the clock passes a group's timestamps
+                                  at once, so no snapshot sees its intermediate states        */
   uint32_t log_commits;        /* 1 = keep the per-ts commit log and per-txn outcomes         */
   uint32_t max_txn;            /* largest stream a run may carry (sizes the logs)             */
   uint32_t spin_limit_log2;    /* bounded waits give up after 2^this polls (default 24)       */
@@ -262,6 +281,13 @@ csmv_status csmv_bank_read_versions(csmv_bank_t* h, uint64_t* host_slots);
  * host_result[i] = read-only sum (0 otherwise). Any pointer may be NULL. */
 csmv_status csmv_bank_read_log(csmv_bank_t* h, uint32_t* host_log_txn, uint32_t n_log,
                                uint32_t* host_outcome, int32_t* host_result, uint32_t n_txn);
+
+/* Commit groups of the last run (needs log_commits): bit k of host_bits (word k / 32, bit k % 32)
+ * is set when timestamp base + k + 1 ends a commit group - the timestamps of one group commit
+ * (prevalidate 3), whose writes installed one version per account. Runs of other modes and
+ * lanes install every write, and every timestamp ends its own group (all bits set). n_log as
+ * csmv_bank_read_log; host_bits holds (n_log + 31) / 32 words. */
+csmv_status csmv_bank_read_groups(csmv_bank_t* h, uint32_t* host_bits, uint32_t n_log);
 
 /* SM count, CTAs and threads per CTA of the commit kernel, and device bytes the handle holds. */
 csmv_status csmv_bank_device_info(csmv_bank_t* h, int* n_sms, int* ctas, int* threads_per_cta,
@@ -463,12 +489,13 @@ csmv_status csmv_mlp_adam_step(csmv_mlp_t* m, float lr);
 void csmv_mlp_destroy(csmv_mlp_t* m);
 
 /* ------------------------------------------------------------------------------------------
- * Learned conflict scheduler (no counterpart in the reference). It reorders a chunk of a bank
- * stream before the unchanged commit engine runs it - every transaction is still validated by
- * the engine, so results stay exact - to keep transfers that are likely to conflict apart:
+ * Learned conflict scheduler (no counterpart in the reference). It reorders and groups a chunk
+ * of a bank stream before the unchanged commit engine runs it - every transaction is still
+ * validated by the engine, so results stay exact:
  *  1. probe: the first probe_rounds_pct % of the chunk's rounds run in stream order, with
- *     per-transaction abort counts; their transfers label the network's training data
- *     (aborted or not) and refresh per-range abort rates; train_steps Adam steps follow;
+ *     per-transaction abort counts and lock waits; their transfers label the network's
+ *     training data (aborted or waited for a lock: a conflict) and refresh per-range abort
+ *     rates; train_steps Adam steps follow;
  *  2. plan: the network scores the remaining transfers from 64 features (hashed access counts
  *     of the accounts in the chunk, recent abort rates of their ranges); a transfer scoring
  *     above threshold is keyed by its more frequent written account, and the k-th of c
@@ -492,6 +519,20 @@ typedef struct csmv_sched_config {
                                  2 on the dataflow lane (csmv_bank_run_flow_device)           */
   uint64_t seed;
   int32_t device;
+  uint32_t plan;              /* 0 = spread flagged transfers by key (above); 1 = group them:
+                                 flagged transfers are sorted by the two hottest accounts they
+                                 touch (sketch count >= hot_count), so a round's 32 transfers
+                                 share their hot accounts and the engine's group commit
+                                 (prevalidate 3) locks each once for all of them; each hot
+                                 account's rounds are spread evenly over the plan, the other
+                                 transfers keep stream order in rounds of their own            */
+  uint32_t hot_count;         /* plan 1: accesses in the chunk that make an account hot
+                                 (0 = the chunk's transfers / 16384, at least 2)               */
+  uint32_t score;             /* 0 = the network's predicted probability flags transfers;
+                                 1 = the raw sketch-count score (the transfer's largest access
+                                 count / the chunk's largest), no network - the ablation      */
+  uint32_t backoff_ns;        /* per-transaction retry backoff: score x backoff_ns for scores
+                                 >= 1/4, else 0 (0 = no backoff array)                          */
 } csmv_sched_config;
 
 typedef struct csmv_sched_report {

@@ -150,18 +150,26 @@ __device__ __forceinline__ bool read_stamped(const unsigned long long* item, uin
   return found;
 }
 
+// Latest committed version of an item and its stamp (the read of TXReadLatest without the read
+// set). Returns false when the stamp's version could not be found.
+template <int DEPTH>
+__device__ __forceinline__ bool read_latest(const VersionStore& vs,
+                                            const unsigned long long* commit_words, uint32_t addr,
+                                            uint32_t& stamp, int32_t& v) {
+  const unsigned long long* item = vs.slots + (size_t)addr * DEPTH;
+  stamp = (uint32_t)ld_relaxed_gpu(commit_words + addr);
+  if (read_stamped<DEPTH>(item, stamp, v)) return true;
+  stamp = (uint32_t)ld_acquire_gpu(commit_words + addr);
+  return read_stamped<DEPTH>(item, stamp, v);
+}
+
 template <int DEPTH, int MAXR>
 __device__ __forceinline__ int32_t TXReadLatest(const VersionStore& vs,
                                                 const unsigned long long* commit_words,
                                                 uint32_t addr, ReadSet<MAXR>& rs,
                                                 uint32_t& stamp, bool* isAborted) {
-  const unsigned long long* item = vs.slots + (size_t)addr * DEPTH;
   int32_t v = 0;
-  stamp = (uint32_t)ld_relaxed_gpu(commit_words + addr);
-  if (!read_stamped<DEPTH>(item, stamp, v)) {
-    stamp = (uint32_t)ld_acquire_gpu(commit_words + addr);
-    if (!read_stamped<DEPTH>(item, stamp, v)) *isAborted = true;
-  }
+  if (!read_latest<DEPTH>(vs, commit_words, addr, stamp, v)) *isAborted = true;
 #pragma unroll
   for (int i = 0; i < MAXR; i++)
     if (i == (int)rs.n) rs.addr[i] = addr;

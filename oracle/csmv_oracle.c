@@ -465,13 +465,41 @@ int orc_bank_check(uint32_t n_txn, const uint32_t* op, const uint32_t* off, cons
                    uint32_t n_accounts, const int32_t* init, int depth, uint32_t final_ts,
                    const uint32_t* log_txn, const uint32_t* outcome, const int32_t* result,
                    const uint64_t* final_slots, char* msg, int msg_len) {
-  int rc = 0;
+  return orc_bank_check_groups(n_txn, op, off, addr, n_accounts, init, depth, final_ts, log_txn,
+                               outcome, result, NULL, final_slots, msg, msg_len);
+}
+
+#define GROUP_END(g, ts) (!(g) || (((g)[((ts)-1u) >> 5] >> (((ts)-1u) & 31u)) & 1u))
+#define ORC_GROUP_MAX 4096
+
+/* Installs of one commit group: each account's last write of the group, as one version. The
+ * engine's group commit installs exactly these (the versions in between are never visible). */
+static void flush_group(uint64_t* slots, int depth, uint32_t* ga, uint32_t* gts, int32_t* gv,
+                        int* gn) {
+  for (int i = *gn - 1; i >= 0; i--) {
+    int later = 0;
+    for (int j = i + 1; j < *gn && !later; j++) later = ga[j] == ga[i];
+    if (!later) orc_packed_writeback(slots + (uint64_t)ga[i] * depth, depth, gts[i], gv[i]);
+  }
+  *gn = 0;
+}
+
+int orc_bank_check_groups(uint32_t n_txn, const uint32_t* op, const uint32_t* off,
+                          const uint32_t* addr, uint32_t n_accounts, const int32_t* init,
+                          int depth, uint32_t final_ts, const uint32_t* log_txn,
+                          const uint32_t* outcome, const int32_t* result,
+                          const uint32_t* group_end, const uint64_t* final_slots, char* msg,
+                          int msg_len) {
+  int rc = 0, gn = 0;
   uint8_t* seen = calloc(n_txn ? n_txn : 1, 1);
   int32_t* vals = malloc(sizeof(int32_t) * (n_accounts ? n_accounts : 1));
   uint64_t* slots = malloc(sizeof(uint64_t) * (size_t)n_accounts * depth + 8);
   uint32_t* bucket_head = malloc(sizeof(uint32_t) * ((size_t)final_ts + 1));
   uint32_t* next = malloc(sizeof(uint32_t) * (n_txn ? n_txn : 1));
-  if (!seen || !vals || !slots || !bucket_head || !next) {
+  uint32_t* ga = malloc(sizeof(uint32_t) * ORC_GROUP_MAX);
+  uint32_t* gts = malloc(sizeof(uint32_t) * ORC_GROUP_MAX);
+  int32_t* gv = malloc(sizeof(int32_t) * ORC_GROUP_MAX);
+  if (!seen || !vals || !slots || !bucket_head || !next || !ga || !gts || !gv) {
     rc = fail(msg, msg_len, "oracle out of memory");
     goto out;
   }
@@ -529,11 +557,29 @@ int orc_bank_check(uint32_t n_txn, const uint32_t* op, const uint32_t* off, cons
       int nw = orc_bank_exec(op[t], addr + off[t], v, wa, wv, &r);
       for (int k = 0; k < nw; k++) {
         vals[wa[k]] = wv[k];
-        orc_packed_writeback(slots + (uint64_t)wa[k] * depth, depth, ts, wv[k]);
+        if (gn == ORC_GROUP_MAX) {
+          rc = fail(msg, msg_len, "ts %u: commit group holds more than %d writes", ts,
+                    ORC_GROUP_MAX);
+          goto out;
+        }
+        ga[gn] = wa[k];
+        gts[gn] = ts;
+        gv[gn] = wv[k];
+        gn++;
       }
+    }
+    if (ts > 0 && GROUP_END(group_end, ts)) flush_group(slots, depth, ga, gts, gv, &gn);
+    if (ts > 0 && !GROUP_END(group_end, ts) && bucket_head[ts] != 0xFFFFFFFFu) {
+      rc = fail(msg, msg_len, "txn %u: snapshot %u falls inside a commit group", bucket_head[ts],
+                ts);
+      goto out;
     }
     for (uint32_t t = bucket_head[ts]; t != 0xFFFFFFFFu; t = next[t])
       if ((rc = check_snapshot_txn(t, op, off, addr, vals, result, msg, msg_len))) goto out;
+  }
+  if (gn) {
+    rc = fail(msg, msg_len, "the last commit group does not end at the final ts %u", final_ts);
+    goto out;
   }
   /* 3. invariant and final version state */
   {
@@ -565,6 +611,9 @@ out:
   free(slots);
   free(bucket_head);
   free(next);
+  free(ga);
+  free(gts);
+  free(gv);
   return rc;
 }
 
@@ -609,6 +658,52 @@ int orc_bank_sim_1warp(uint32_t n_txn, const uint32_t* op, const uint32_t* off,
     while (pending) {
       st->rounds++;
       uint32_t snap = clock, cand = 0;
+      if (prevalidate == 3 && (op[g * 32] & 3u) != 0) {
+        /* group commit: with one warp every lock is free and every read current, so the round's
+         * pending transfers take consecutive timestamps in lane order and run as a chain; each
+         * written account gets one version, its last writer's */
+        uint32_t ga[64], gts[64];
+        int32_t gv[64];
+        int gn = 0;
+        for (int l = 0; l < 32; l++) {
+          if (!((pending >> l) & 1)) continue;
+          uint32_t t = g * 32 + l, nr = (op[t] >> 2) & 63;
+          int32_t v[64], r = 0, wv2[2];
+          uint32_t wa2[2];
+          for (uint32_t k = 0; k < nr; k++) {
+            uint32_t x = addr[off[t] + k];
+            int found = -1;
+            for (int j = gn - 1; j >= 0; j--)
+              if (ga[j] == x) {
+                found = j;
+                break;
+              }
+            if (found >= 0) {
+              v[k] = gv[found];
+            } else if (orc_packed_read(slots + (uint64_t)x * depth, depth, 0xFFFFFFFEu, &v[k])) {
+              return 1;
+            }
+          }
+          uint32_t ts = ++clock;
+          int nw = orc_bank_exec(op[t], addr + off[t], v, wa2, wv2, &r);
+          for (int k = 0; k < nw; k++) {
+            ga[gn] = wa2[k];
+            gts[gn] = ts;
+            gv[gn] = wv2[k];
+            gn++;
+          }
+          log_txn[ts - 1] = t;
+          outcome[t] = ts;
+          result[t] = 0;
+          if (nw > 0)
+            st->commits_update++;
+          else
+            st->commits_nowrite++;
+        }
+        flush_group(slots, depth, ga, gts, gv, &gn);
+        pending = 0;
+        continue;
+      }
       if (prevalidate == 2) { /* intra-warp chaining: the round runs serially in lane order */
         int32_t* round_val = (int32_t*)malloc(sizeof(int32_t) * 32 * 64);
         uint32_t round_addr[32 * 2];

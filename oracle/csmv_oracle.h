@@ -19,6 +19,8 @@
  *   - orc_memcd_serial      serial GET/SET semantics of the cache, memcdSH.cu:343-440
  *   - orc_memcd_check       replay of a cache batch's commit log (exactness oracle)
  *   - orc_bank_check        serial replay of a commit log in commit-ts order (exactness oracle)
+ *   - orc_bank_check_groups the same for group commits (one installed version per account and
+ *                           group, no snapshot inside a group)
  *   - orc_bank_sim_1warp    deterministic model of one client warp + one server
  *   - orc_bank_serial / orc_bank_locked   CPU baselines (single thread / striped locks)
  *
@@ -134,6 +136,16 @@ int orc_bank_check(uint32_t n_txn, const uint32_t* op, const uint32_t* off, cons
                    uint32_t n_accounts, const int32_t* init, int depth, uint32_t final_ts,
                    const uint32_t* log_txn, const uint32_t* outcome, const int32_t* result,
                    const uint64_t* final_slots, char* msg, int msg_len);
+
+/* The same with commit groups: group_end is a bitmap over timestamps 1..final_ts (bit ts-1 set
+ * when ts ends a group; NULL = every timestamp ends its own). A group's writes install one
+ * version per account - its last write - and no snapshot may fall inside a group. */
+int orc_bank_check_groups(uint32_t n_txn, const uint32_t* op, const uint32_t* off,
+                          const uint32_t* addr, uint32_t n_accounts, const int32_t* init,
+                          int depth, uint32_t final_ts, const uint32_t* log_txn,
+                          const uint32_t* outcome, const int32_t* result,
+                          const uint32_t* group_end, const uint64_t* final_slots, char* msg,
+                          int msg_len);
 
 /* Deterministic model of the GB300 engine with one client warp and one server. */
 typedef struct orc_sim_stats {

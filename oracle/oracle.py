@@ -79,6 +79,7 @@ def lib() -> C.CDLL:
             "orc_memcd_set_slot": (I, [P, P, P, I, C.c_int32]),
             "orc_bank_exec": (I, [U, P, P, P, P, P]),
             "orc_bank_check": (I, [U, P, P, P, U, P, I, U, P, P, P, P, C.c_char_p, I]),
+            "orc_bank_check_groups": (I, [U, P, P, P, U, P, I, U, P, P, P, P, P, C.c_char_p, I]),
             "orc_bank_sim_1warp": (I, [U, P, P, P, U, P, I, I, I, P, P, P, P, P]),
             "orc_bank_serial": (I, [U, P, P, P, U, P, P]),
             "orc_bank_locked": (I, [U, P, P, P, U, P, I, P]),
@@ -134,17 +135,19 @@ def generate(w: Workload):
 
 
 def check(op, off, addr, n_accounts, init, depth, final_ts, log_txn, outcome, result,
-          final_slots=None) -> str | None:
-    """Serial replay in commit-ts order; None when the run is exact, else the first violation."""
+          final_slots=None, groups=None) -> str | None:
+    """Serial replay in commit-ts order; None when the run is exact, else the first violation.
+    groups: bitmap (uint32 words) of the timestamps that end a commit group (None: every one)."""
     msg = C.create_string_buffer(512)
     init = np.ascontiguousarray(init, np.int32)
     log_txn = np.ascontiguousarray(log_txn, np.uint32)
     if log_txn.size == 0:
         log_txn = np.zeros(1, np.uint32)
-    rc = lib().orc_bank_check(
+    g = np.ascontiguousarray(groups, np.uint32) if groups is not None else None
+    rc = lib().orc_bank_check_groups(
         C.c_uint32(len(op)), p(op), p(off), p(addr), C.c_uint32(n_accounts), p(init),
         C.c_int(depth), C.c_uint32(final_ts), p(log_txn), p(np.ascontiguousarray(outcome, np.uint32)),
-        p(np.ascontiguousarray(result, np.int32)),
+        p(np.ascontiguousarray(result, np.int32)), p(g) if g is not None else None,
         p(np.ascontiguousarray(final_slots, np.uint64)) if final_slots is not None else None,
         msg, 512)
     return None if rc == 0 else msg.value.decode()

@@ -27,6 +27,7 @@ def run_checked(w, *, init_value=1000, check=True, stream=None, txn_aborts=None,
         st = bank.run(s, txn_aborts=txn_aborts, split_round=split_round,
                       deferred_warps=deferred_warps)
         log_txn, outcome, result = bank.log(w.n_txn, st.final_ts)
+        groups = bank.groups(st.final_ts)
         slots = bank.versions()
     assert st.error == 0
     assert st.commits == w.n_txn, (st.commits, w.n_txn)
@@ -40,7 +41,7 @@ def run_checked(w, *, init_value=1000, check=True, stream=None, txn_aborts=None,
     if check:
         init = np.full(w.n_accounts, init_value, np.int32)
         err = orc.check(s.op, s.off, s.addr, w.n_accounts, init, depth, st.final_ts, log_txn,
-                        outcome, result, slots)
+                        outcome, result, slots, groups=groups)
         assert err is None, err
     return st, s, (log_txn, outcome, result, slots)
 
@@ -83,6 +84,24 @@ def to_device(torch, s):
     d = [torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).cuda() for a in (s.op, s.off, s.addr)]
     return cg.BankStream(s.n_txn, d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(),
                          int(s.addr.shape[0])), d
+
+
+def concat_groups(parts):
+    """Group-end bitmaps of consecutive runs joined into one over the runs' timestamps:
+    parts = [(bitmap words, timestamps the run used), ...]."""
+    bits = [np.unpackbits(np.ascontiguousarray(w, np.uint32).view(np.uint8),
+                          bitorder="little")[:n] for w, n in parts]
+    allb = np.concatenate(bits) if bits else np.zeros(0, np.uint8)
+    pad = np.zeros((-len(allb)) % 32, np.uint8)
+    return np.packbits(np.concatenate([allb, pad]), bitorder="little").view(np.uint32)
+
+
+def zipf_bank_workload(n_txn, seed=2026):
+    """The contended bank: 2^20 accounts at 1000, Zipf(0.99) account choice, transfers reading 4
+    and writing 2 accounts (skipped when funds are short), 20 % read-only rounds summing 32."""
+    return cg.bank_workload(1 << 20, n_txn, seed=seed, pr_read_pct=20, ro_reads=32, up_reads=4,
+                            kind=cg.KIND_TRANSFER, amt_lo=1, amt_hi=10, dist=cg.DIST_ZIPF,
+                            zipf_theta=0.99)
 
 
 def sub_stream(s, lo, hi):

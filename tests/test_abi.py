@@ -34,7 +34,7 @@ def test_every_declared_symbol_is_exported():
 
 def test_library_loads_and_reports_version():
     L = cg.lib()
-    assert L.csmv_abi_version() == 2
+    assert L.csmv_abi_version() == 3
     assert L.csmv_status_str(4) == b"bounded device wait timed out"
 
 
@@ -43,7 +43,8 @@ def test_config_validation_is_a_status():
                 dict(client_warps=16), dict(validate=1, batch=0, writeback=0), dict(max_txn=33),
                 dict(spin_limit_log2=2), dict(n_accounts=1), dict(batch=9),
                 dict(batch=3, validate=1, writeback=1), dict(batch=3, cluster_size=3),
-                dict(batch=3, cluster_size=4, client_warps=15), dict(flow_warps=17)):
+                dict(batch=3, cluster_size=4, client_warps=15), dict(flow_warps=17),
+                dict(prevalidate=4), dict(prevalidate=3, validate=1, batch=1)):
         with pytest.raises(cg.CsmvError) as e:
             cg.Bank(cg.bank_config(**bad))
         assert e.value.status == 1, bad

@@ -17,11 +17,11 @@ from gpu_util import c1_workload, defer_plan, run_checked, sub_stream, to_device
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("prevalidate", [1, 0, 2])
+@pytest.mark.parametrize("prevalidate", [1, 0, 2, 3])
 @pytest.mark.parametrize("validate", [cg.VALIDATE_STAMP, cg.VALIDATE_RING, cg.VALIDATE_RING_LANE])
 def test_one_client_warp_equals_oracle_model(prevalidate, validate):
-    if prevalidate == 2 and validate != cg.VALIDATE_STAMP:
-        pytest.skip("intra-warp chaining is a stamp-protocol mode")
+    if prevalidate >= 2 and validate != cg.VALIDATE_STAMP:
+        pytest.skip("intra-warp chaining and group commit are stamp-protocol modes")
     w = c1_workload(n_txn=32 * 96, n_accounts=40, pr_read_pct=20, up_reads=3, seed=11)
     st, s, (log_txn, outcome, result, slots) = run_checked(
         w, ctas=1, client_warps=1, prevalidate=prevalidate, validate=validate, batch=cg.BATCH_WARP,
@@ -51,6 +51,10 @@ VARIANTS = {
     "stamp-cta-noprevalid": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CTA, prevalidate=0),
     "stamp-cta-chain": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CTA, prevalidate=2),
     "stamp-cluster2": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CLUSTER, cluster_size=2),
+    "stamp-cta-group": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CTA, prevalidate=3),
+    "stamp-warp-group": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_WARP, prevalidate=3),
+    "stamp-cluster2-group": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CLUSTER,
+                                 cluster_size=2, prevalidate=3),
     "stamp-cluster8": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CLUSTER, cluster_size=8),
 }
 
@@ -63,7 +67,7 @@ def test_c1_plain_bank_exact(variant):
 
 
 @pytest.mark.parametrize("validate,prevalidate", [(cg.VALIDATE_STAMP, 1), (cg.VALIDATE_STAMP, 2),
-                                                  (cg.VALIDATE_RING, 1)])
+                                                  (cg.VALIDATE_STAMP, 3), (cg.VALIDATE_RING, 1)])
 @pytest.mark.parametrize("depth", [2, 4, 16])
 def test_high_contention_exact(depth, validate, prevalidate):
     """16 accounts, 32 client warps: most attempts conflict; the ring form runs with a 64-record
@@ -71,7 +75,8 @@ def test_high_contention_exact(depth, validate, prevalidate):
     w = c1_workload(n_txn=32 * 600, n_accounts=16, pr_read_pct=30, ro_reads=8, up_reads=3, seed=3)
     st, _, _ = run_checked(w, ctas=4, client_warps=8, version_depth=depth, ring_size=64,
                            validate=validate, prevalidate=prevalidate)
-    assert st.aborts > 0
+    if prevalidate != 3:  # group commit waits for write locks instead of aborting on them
+        assert st.aborts > 0
 
 
 def test_two_accounts_extreme():
@@ -83,20 +88,22 @@ def test_single_round():
     run_checked(c1_workload(n_txn=32, n_accounts=100), ctas=1, client_warps=1)
 
 
-@pytest.mark.parametrize("prevalidate", [2, 1])
+@pytest.mark.parametrize("prevalidate", [3, 2, 1])
 def test_zipf_contended_exact(prevalidate):
     """1M accounts, Zipf 0.99, read 4 / write 2, 20% read-only scans of 32, one CTA per SM."""
     w = cg.bank_workload(1 << 20, 1 << 16, seed=9, pr_read_pct=20, ro_reads=32, up_reads=4,
                          kind=cg.KIND_TRANSFER, amt_lo=1, amt_hi=10, dist=cg.DIST_ZIPF,
                          zipf_theta=0.99)
     st, _, _ = run_checked(w, ctas=152, client_warps=2, version_depth=8, prevalidate=prevalidate)
-    assert st.aborts > 0
+    if prevalidate != 3:  # group commit waits for write locks instead of aborting on them
+        assert st.aborts > 0
 
 
-def test_hotspot_full_gpu_exact():
+@pytest.mark.parametrize("prevalidate", [2, 3])
+def test_hotspot_full_gpu_exact(prevalidate):
     w = cg.bank_workload(1 << 20, 1 << 18, seed=4, pr_read_pct=10, ro_reads=8, up_reads=4,
                          dist=cg.DIST_HOTSPOT, hot_frac=0.01, hot_prob=0.9, shift_every=1 << 16)
-    run_checked(w, ctas=0, client_warps=15, prevalidate=2)
+    run_checked(w, ctas=0, client_warps=15, prevalidate=prevalidate)
 
 
 def test_runs_continue_the_commit_order():

@@ -7,7 +7,7 @@ import pytest
 
 import csmv_gb300 as cg
 import oracle as orc
-from gpu_util import c1_workload, to_device
+from gpu_util import c1_workload, concat_groups, to_device, zipf_bank_workload
 
 pytestmark = pytest.mark.gpu
 HOLE = 0xFFFFFFFF
@@ -23,7 +23,7 @@ def test_scheduled_chunk_is_a_permutation_and_replays_exactly(threshold, defer):
     ds, keep = to_device(torch, s)
     with cg.Bank(n_accounts=n_acc, max_txn=n, ctas=16, client_warps=4) as bank, \
             cg.Scheduler(n_accounts=n_acc, max_txn=n, threshold=threshold, defer_threshold=defer,
-                         deferred_warps=8, train_steps=3) as sched:
+                         deferred_warps=8, train_steps=3, plan=0) as sched:
         bank.load()
         r1 = sched.probe(bank, ds)
         f1 = r1.probe.final_ts
@@ -72,7 +72,8 @@ def test_trained_scheduler_lowers_abort_rate_on_shifting_hotspot():
         with cg.Bank(n_accounts=n_acc, max_txn=chunk, ctas=152, client_warps=2, version_depth=8,
                      log_commits=0) as bank:
             bank.load()
-            sched = cg.Scheduler(n_accounts=n_acc, max_txn=chunk) if arm == "learned" else None
+            sched = cg.Scheduler(n_accounts=n_acc, max_txn=chunk, plan=0) \
+                if arm == "learned" else None
             for lo, hi in bounds:
                 c = cg.Stream(np.ascontiguousarray(s.op[lo:hi]), np.ascontiguousarray(s.off[lo:hi]),
                               s.addr)
@@ -108,7 +109,7 @@ def test_serial_lane_plan_replays_exactly(lane):
     ds, keep = to_device(torch, s)
     with cg.Bank(n_accounts=n_acc, max_txn=n, ctas=16, client_warps=4) as bank, \
             cg.Scheduler(n_accounts=n_acc, max_txn=n, threshold=0.0, defer_threshold=0.0,
-                         serial_lane=lane, train_steps=2) as sched:
+                         serial_lane=lane, train_steps=2, plan=0) as sched:
         bank.load()
         r1 = sched.probe(bank, ds)
         f1, np_ = r1.probe.final_ts, r1.n_probe
@@ -131,3 +132,78 @@ def test_serial_lane_plan_replays_exactly(lane):
                     np.concatenate([out1, out2[:n2], out3]).astype(np.uint32),
                     np.concatenate([res1, res2[:n2], res3]).astype(np.int32), slots)
     assert err is None, err
+
+
+def _scheduled_chunk_checked(bank, sched, s, ds, n, n_acc, depth):
+    """Probe and planned runs of one chunk, replayed together with their commit groups."""
+    r1 = sched.probe(bank, ds)
+    f1, np_ = r1.probe.final_ts, r1.n_probe
+    log1, out1, res1 = bank.log(np_, f1)
+    g1 = bank.groups(f1)
+    r2 = sched.plan_run(bank, ds)
+    f2 = r2.planned.final_ts
+    perm, _, split = sched.plan(n)
+    log2, out2, res2 = bank.log(n - np_, f2 - f1)
+    g2 = bank.groups(f2 - f1)
+    slots = bank.versions()
+    assert split == 0 and sorted(perm.tolist()) == list(range(np_, n))
+    kinds = (s.op[perm] & 3).reshape(-1, 32)
+    assert ((kinds == 0) == (kinds[:, :1] == 0)).all()  # rounds stay uniform in kind
+    op_c = np.concatenate([s.op[:np_], s.op[perm]])
+    off_c = np.concatenate([s.off[:np_], s.off[perm]])
+    log_c = np.concatenate([log1, np.where(log2 != HOLE, log2 + np_, HOLE)]).astype(np.uint32)
+    err = orc.check(op_c, off_c, s.addr, n_acc, np.full(n_acc, 1000, np.int32), depth, f2, log_c,
+                    np.concatenate([out1, out2]), np.concatenate([res1, res2]), slots,
+                    groups=concat_groups([(g1, f1), (g2, f2 - f1)]))
+    assert err is None, err
+    assert r1.probe.commits + r2.planned.commits == n
+    return r1, r2
+
+
+@pytest.mark.parametrize("score", [0, 1])
+def test_grouped_plan_replays_exactly(score):
+    """Grouped plan (plan 1) in front of group commit on a small contended bank, with the network
+    (score 0) or the raw sketch-count score (score 1) flagging transfers."""
+    torch = pytest.importorskip("torch")
+    n_acc, n = 1 << 14, 1 << 15
+    w = c1_workload(n_txn=n, n_accounts=n_acc, dist=cg.DIST_ZIPF, zipf_theta=0.99, seed=10,
+                    up_reads=4, pr_read_pct=20)
+    s = cg.generate(w)
+    ds, keep = to_device(torch, s)
+    with cg.Bank(n_accounts=n_acc, max_txn=n, ctas=16, client_warps=4, prevalidate=3) as bank, \
+            cg.Scheduler(n_accounts=n_acc, max_txn=n, plan=1, score=score, threshold=0.05,
+                         train_steps=2) as sched:
+        bank.load()
+        r1, r2 = _scheduled_chunk_checked(bank, sched, s, ds, n, n_acc, 4)
+    assert r2.n_flagged > 0
+
+
+def test_grouped_plan_at_the_bench_shape_replays_exactly():
+    """The benchmark's configuration, checked end to end: one 2^20-transaction Zipf(0.99) batch
+    on 2^20 accounts (read 4 / write 2, 20 % read-only scans of 32), 152 CTAs of two client warps,
+    8 versions per account, group commit. The scheduler probes 2 % of the rounds in stream order,
+    trains, and runs its grouped plan; the engine locks, timestamps and validates every
+    transaction. Probe and planned runs replay exactly together (groups included), the plain
+    engine's run of the same batch does too, and the lock waits it reports label conflicts."""
+    torch = pytest.importorskip("torch")
+    n_acc, n, depth = 1 << 20, 1 << 20, 8
+    s = cg.generate(zipf_bank_workload(n))
+    ds, keep = to_device(torch, s)
+    cfg = dict(n_accounts=n_acc, max_txn=n, ctas=152, client_warps=2, version_depth=depth,
+               prevalidate=3)
+    with cg.Bank(**cfg) as bank, \
+            cg.Scheduler(n_accounts=n_acc, max_txn=n, plan=1, probe_rounds_pct=2) as sched:
+        bank.load()
+        r1, r2 = _scheduled_chunk_checked(bank, sched, s, ds, n, n_acc, depth)
+    assert r2.n_flagged > 0 and r2.planned.error == 0
+    waits = np.zeros(n, np.uint32)
+    with cg.Bank(**cfg) as bank:
+        bank.load()
+        st = bank.run(s, txn_waits=waits)
+        log_txn, outcome, result = bank.log(n, st.final_ts)
+        err = orc.check(s.op, s.off, s.addr, n_acc, np.full(n_acc, 1000, np.int32), depth,
+                        st.final_ts, log_txn, outcome, result, bank.versions(),
+                        groups=bank.groups(st.final_ts))
+    assert err is None, err
+    upd = (s.op & 3) != 0
+    assert 0 < waits[upd].mean() < 1 and not waits[~upd].any()

@@ -251,6 +251,46 @@ def test_one_warp_model_is_exact(prevalidate, locks):
         assert (st.aborts_prevalid if prevalidate else st.aborts_read_write) > 0
 
 
+def round_groups(op, log):
+    """Group-end bitmap of a one-warp group-commit log: each round's timestamps form a group."""
+    n = len(log)
+    ends = np.zeros(((n + 31) // 32) * 32, bool)
+    rnd = np.asarray(log) // 32
+    ends[:n] = np.append(rnd[1:] != rnd[:-1], True)
+    return np.packbits(ends.reshape(-1, 32)[:, ::-1], axis=1).view(">u4").astype(np.uint32).ravel()
+
+
+def test_group_commit_model_installs_one_version_per_account_and_group():
+    """The one-warp model of group commit (prevalidate 3) replays exactly when the checker knows
+    the commit groups; without them the replay installs every write and the version slots
+    differ, so the group bitmap is what the comparison rests on."""
+    w = small_workload(n_txn=32 * 64, n_accounts=40)
+    op, off, addr = orc.generate(w)
+    init = np.full(40, 100, np.int32)
+    slots, log, outcome, result, st = orc.sim_1warp(op, off, addr, 40, init, 4, 3, True)
+    assert st.commits_update + st.commits_readonly + st.commits_nowrite == len(op)
+    assert st.rounds == len(op) // 32
+    g = round_groups(op, log)
+    assert orc.check(op, off, addr, 40, init, 4, st.final_ts, log, outcome, result, slots,
+                     groups=g) is None
+    assert "slot" in orc.check(op, off, addr, 40, init, 4, st.final_ts, log, outcome, result,
+                               slots)
+
+
+def test_check_rejects_a_snapshot_inside_a_commit_group():
+    w = small_workload(n_txn=32 * 64, n_accounts=40)
+    op, off, addr = orc.generate(w)
+    init = np.full(40, 100, np.int32)
+    slots, log, outcome, result, st = orc.sim_1warp(op, off, addr, 40, init, 4, 3, True)
+    g = round_groups(op, log)
+    ro = np.flatnonzero((op & 3) == 0)
+    inner = [ts for ts in range(1, st.final_ts) if not (g[(ts - 1) >> 5] >> ((ts - 1) & 31)) & 1]
+    out2 = outcome.copy()
+    out2[ro[-1]] = inner[len(inner) // 2] | orc.SNAP_FLAG
+    err = orc.check(op, off, addr, 40, init, 4, st.final_ts, log, out2, result, slots, groups=g)
+    assert err is not None and "inside a commit group" in err
+
+
 def test_cpu_baselines_agree_on_commutative_stream():
     # unconditional transfers with two reads commute: any serialisation ends in the same state
     w = small_workload(kind=2, up_reads=2, n_accounts=1000, n_txn=32 * 3000)
