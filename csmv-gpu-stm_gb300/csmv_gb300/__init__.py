@@ -181,6 +181,7 @@ def lib() -> C.CDLL:
         "csmv_bank_read_versions": (I32, [P, P]),
         "csmv_bank_read_log": (I32, [P, P, U32, P, P, U32]),
         "csmv_bank_read_groups": (I32, [P, P, U32]),
+        "csmv_measure_atomics": (I32, [C.c_int32, P]),
         "csmv_bank_device_info": (I32, [P, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                         C.POINTER(C.c_int), C.POINTER(C.c_size_t)]),
         "csmv_bank_destroy": (None, [P]),
@@ -860,6 +861,18 @@ def autotune(stream: Stream, repeats: int = 3, init: np.ndarray | None = None, *
            "csmv_bank_autotune")
     trials = [{n: getattr(t, n) for n, _ in TuneTrial._fields_} for t in res.trials[:res.n_trials]]
     return res.best, trials
+
+
+class AtomicRates(C.Structure):
+    _fields_ = [("same_word_per_s", C.c_double), ("spread_per_s", C.c_double),
+                ("cas_chain_ns", C.c_double), ("kernel_ms", C.c_double)]
+
+
+def measure_atomics(device: int = 0) -> dict:
+    """The device's L2 atomic rates (csmv_measure_atomics)."""
+    r = AtomicRates()
+    _check(lib().csmv_measure_atomics(device, C.byref(r)), "csmv_measure_atomics")
+    return {n: getattr(r, n) for n, _ in AtomicRates._fields_}
 
 
 def cuda_device_present() -> bool:

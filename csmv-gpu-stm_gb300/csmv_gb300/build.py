@@ -66,9 +66,9 @@ def build(verbose: bool = False) -> Path:
     objs = [BUILD / (s.name + ".o") for s in units]
     if _stale(LIB, objs):
         _run([nv, *ARCH, "-shared", "-o", str(LIB), *map(str, objs)])
-    devtest = CSRC / "devtest" / "devtest.cu"
-    if _stale(DEVTEST_LIB, [devtest] + headers):
-        _run([nv, *ARCH, *NVCC_FLAGS, "-shared", str(devtest), "-o", str(DEVTEST_LIB)])
+    devtests = sorted((CSRC / "devtest").glob("*.cu"))
+    if _stale(DEVTEST_LIB, devtests + headers):
+        _run([nv, *ARCH, *NVCC_FLAGS, "-shared", *map(str, devtests), "-o", str(DEVTEST_LIB)])
     for main in sorted(HOST.glob("*.cpp")):
         exe = BIN / main.stem
         if _stale(exe, [main, LIB] + headers):

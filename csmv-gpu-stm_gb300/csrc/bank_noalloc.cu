@@ -9,13 +9,18 @@
 // pre-validation, version depth 4) with all of its scratch in the file-scope device array
 // below. The caller passes only inputs and outputs, all in device memory.
 //
-// Limits: at most kNoAllocMaxAccounts accounts and kNoAllocMaxTxn transactions per call; the
-// array is kNoAllocScratchBytes (about 4.8 MiB) and every GPU that loads the library holds it
-// until the process exits. Calls share the array, so two calls that overlap on the GPU (on
-// different streams, or from different host threads) race and corrupt each other's results:
-// serialise them. The first call on a device looks up the array's device address (a host-side
-// reference to a __device__ array is not a device address) and sets the kernel's shared-memory
-// limit; make that first call before any stream capture.
+// Limits: at most CSMV_NOALLOC_MAX_ACCOUNTS accounts and CSMV_NOALLOC_MAX_TXN transactions per
+// call, and at most kLogCap = 8 x CSMV_NOALLOC_MAX_TXN commit timestamps (a transaction that
+// fails validation after drawing a timestamp uses one too); past that the kernel stops and the
+// call returns CSMV_ERR_CAPACITY. The array is kNoAllocScratchBytes (about 4.8 MiB) and every GPU
+// that loads the library holds it until the process exits. Calls share the array, so two calls
+// that overlap on the GPU (on different streams, or from different host threads) race and
+// corrupt each other's results: serialise them. The first call on a device looks up the
+// array's device address (a host-side reference to a __device__ array is not a device address)
+// and sets the kernel's shared-memory limit, and caches both; make that first call before any
+// stream capture. A cudaDeviceReset unloads the module and voids the cache: a process that
+// resets a device must not call this entry point on it afterwards. The caller's current device
+// is restored before the call returns.
 #include <chrono>
 #include <cstring>
 #include <mutex>
@@ -98,22 +103,53 @@ __global__ void noalloc_final_values(const unsigned long long* slots, int32_t* v
   }
 }
 
+// Restores the caller's current device when the call returns.
+struct DeviceRestore {
+  int prev = -1;
+  DeviceRestore() {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+  }
+  ~DeviceRestore() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+csmv_status run_noalloc(int32_t device, void* cuda_stream, uint32_t n_accounts,
+                        const int32_t* dev_init_values, const csmv_bank_stream* stream_desc,
+                        uint32_t client_warps, uint32_t ctas, int32_t* dev_values,
+                        uint32_t* dev_outcome, int32_t* dev_result, csmv_stats* out);
+
 }  // namespace
 
 extern "C" csmv_status csmv_bank_run_noalloc(int32_t device, void* cuda_stream,
                                              uint32_t n_accounts, const int32_t* dev_init_values,
-                                             const csmv_bank_stream* dev_stream,
+                                             const csmv_bank_stream* stream_desc,
                                              uint32_t client_warps, uint32_t ctas,
                                              int32_t* dev_values, uint32_t* dev_outcome,
                                              int32_t* dev_result, csmv_stats* out) {
+  DeviceRestore restore;
+  return run_noalloc(device, cuda_stream, n_accounts, dev_init_values, stream_desc, client_warps,
+                     ctas, dev_values, dev_outcome, dev_result, out);
+}
+
+namespace {
+
+csmv_status run_noalloc(int32_t device, void* cuda_stream, uint32_t n_accounts,
+                        const int32_t* dev_init_values, const csmv_bank_stream* stream_desc,
+                        uint32_t client_warps, uint32_t ctas, int32_t* dev_values,
+                        uint32_t* dev_outcome, int32_t* dev_result, csmv_stats* out) {
   auto bad = [](const char* why) {
     set_error("csmv_bank_run_noalloc: %s", why);
     return CSMV_ERR_INVALID_ARG;
   };
+  const csmv_bank_stream* dev_stream = stream_desc;  // a host struct holding device arrays
   if (device < 0 || device >= kMaxDevices) return bad("device out of range");
   if (!dev_init_values || !dev_stream || !dev_values || !dev_outcome || !dev_result)
     return bad("null pointer");
   if (!dev_stream->op || !dev_stream->off || !dev_stream->addr) return bad("null stream array");
+  if (dev_stream->split_round || dev_stream->deferred_warps)
+    return bad("the deferred queue (split_round, deferred_warps) is not available here");
+  if (dev_stream->txn_waits) return bad("txn_waits is not produced here (no group commit)");
   if (n_accounts < 2) return bad("n_accounts < 2");
   if (n_accounts > CSMV_NOALLOC_MAX_ACCOUNTS) {
     set_error("csmv_bank_run_noalloc: %u accounts exceed the fixed scratch limit of %u", n_accounts,
@@ -184,6 +220,8 @@ extern "C" csmv_status csmv_bank_run_noalloc(int32_t device, void* cuda_stream,
   p.batch = CSMV_BATCH_CTA;
   p.prevalidate = 1;
   p.spin_log2 = 24;
+  p.txn_aborts = dev_stream->txn_aborts;  // device memory, like op
+  p.backoff = dev_stream->backoff;
   void* args[] = {&p};
   CSMV_CUDA(cudaLaunchCooperativeKernel((const void*)kKernel, dim3(grid), dim3(threads), args, smem,
                                         stream));
@@ -210,9 +248,17 @@ extern "C" csmv_status csmv_bank_run_noalloc(int32_t device, void* cuda_stream,
     out->total_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
+  if (h_gs.error == ERR_CAPACITY) {
+    set_error("csmv_bank_run_noalloc: the run used more than the fixed scratch's %u commit "
+              "timestamps (aborted attempts draw timestamps too)",
+              kLogCap);
+    return CSMV_ERR_CAPACITY;
+  }
   if (h_gs.error) {
     set_error("csmv_bank_run_noalloc: device error %u", h_gs.error);
     return h_gs.error == ERR_DATA ? CSMV_ERR_INVALID_ARG : CSMV_ERR_TIMEOUT;
   }
   return CSMV_OK;
 }
+
+}  // namespace

@@ -32,7 +32,11 @@ inline uint32_t scale(uint32_t r, uint32_t n) {  // multiply-shift into [0, n)
 
 // Zipf(theta) over ranks 1..n by rejection-inversion (W. Hormann and G. Derflinger,
 // "Rejection-inversion to generate variates from monotone discrete distributions",
-// ACM TOMACS 6(3):169-184, 1996).
+// ACM TOMACS 6(3):169-184, 1996). H is the integral of h(x) = x^-theta written as
+// log(x) * expm1((1-theta) log x) / ((1-theta) log x) and Hinv its inverse through log1p, so
+// both stay accurate as theta approaches 1; the helpers log1p(x)/x and expm1(x)/x fall back to
+// their Taylor series near 0. This numerically stable form is the one of the widely published
+// Apache Commons Math sampler (RejectionInversionZipfSampler), restated here.
 class Zipf {
  public:
   Zipf(double theta, uint32_t n) : s_(theta), n_(n) {

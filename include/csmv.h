@@ -302,18 +302,27 @@ void csmv_bank_destroy(csmv_bank_t* h);
  * pre-validation, 4 versions per account) with its scratch - version store, commit words,
  * completion bitmap, commit log - in one fixed device array of about 4.8 MiB, which every GPU
  * that loads the library holds until the process exits. Limits: n_accounts <= 65536 and
- * n_txn <= 65536 per call (larger sizes return CSMV_ERR_CAPACITY). All pointers are device
- * memory owned by the caller: dev_init_values[n_accounts] in; dev_values[n_accounts] (latest
- * value of each account), dev_outcome[n_txn] and dev_result[n_txn] (as csmv_bank_read_log) out.
- * cuda_stream is a cudaStream_t (NULL = the legacy default stream); the call returns after the
- * stream has finished the run. Calls share the array and keep nothing between them, so calls
- * that overlap on the GPU race: serialise them. The first call on a device looks up the array's
- * device address; make that first call before any stream capture. */
+ * n_txn <= 65536 per call (larger sizes return CSMV_ERR_CAPACITY), and at most
+ * CSMV_NOALLOC_MAX_TIMESTAMPS commit timestamps per call - a transaction that fails validation
+ * after drawing a timestamp uses one too, so a very contended stream can run out; the kernel
+ * then stops and the call returns CSMV_ERR_CAPACITY with a message naming that limit.
+ * stream_desc is a HOST struct whose op, off and addr arrays (and txn_aborts / backoff, when
+ * set) are in device memory; split_round, deferred_warps and txn_waits must be 0. The other
+ * pointers are device memory owned by the caller: dev_init_values[n_accounts] in;
+ * dev_values[n_accounts] (latest value of each account), dev_outcome[n_txn] and dev_result[n_txn]
+ * (as csmv_bank_read_log) out. cuda_stream is a cudaStream_t (NULL = the legacy default stream);
+ * the call returns after the stream has finished the run, with the caller's current device
+ * restored; out->kernel_ms is 0 (no events are created), out->total_ms is the host wall time.
+ * Calls share the array and keep nothing between them, so calls that overlap on the GPU race:
+ * serialise them. The first call on a device looks up the array's device address and caches
+ * it; make that first call before any stream capture, and make no call on a device after a
+ * cudaDeviceReset of it (the reset voids the cached address). */
 #define CSMV_NOALLOC_MAX_ACCOUNTS 65536
 #define CSMV_NOALLOC_MAX_TXN 65536
+#define CSMV_NOALLOC_MAX_TIMESTAMPS (8 * CSMV_NOALLOC_MAX_TXN)
 csmv_status csmv_bank_run_noalloc(int32_t device, void* cuda_stream, uint32_t n_accounts,
                                   const int32_t* dev_init_values,
-                                  const csmv_bank_stream* dev_stream, uint32_t client_warps,
+                                  const csmv_bank_stream* stream_desc, uint32_t client_warps,
                                   uint32_t ctas, int32_t* dev_values, uint32_t* dev_outcome,
                                   int32_t* dev_result, csmv_stats* out);
 
@@ -590,6 +599,22 @@ typedef struct csmv_tune_result {
 } csmv_tune_result;
 csmv_status csmv_bank_autotune(const csmv_bank_config* base, const csmv_bank_stream* host_sample,
                                const int32_t* host_init, uint32_t repeats, csmv_tune_result* out);
+
+/* ------------------------------------------------------------------------------------------
+ * L2 atomic rates of the device (no counterpart in the reference): the bounds of the commit
+ * path, which runs on L2 atomics and on chains of dependent L2 round trips (a contended lock
+ * passes between warps through a few of them). Measured by the library's own kernels with CUDA
+ * events: returning atomicAdds of a full grid on one word, and on pseudo-random words of a
+ * 64 MB (L2-resident) buffer; and the latency of one dependent 64-bit CAS (one thread, a chain
+ * of CASes on one word). Allocates and frees a 64 MB buffer.
+ * ------------------------------------------------------------------------------------------ */
+typedef struct csmv_atomic_rates {
+  double same_word_per_s;  /* returning atomics per second on a single word                  */
+  double spread_per_s;     /* returning atomics per second spread over L2                    */
+  double cas_chain_ns;     /* latency of one dependent CAS (one L2 round trip)               */
+  double kernel_ms;        /* device time of the measurement                                 */
+} csmv_atomic_rates;
+csmv_status csmv_measure_atomics(int32_t device, csmv_atomic_rates* out);
 
 /* Page-locked host buffers for staging streams (the e2e path copies from pinned memory).
  * Replaces CUDA_DUAL_ALLOC's cudaMallocHost half (memcachedGPU/cuda_util.h:50-60). */

@@ -1,11 +1,12 @@
 #!/bin/bash
 # ref_build.sh - builds the oracle's parity pin from the reference sources where they lie.
 # TEST INFRASTRUCTURE ONLY. Output goes to oracle/_ref/ (git-ignored); nothing is copied.
-#   usage: oracle/ref_build.sh [reference_root]     (default /root/reference)
-# Exits 0 without building when the reference tree is absent (the GPU machine has none).
+#   usage: oracle/ref_build.sh [reference_root]
+# The reference tree is the argument, else $CSMV_REFERENCE, else a checkout named "reference"
+# beside this repository. Exits 0 without building when no tree is found (the GPU machine has none).
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-${CSMV_REFERENCE:-/root/reference}}"
+REF="${1:-${CSMV_REFERENCE:-$HERE/../../reference}}"
 if [ ! -f "$REF/bank/csmv_sh/API.cu" ]; then
   echo "ref_build: no reference tree at $REF; skipping"
   exit 0

@@ -49,10 +49,12 @@ def _engine(torch, w, s, init):
         return bank.values(), outcome, result, st
 
 
-def _call(torch, fn, w, s, init, **kw):
+def _call(torch, fn, w, s, init, aborts=None, **kw):
     d = [_dev(torch, x) for x in (s.op, s.off, s.addr)]
     ds = cg.BankStream(w.n_txn, d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(),
                        int(s.addr.shape[0]))
+    if aborts is not None:
+        ds.txn_aborts = aborts.data_ptr()
     d_init = _dev(torch, init)
     vals = torch.full((w.n_accounts,), -7, dtype=torch.int32, device="cuda")
     outc = torch.full((w.n_txn,), -7, dtype=torch.int32, device="cuda")
@@ -95,3 +97,48 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     s = cg.generate(w)
     rc, *_ = _call(torch, fn, w, s, np.zeros(100, np.int32))
     assert rc == 5 and b"scratch limit" in cg.lib().csmv_last_error()
+
+
+def test_noalloc_full_grid_keeps_the_invariants_on_two_calls_in_a_row():
+    """The default launch shape (every co-resident CTA, 15 client warps each) on a contended bank:
+    many warps overlap, timestamps interleave across CTAs and the completion-bitmap ring turns
+    over. No commit log leaves the fixed scratch, so the checks are the invariants: every
+    transaction commits once, the balance is conserved, each outcome is a distinct commit
+    timestamp within the run or a snapshot, and the per-transaction failed-attempt counts passed
+    through add up to the aborts reported."""
+    torch = pytest.importorskip("torch")
+    fn = _noalloc()
+    w = c1_workload(n_txn=MAX_TXN, n_accounts=4096, seed=23, pr_read_pct=20,
+                    dist=cg.DIST_ZIPF, zipf_theta=0.9, up_reads=4)
+    s = cg.generate(w)
+    init = np.full(w.n_accounts, 1000, np.int32)
+    for _ in range(2):
+        ab = torch.zeros(w.n_txn, dtype=torch.int32, device="cuda")
+        rc, vals, outc, res, st = _call(torch, fn, w, s, init, aborts=ab, ctas=0, client_warps=15)
+        assert rc == 0, cg.lib().csmv_last_error()
+        assert st.commits_update + st.commits_readonly + st.commits_nowrite == w.n_txn
+        assert int(vals.astype(np.int64).sum()) == int(init.astype(np.int64).sum())
+        snap = (outc & np.uint32(cg.SNAP_FLAG)) != 0
+        ts = outc[~snap]
+        assert ts.size == st.commits_update and len(np.unique(ts)) == ts.size
+        assert ts.min() >= 1 and ts.max() <= st.final_ts
+        assert ((outc[snap] & np.uint32(0x7FFFFFFF)) <= st.final_ts).all()
+        assert int(ab.sum()) == st.aborts
+
+
+def test_noalloc_reports_a_full_timestamp_log_as_capacity():
+    """Four accounts, every transfer reading all four and writing two, unconditionally, on every
+    SM: two warps can hold disjoint pairs of locks at once and each then fails to validate the
+    other pair's reads, so nearly every timestamp drawn ends as a hole and the run needs more
+    timestamps than the fixed scratch's log holds; the call must stop and say so
+    (CSMV_ERR_CAPACITY, with a message naming the limit)."""
+    torch = pytest.importorskip("torch")
+    fn = _noalloc()
+    w = c1_workload(n_txn=MAX_TXN, n_accounts=4, seed=5, pr_read_pct=0, up_reads=4,
+                    kind=cg.KIND_TRANSFER_ALWAYS)
+    s = cg.generate(w)
+    rc, _, _, _, st = _call(torch, fn, w, s, np.full(4, 1000, np.int32), ctas=0, client_warps=15)
+    if rc == 0:
+        pytest.skip(f"the run fit in the log ({st.final_ts} timestamps)")
+    assert rc == 5, cg.lib().csmv_last_error()
+    assert b"commit timestamps" in cg.lib().csmv_last_error()
