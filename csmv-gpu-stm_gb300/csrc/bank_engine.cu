@@ -110,6 +110,8 @@ static csmv_status validate_config(const csmv_bank_config* c) {
   if (c->max_txn == 0 || c->max_txn % 32) return bad("max_txn must be a positive multiple of 32");
   if (c->spin_limit_log2 < 10 || c->spin_limit_log2 > 30) return bad("spin_limit_log2");
   if (c->flow_warps > 16) return bad("flow_warps must be 0 (default) or 1..16");
+  if (c->max_reads != 0 && c->max_reads != 4 && c->max_reads != 8)
+    return bad("max_reads must be 0 (8), 4 or 8");
   return CSMV_OK;
 }
 
@@ -130,6 +132,7 @@ static void free_all(csmv_bank_t* h) {
   cudaFree(h->d_backoff);
   cudaFree(h->d_waits);
   cudaFree(h->grp);
+  cudaFree(h->tk);
   flow_scratch_free(h->flow);
   h->flow = nullptr;
   if (h->ev0) cudaEventDestroy(h->ev0);
@@ -155,10 +158,15 @@ extern "C" csmv_status csmv_bank_create(const csmv_bank_config* cfg, csmv_bank_t
   h->cfg = *cfg;
   h->n_sms = n_sms;
   const bool cluster = cfg->batch == CSMV_BATCH_CLUSTER;
-  h->kernel = cluster ? pick_cluster(cfg->version_depth) : pick_kernel(cfg->version_depth);
+  const bool r4 = cfg->max_reads == 4;
+  if (r4)
+    h->kernel = cluster ? pick_cluster_r4(cfg->version_depth) : pick_kernel_r4(cfg->version_depth);
+  else
+    h->kernel = cluster ? pick_cluster(cfg->version_depth) : pick_kernel(cfg->version_depth);
   h->threads = (int)(cfg->client_warps + 1) * 32;
   // cluster form: every CTA reserves the cluster's mailboxes; the leader's are used
-  h->smem = cta_shared_bytes<kMaxR, kMaxW>(cfg->client_warps * (cluster ? cfg->cluster_size : 1u));
+  const uint32_t n_mail = cfg->client_warps * (cluster ? cfg->cluster_size : 1u);
+  h->smem = r4 ? cta_shared_bytes_r4(n_mail) : cta_shared_bytes<kMaxR, kMaxW>(n_mail);
   if (cfg->prevalidate == 3)  // one group-commit table per client warp of the CTA
     h->smem = group_scratch_offset(h->smem) + cfg->client_warps * sizeof(GroupScratch);
   auto fail = [&](csmv_status s) {
@@ -229,6 +237,7 @@ extern "C" csmv_status csmv_bank_create(const csmv_bank_config* cfg, csmv_bank_t
       {(void**)&h->d_backoff, (size_t)cfg->max_txn * 4},
       {(void**)&h->d_waits, (size_t)cfg->max_txn * 4},
       {(void**)&h->grp, (size_t)((h->log_cap + 31u) / 32u) * 4},
+      {(void**)&h->tk, n * 8},
   };
   h->grp_words = (h->log_cap + 31u) / 32u;
   for (auto& a : allocs) {
@@ -313,6 +322,7 @@ BankParams csmv::bank_params(const csmv_bank_t* h, const uint32_t* op, const uin
   p.spin_log2 = c.spin_limit_log2;
   p.txn_aborts = txn_aborts;
   p.grp = (c.log_commits && c.prevalidate == 3 && c.validate == CSMV_VALIDATE_STAMP) ? h->grp : nullptr;
+  p.tk = h->tk;
   return p;
 }
 
@@ -383,6 +393,8 @@ static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* of
     CSMV_CUDA(cudaMemsetAsync(txn_waits, 0, (size_t)n_txn * 4, h->stream));
   if (serial) p.grp = nullptr;
   if (p.grp) CSMV_CUDA(cudaMemsetAsync(h->grp, 0, (size_t)h->grp_words * 4, h->stream));
+  if (!serial && c.prevalidate == 3)  // empty lock queues (a failed run may have left tickets)
+    CSMV_CUDA(cudaMemsetAsync(h->tk, 0, (size_t)c.n_accounts * 8, h->stream));
   h->last_grouped = p.grp != nullptr;
   csmv_status bst = bank_begin_run(h);
   if (bst != CSMV_OK) return bst;

@@ -12,6 +12,11 @@ namespace csmv {
 constexpr uint32_t kDoneWords = 1u << 16;  // 2^21 timestamps in flight at most
 using KernelFn = void (*)(BankParams);
 
+// kernels for transfers of at most four reads (bank_engine_r4.cu)
+KernelFn pick_kernel_r4(uint32_t depth);
+KernelFn pick_cluster_r4(uint32_t depth);
+size_t cta_shared_bytes_r4(uint32_t n_mail);
+
 struct FlowScratch;                                        // bank_flow.cu
 void flow_scratch_free(FlowScratch* f);                    // frees the dataflow lane's buffers
 csmv_status flow_scratch_reset(FlowScratch* f, cudaStream_t s);  // zeroes its per-account counts
@@ -42,6 +47,7 @@ struct csmv_bank_t {
   uint32_t* d_backoff = nullptr;  // host-buffer runs: the stream's backoff array, copied in
   uint32_t* d_waits = nullptr;    // host-buffer runs: per-transaction lock waits, copied out
   uint32_t* grp = nullptr;        // group-end bitmap of the last run (log_commits)
+  uint32_t* tk = nullptr;         // group commit: per account {next ticket, ticket served}
   uint32_t grp_words = 0;
   bool last_grouped = false;      // the last run was a group-commit run of the engine
   uint64_t addr_cap = 0;

@@ -102,6 +102,8 @@ struct BankParams {
   uint32_t* grp;            // group commit with log: bit (ts-1-log_base) = ts ends a commit group
   uint32_t* txn_waits;      // optional [n_rounds*32]: 1 when the transaction's group waited for a
                             // lock another warp held (group commit)
+  uint32_t* tk;             // group commit: per account {next ticket, ticket served} of its
+                            // lock's wait queue
   const uint32_t* backoff;  // optional [n_rounds*32]: longest pause (ns) before a retry of each
                             // transaction (a scheduler's per-transaction backoff)
 };
@@ -372,31 +374,54 @@ __device__ __forceinline__ bool group_cas_lock(unsigned long long* cw, uint32_t 
 }
 
 // Waits for account x's lock and takes it, with the account's version slots (ed) and latest value
-// (v) read as the lock is taken: the poll that finds the lock free is an acquire load, so the
+// (v) read as the lock is taken. Waiters queue first-come first-served on the account's ticket
+// pair (tk[2x] = next ticket, tk[2x + 1] = ticket being served): a warp takes a ticket, waits
+// until it is served, then takes the lock as soon as its holder releases it and serves the next
+// ticket - so only the head of the queue polls the commit word, and a waiter far from the
+// account's L2 slice is not overtaken forever by nearer ones (a plain polling race hands a hot
+// lock to whoever sees the release first). A round's fast path (group_cas_lock) may still take a
+// free lock ahead of the queue. The poll that finds the lock free is an acquire load, so the
 // slots loaded after it hold the version of the stamp it saw, and a CAS that succeeds at that
-// stamp proves them current (*stale stays false). Every waiter polls at the same short interval
-// (a back-off that grows with the wait would hand a contended lock to the newest waiters and
-// starve the oldest). Bounded: false after 2^18 polls (about 100 ms), or once another warp
-// raised a device error.
+// stamp proves them current (*stale stays false). A waiter never leaves the queue while its run
+// is healthy (the tickets behind it would wait forever): the waits are bounded only by the
+// device error word and by 2^spin_log2 polls, after which the run fails with ERR_WAIT_TURN.
 template <int DEPTH>
 __device__ __forceinline__ bool group_wait_lock(const BankParams& p, uint32_t x, uint32_t me,
                                                 uint32_t& stamp, bool& stale,
                                                 SlotEditor<DEPTH>& ed, int32_t& v) {
-  for (uint32_t it = 0; it < (1u << 18); it++) {
+  uint32_t* next = p.tk + 2u * (size_t)x;
+  uint32_t* serving = next + 1;
+  const uint32_t mine = atomicAdd(next, 1u);
+  const uint64_t limit = 1ull << min(p.spin_log2, 22u);  // at most a few seconds
+  bool turn = false;
+  for (uint64_t it = 0; it < limit; it++) {
+    const uint32_t now = ld_acquire_gpu(serving);
+    if (now == mine) {
+      turn = true;
+      break;
+    }
+    if ((it & 63u) == 63u && ld_relaxed_gpu(&p.gs->error) != 0u) return false;
+    __nanosleep(min(64u * (mine - now), 1024u));  // farther back in the queue: poll less often
+  }
+  bool got = false;
+  for (uint64_t it = 0; turn && it < limit; it++) {
     const unsigned long long w = ld_acquire_gpu(&p.cw[x]);
     if ((w >> 32) == 0ull) {
       ed.load(p.slots + (size_t)x * DEPTH);
       if (atomicCAS(&p.cw[x], w, w | ((unsigned long long)me << 32)) == w) {
         stamp = (uint32_t)w;
         stale = !ed.find(stamp, v);
-        return true;
+        got = true;
+        break;
       }
-      continue;  // another waiter took it: poll again
+      continue;  // a fast-path CAS took it first: poll again
     }
-    if ((it & 63u) == 63u && ld_relaxed_gpu(&p.gs->error) != 0u) return false;
-    __nanosleep(64);
+    if ((it & 63u) == 63u && ld_relaxed_gpu(&p.gs->error) != 0u) break;
+    __nanosleep(32);
   }
-  return false;
+  if (turn) atomicAdd(serving, 1u);  // the next ticket's turn (also when this wait failed)
+  if (!got) raise_error(&p.gs->error, ERR_WAIT_TURN);
+  return got;
 }
 
 // One attempt of a transfer round as a commit group, warp-collective. Every active lane's

@@ -181,6 +181,10 @@ typedef struct csmv_bank_config {
   uint32_t spin_limit_log2;    /* bounded waits give up after 2^this polls (default 24)       */
   int32_t device;
   uint32_t flow_warps;         /* warps of the dataflow lane's execution CTA, 1..16 (0 = 8)    */
+  uint32_t max_reads;          /* reads of a transfer the commit kernel holds: 0 or 8 = up to 8;
+                                  4 = up to 4 (a leaner kernel; a transfer with more reads is
+                                  malformed, CSMV_ERR_INVALID_ARG). Read-only transactions may
+                                  read up to 32 accounts either way                            */
 } csmv_bank_config;
 
 void csmv_bank_config_default(csmv_bank_config* cfg);

@@ -44,7 +44,8 @@ def test_config_validation_is_a_status():
                 dict(spin_limit_log2=2), dict(n_accounts=1), dict(batch=9),
                 dict(batch=3, validate=1, writeback=1), dict(batch=3, cluster_size=3),
                 dict(batch=3, cluster_size=4, client_warps=15), dict(flow_warps=17),
-                dict(prevalidate=4), dict(prevalidate=3, validate=1, batch=1)):
+                dict(prevalidate=4), dict(prevalidate=3, validate=1, batch=1),
+                dict(max_reads=5)):
         with pytest.raises(cg.CsmvError) as e:
             cg.Bank(cg.bank_config(**bad))
         assert e.value.status == 1, bad

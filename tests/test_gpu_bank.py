@@ -52,6 +52,9 @@ VARIANTS = {
     "stamp-cta-chain": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CTA, prevalidate=2),
     "stamp-cluster2": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CLUSTER, cluster_size=2),
     "stamp-cta-group": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CTA, prevalidate=3),
+    "stamp-cta-group-r4": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CTA, prevalidate=3,
+                               max_reads=4),
+    "stamp-cta-r4": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CTA, max_reads=4),
     "stamp-warp-group": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_WARP, prevalidate=3),
     "stamp-cluster2-group": dict(validate=cg.VALIDATE_STAMP, batch=cg.BATCH_CLUSTER,
                                  cluster_size=2, prevalidate=3),
@@ -79,6 +82,15 @@ def test_high_contention_exact(depth, validate, prevalidate):
         assert st.aborts > 0
 
 
+def test_transfer_wider_than_max_reads_is_refused():
+    """A transfer reading more accounts than the kernel holds (max_reads = 4) fails the run as
+    malformed instead of being cut short."""
+    w = c1_workload(n_txn=32 * 64, n_accounts=512, up_reads=6, seed=6)
+    with pytest.raises(cg.CsmvError) as e:
+        run_checked(w, ctas=4, client_warps=2, prevalidate=3, max_reads=4)
+    assert e.value.status == 1
+
+
 def test_two_accounts_extreme():
     w = c1_workload(n_txn=32 * 40, n_accounts=2, pr_read_pct=0, up_reads=2, seed=5)
     run_checked(w, ctas=2, client_warps=2, init_value=50)
@@ -88,13 +100,14 @@ def test_single_round():
     run_checked(c1_workload(n_txn=32, n_accounts=100), ctas=1, client_warps=1)
 
 
-@pytest.mark.parametrize("prevalidate", [3, 2, 1])
-def test_zipf_contended_exact(prevalidate):
+@pytest.mark.parametrize("prevalidate,max_reads", [(3, 8), (3, 4), (2, 8), (1, 8)])
+def test_zipf_contended_exact(prevalidate, max_reads):
     """1M accounts, Zipf 0.99, read 4 / write 2, 20% read-only scans of 32, one CTA per SM."""
     w = cg.bank_workload(1 << 20, 1 << 16, seed=9, pr_read_pct=20, ro_reads=32, up_reads=4,
                          kind=cg.KIND_TRANSFER, amt_lo=1, amt_hi=10, dist=cg.DIST_ZIPF,
                          zipf_theta=0.99)
-    st, _, _ = run_checked(w, ctas=152, client_warps=2, version_depth=8, prevalidate=prevalidate)
+    st, _, _ = run_checked(w, ctas=152, client_warps=2, version_depth=8, prevalidate=prevalidate,
+                           max_reads=max_reads)
     if prevalidate != 3:  # group commit waits for write locks instead of aborting on them
         assert st.aborts > 0
 
