@@ -8,29 +8,37 @@ is 2^24 transactions, seeded; a step is one batch of 2^20 consecutive transactio
 transactions and the account state carries over between steps. Stream arrays are larger than
 L2 (28 MB per batch), so no L2 flush is needed between steps.
 
-Two arms run the same batches on separate banks:
-  plain    the commit engine alone (csmv_bank_run_device): every transfer through the stamp
-           protocol, client warps + per-CTA commit server on every SM
-  learned  the learned conflict scheduler in front of the same engine (csmv_sched_run): a probe
-           slice in stream order trains the conflict predictor, the predictor routes likely-
-           conflicting transfers to the dataflow lane (run after the rest, each transfer as
-           soon as the transfers it depends on have run) and spaces the rest
-value = the learned arm's committed tx/s (GPU time of the whole step, inputs resident in HBM);
-e2e = the same through host buffers (pinned -> device copies and the statistics read inside
-the timed region). Both arms' throughput and abort rate are in "plain" / "learned".
+value = the learned arm: the learned conflict scheduler (csmv_sched_run) in front of the commit
+engine in group-commit mode. The scheduler probes 2 % of a batch's rounds in stream order, trains
+its network on the probe's conflicts (aborts and lock waits), and reorders and groups the rest:
+transfers it flags are sorted by the hot accounts they touch into rounds of 32, each hot
+account's rounds spread over the batch, with a per-transaction retry backoff. EVERY transaction
+of the batch then goes through the engine: its warp takes the write locks, the CTA's commit
+server draws the timestamps, every read of an account the group does not lock is validated, and
+the versions are installed - nothing bypasses validation. GPU-resident inputs; wall time of the
+step between device synchronisations.
+e2e = the same through host buffers: the batch's op/off arrays and address range are copied from
+pinned memory inside the timed region, and each run's per-transaction outcomes and read-only
+results are copied back.
 
-Extra sections: "hotspot" (1 % hot set drawing 30 % of the accesses, moving every 2^20
-transactions: learned vs plain), "uniform" (the same bank with uniform accounts, plain engine),
-"memcd" (8-way cache of 2^20 sets, Zipf(0.99) keys over 4 M, 99 % GET rounds, 64 K-request
-batches through the batch call: throughput and p50/p99 batch latency) and "serving" (the same
-cache behind the serving loop under open-loop Poisson arrivals at 10-100 % of its closed-loop
-peak, batches of 1 K-64 K requests, 95 % GET rounds: achieved req/s and p50/p99 latency).
+Comparison arms on the same batches (reported beside the headline, not in it):
+  plain              the engine alone in stream order with the reference's commit method
+                     (per-transaction validation, intra-warp pre-validation, CTA-batched
+                     timestamps: batchedAtrInsert), the method the benchmark spec calls plain
+  group_stream       the engine's group commit in stream order, no scheduler
+  dataflow_lane      the earlier path: the scheduler deferring flagged transfers to the dataflow
+                     lane, which executes them in stream order WITHOUT locks or validation
+                     (labelled as such; not CSMV)
+Extra sections: "hotspot" (learned vs plain on a shifting hotspot), "uniform", "c1" (the small
+bank of the reference's own configuration), "variants" (the engine's validation / batching /
+write-back / cluster modes on uniform and Zipf banks), "memcd", "serving", "atomics" (the L2
+atomic rates of the GPU, the engine's roofline).
 
 --impl reference runs the reference arm: the path's CPU execution (the oracle port, striped
-locks on every host core) on the same batches. --case NAME runs one small invocation of one
-kernel for profiling (engine, serial, flow, mlp, memcd, sched). Multi-GPU: replicas only (no
-collective on the path); each rank runs its own instance on its own GPU, value sums the ranks'
-transactions over the slowest rank's time.
+locks on every host core) on the same batches, generated by the oracle's own generator.
+--case NAME runs one small invocation of one kernel for profiling (engine, group, serial, flow,
+mlp, memcd, sched). Multi-GPU: replicas only (no collective on the path); each rank runs its own
+instance on its own GPU, value sums the ranks' transactions over the slowest rank's time.
 """
 from __future__ import annotations
 
@@ -55,24 +63,29 @@ WORKLOAD = dict(seed=2026, pr_read_pct=20, ro_reads=32, up_reads=4, amt_lo=1, am
                 zipf_theta=0.99)
 B_UPDATE = 16 * 4 + 12 * 2   # algorithmic bytes of a transfer: 4 versioned reads, 2 writes
 B_RO = 16 * 32               # a 32-account read-only scan
-SCHED = dict(serial_lane=2, defer_threshold=0.0, probe_every=3, probe_rounds_pct=2)
-FLOW_WARPS = 8  # warps of the dataflow lane's execution CTA
+ENGINE = dict(prevalidate=3, max_reads=4)          # group commit, kernels for <= 4 reads
+SCHED = dict(plan=1, probe_rounds_pct=2, probe_every=3)
+PLAIN = dict(prevalidate=1, max_reads=4)           # the reference's commit method
+FLOW = dict(plan=0, serial_lane=2, defer_threshold=0.0, probe_every=3, probe_rounds_pct=2)
+TRIPS_PER_HOLD = 4  # dependent L2 round trips of a contended lock's hand-off and hold: the lock
+                    # CAS, the timestamp draw, the validation load, the releasing store
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="csmv", choices=["csmv", "reference"])
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--dist", default="zipf", choices=["zipf", "uniform", "hotspot"])
-    ap.add_argument("--client-warps", type=int, default=int(os.environ.get("CSMV_CLIENT_WARPS", 2)))
+    ap.add_argument("--client-warps", type=int, default=int(os.environ.get("CSMV_CLIENT_WARPS", 1)))
     ap.add_argument("--ctas", type=int, default=int(os.environ.get("CSMV_CTAS", 152)))
     ap.add_argument("--depth", type=int, default=int(os.environ.get("CSMV_DEPTH", 8)))
     ap.add_argument("--case", default=None,
-                    choices=["engine", "serial", "flow", "mlp", "memcd", "sched"])
-    ap.add_argument("--no-extras", action="store_true", help="skip hotspot/uniform/memcd sections")
+                    choices=["engine", "group", "serial", "flow", "mlp", "memcd", "sched"])
+    ap.add_argument("--case-txn", type=int, default=1 << 18)
+    ap.add_argument("--no-extras", action="store_true", help="skip the extra sections")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (use the flags)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -185,53 +198,77 @@ class DevBatch:
 
 
 def launches_learned(rep) -> int:
-    """Kernels the scheduler and the engine launched for one chunk (see sched_engine.cu)."""
+    """Kernels the scheduler and the engine launched for one chunk (sched_engine.cu, plan 1)."""
     n = 1  # access counts
     if rep.n_probe:
         n += 1 + 1 + 2 + 4  # features, probe engine run, labels + rates, 2 x (grad + adam)
     n += 2 + 2  # features and network forward; read-only flags and scan
     if rep.n_planned:
-        n += 6  # keys, buckets, scan, scatter, read-only list, emit
-        n += 1 if rep.planned.commits else 0  # concurrent engine run
-        if rep.n_serial:                      # dataflow lane: analysis, sort, run, commit
-            n += 17 + 5 * (((N_ACCOUNTS - 1).bit_length() + 7) // 8)
+        # hot flags, 3-kernel scan, keys, 3-kernel scan, cold flags, 3-kernel scan, scatter,
+        # round buckets, 3-kernel scan, round scatter, expand, read-only list, emit, backoff
+        n += 1 + 3 + 1 + 3 + 1 + 3 + 1 + 1 + 3 + 1 + 1 + 1 + 1 + 1
+        n += 1 if rep.planned.commits else 0  # the planned engine run
     return n
 
 
 def new_bank(cg, args, local, max_txn, **over):
     kw = dict(n_accounts=N_ACCOUNTS, version_depth=args.depth, client_warps=args.client_warps,
-              ctas=args.ctas, max_txn=max_txn, log_commits=0, device=local, flow_warps=FLOW_WARPS)
+              ctas=args.ctas, max_txn=max_txn, log_commits=1, device=local, **ENGINE)
     kw.update(over)
     bank = cg.Bank(**kw)
     bank.load()
     return bank
 
 
+def plan_lock_rounds(op, off, addr, order):
+    """Largest number of rounds (32 consecutive transactions of `order`) that write one account:
+    the length of the busiest account's lock chain in this plan."""
+    n = (len(order) // 32) * 32
+    o = np.asarray(order[:n]).reshape(-1, 32)
+    upd = (op[o[:, 0]] & 3) != 0
+    o = o[upd]
+    w = np.stack([addr[off[o]], addr[off[o] + 1]], 2).reshape(o.shape[0], 64).astype(np.int64)
+    w.sort(axis=1)
+    first = np.ones_like(w, dtype=bool)
+    first[:, 1:] = w[:, 1:] != w[:, :-1]
+    counts = np.bincount(w[first], minlength=1)
+    top = int(np.argmax(counts))
+    return int(counts[top]), top, int(o.shape[0])
+
+
 # ---------------------------------------------------------------------------------------------
 # arms
 # ---------------------------------------------------------------------------------------------
 
-def run_plain(cg, dev, addr_dev, n_addr, args, local, warm, timed):
-    bank = new_bank(cg, args, local, args.batch)
-    res = dict(ms=0.0, commits=0, aborts=0, ro=0, upd=0)
-    for i in range(warm + timed):
+def run_engine(cg, dev, addr_dev, n_addr, args, local, batches, **over):
+    """The engine alone on device batches (stream order); device time from the engine's events."""
+    bank = new_bank(cg, args, local, args.batch, **over)
+    res = dict(ms=0.0, commits=0, aborts=0, ro=0, upd=0, steps=0)
+    for j, i in enumerate(batches):
         st = bank.run_device(dev[i].stream(cg, addr_dev, n_addr))
-        if i >= warm:
-            res["ms"] += st.kernel_ms
-            res["commits"] += st.commits
-            res["aborts"] += st.aborts
-            res["ro"] += st.commits_readonly
-            res["upd"] += st.commits_update + st.commits_nowrite
+        if j == 0:
+            continue  # warm-up
+        res["ms"] += st.kernel_ms
+        res["commits"] += st.commits
+        res["aborts"] += st.aborts
+        res["ro"] += st.commits_readonly
+        res["upd"] += st.commits_update + st.commits_nowrite
+        res["steps"] += 1
     info = bank.device_info()
     bank.close()
+    res["tx_s"] = res["commits"] / (res["ms"] * 1e-3) if res["ms"] else 0.0
+    res["abort_rate"] = res["aborts"] / max(1, res["aborts"] + res["commits"])
     return res, info
 
 
-def run_learned(torch, cg, dev, addr_dev, n_addr, args, local, warm, timed):
-    bank = new_bank(cg, args, local, args.batch)
-    sched = cg.Scheduler(n_accounts=N_ACCOUNTS, max_txn=args.batch, device=local, **SCHED)
-    res = dict(wall=0.0, commits=0, aborts=0, launches=0, serial_ms=0.0, serial_txn=0,
-               plan_ms=0.0, train_ms=0.0)
+def run_learned(torch, cg, dev, addr_dev, n_addr, args, local, warm, timed, sched_cfg=SCHED,
+                bank_over=None):
+    bank = new_bank(cg, args, local, args.batch, **(bank_over or {}))
+    sched = cg.Scheduler(n_accounts=N_ACCOUNTS, max_txn=args.batch, device=local, **sched_cfg)
+    res = dict(wall=0.0, commits=0, aborts=0, launches=0, plan_ms=0.0, train_ms=0.0,
+               engine_ms=0.0, serial_ms=0.0, serial_txn=0, flagged=0, ww=0, rw=0, age=0,
+               device_ms=0.0, rounds=0)
+    last = None
     for i in range(warm + timed):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -243,19 +280,34 @@ def run_learned(torch, cg, dev, addr_dev, n_addr, args, local, warm, timed):
             res["commits"] += rep.commits
             res["aborts"] += rep.aborts
             res["launches"] += launches_learned(rep)
-            res["serial_ms"] += rep.serial.kernel_ms
-            res["serial_txn"] += rep.n_serial
             res["plan_ms"] += rep.plan_ms
             res["train_ms"] += rep.train_ms
+            res["engine_ms"] += rep.probe.kernel_ms + rep.planned.kernel_ms
+            res["serial_ms"] += rep.serial.kernel_ms
+            res["serial_txn"] += rep.n_serial
+            res["flagged"] += rep.n_flagged
+            res["device_ms"] += rep.kernel_ms + rep.plan_ms + rep.train_ms
+            res["rounds"] += rep.probe.rounds + rep.planned.rounds
+            for part in (rep.probe, rep.planned):
+                res["ww"] += part.aborts_write_write
+                res["rw"] += part.aborts_read_write
+                res["age"] += part.aborts_data_age
+            last = (i, rep)
+    i, rep = last
+    perm, probe_rounds, _ = sched.plan(dev[i].n)
     sched.close()
     bank.close()
+    res["tx_s"] = res["commits"] / res["wall"]
+    res["abort_rate"] = res["aborts"] / max(1, res["aborts"] + res["commits"])
+    res["last_plan"] = (i, perm)
     return res
 
 
 def e2e_learned(torch, cg, host, s_addr, args, local, warm, timed):
     """Host buffers through the public calls: each step copies the batch's op/off arrays and its
-    range of the address array from pinned host memory, runs the scheduler (which returns the
-    statistics to the host) and is timed on the host clock."""
+    range of the address array from pinned host memory, runs the scheduler's probe and planned
+    runs, and copies every transaction's outcome and read-only result back to the host; timed on
+    the host clock."""
     bank = new_bank(cg, args, local, args.batch)
     sched = cg.Scheduler(n_accounts=N_ACCOUNTS, max_txn=args.batch, device=local, **SCHED)
     n = args.batch
@@ -263,7 +315,7 @@ def e2e_learned(torch, cg, host, s_addr, args, local, warm, timed):
     d_off = torch.empty(n, dtype=torch.int32, device="cuda")
     d_addr = torch.empty(s_addr.shape[0], dtype=torch.int32, device="cuda")
     h_addr = torch.from_numpy(s_addr.view(np.int32))
-    commits, wall, h2d = 0, 0.0, 0
+    commits, wall, h2d, d2h, checksum = 0, 0.0, 0, 0, 0
     for i in range(warm + timed):
         b = host[i]
         lo = int(b.off[0])
@@ -276,19 +328,31 @@ def e2e_learned(torch, cg, host, s_addr, args, local, warm, timed):
         torch.cuda.synchronize()
         ds = cg.BankStream(n, d_op.data_ptr(), d_off.data_ptr(), d_addr.data_ptr(),
                            int(s_addr.shape[0]))
-        rep = sched.run(bank, ds)
+        r1 = sched.probe(bank, ds)
+        out_bytes = 0
+        if r1.n_probe:
+            o1, res1 = bank.results(r1.n_probe)
+            out_bytes += o1.nbytes + res1.nbytes
+            checksum ^= int(res1.view(np.uint32).sum(dtype=np.uint64))
+        r2 = sched.plan_run(bank, ds)
+        o2, res2 = bank.results(r2.n_planned)
+        out_bytes += o2.nbytes + res2.nbytes
+        checksum ^= int(res2.view(np.uint32).sum(dtype=np.uint64))
         dt = time.perf_counter() - t0
         if i >= warm:
             wall += dt
-            commits += rep.commits
+            commits += r1.probe.commits + r2.planned.commits
             h2d += b.op.nbytes + b.off.nbytes + (hi - lo) * 4
+            d2h += out_bytes + 2 * 80  # results and the two runs' statistics
     sched.close()
     bank.close()
-    return commits, wall, h2d // max(1, timed)
+    return commits, wall, h2d // max(1, timed), d2h // max(1, timed)
 
 
-def hotspot_section(torch, cg, local):
-    """Learned vs plain on the shifting hotspot: 8 batches of 2^18 transactions."""
+def hotspot_section(torch, cg, args, local):
+    """Learned vs plain on the shifting hotspot: 8 batches of 2^18 transactions. Three arms: plain
+    (the reference's commit method, stream order), group commit in stream order, and the learned
+    scheduler with group commit; tx/s on the host clock with planning and training included."""
     chunk, count = 1 << 18, 8
     s, bs = generate_batches("hotspot", chunk, count, pinned=False, seed=3, pr_read_pct=10,
                              ro_reads=8, up_reads=2, hot_frac=0.01, hot_prob=0.3,
@@ -296,12 +360,13 @@ def hotspot_section(torch, cg, local):
     addr = torch.from_numpy(s.addr.view(np.int32)).cuda()
     dev = [DevBatch(torch, b) for b in bs]
     out = {}
-    for arm in ("plain", "learned"):
+    for arm, over, learned in (("plain", PLAIN, False), ("group_stream", ENGINE, False),
+                               ("learned", ENGINE, True)):
         bank = cg.Bank(n_accounts=N_ACCOUNTS, version_depth=8, client_warps=2, ctas=152,
-                       max_txn=chunk, log_commits=0, device=local)
+                       max_txn=chunk, log_commits=0, device=local, **over)
         bank.load()
-        sched = cg.Scheduler(n_accounts=N_ACCOUNTS, max_txn=chunk, device=local) \
-            if arm == "learned" else None
+        sched = cg.Scheduler(n_accounts=N_ACCOUNTS, max_txn=chunk, device=local, plan=1) \
+            if learned else None
         c = a = 0
         t = 0.0
         for d in dev:
@@ -328,10 +393,82 @@ def uniform_section(torch, cg, args, local):
     s, bs = generate_batches("uniform", args.batch, 4, pinned=False)
     addr = torch.from_numpy(s.addr.view(np.int32)).cuda()
     dev = [DevBatch(torch, b) for b in bs]
-    res, _ = run_plain(cg, dev, addr, s.addr.shape[0], args, local, 1, 3)
-    return {"tx_s": res["commits"] / (res["ms"] * 1e-3),
-            "abort_rate": res["aborts"] / (res["aborts"] + res["commits"]),
-            "workload": "same bank, uniform account choice, plain engine, 3 batches of 2^20"}
+    out = {}
+    for name, over in (("plain", PLAIN), ("group_commit", ENGINE)):
+        res, _ = run_engine(cg, dev, addr, s.addr.shape[0], args, local, [0, 1, 2, 3],
+                            log_commits=0, **over)
+        out[name] = {"tx_s": res["tx_s"], "abort_rate": res["abort_rate"]}
+    out["workload"] = "same bank, uniform account choice, engine alone, 3 batches of 2^20"
+    return out
+
+
+def c1_section(cg, local):
+    """The small bank of the reference's configuration: 4096 accounts at 1000, 8 blocks x 128
+    client threads, 256 transactions per thread (90 % two-account transfers of 1..10, 10 %
+    read-only sums of 8), version depth 4; host buffers, device time of the commit kernel."""
+    n = 8 * 128 * 256
+    w = cg.bank_workload(4096, n, seed=1, pr_read_pct=10, ro_reads=8, up_reads=2,
+                         kind=cg.KIND_TRANSFER, amt_lo=1, amt_hi=10, dist=cg.DIST_UNIFORM)
+    s = cg.generate(w)
+    out = {"workload": "4096 accounts, 8 x 128 client threads x 256 txn, 90/10, depth 4"}
+    for name, over in (("plain", dict(prevalidate=1)), ("group_commit", dict(prevalidate=3))):
+        with cg.Bank(n_accounts=4096, version_depth=4, ctas=8, client_warps=4, max_txn=n,
+                     log_commits=0, device=local, **over) as bank:
+            ms = []
+            for _ in range(4):
+                bank.load()
+                st = bank.run(s)
+                ms.append(st.kernel_ms)
+            ms = sorted(ms[1:])[1]
+            out[name] = {"tx_s": n / (ms * 1e-3), "abort_rate": st.abort_rate, "kernel_ms": ms}
+    return out
+
+
+VARIANT_CELLS = {
+    "stamp-cta-prevalidate": dict(validate=0, batch=2, prevalidate=1),
+    "stamp-warp-prevalidate": dict(validate=0, batch=1, prevalidate=1),
+    "stamp-lane-serverwb": dict(validate=0, batch=0, writeback=1, prevalidate=1),
+    "stamp-cta-chain": dict(validate=0, batch=2, prevalidate=2),
+    "stamp-cta-group": dict(validate=0, batch=2, prevalidate=3),
+    "stamp-cluster2": dict(validate=0, batch=3, cluster_size=2, prevalidate=1),
+    "stamp-cluster4": dict(validate=0, batch=3, cluster_size=4, prevalidate=1),
+    "stamp-cluster8": dict(validate=0, batch=3, cluster_size=8, prevalidate=1),
+    "stamp-cluster2-group": dict(validate=0, batch=3, cluster_size=2, prevalidate=3),
+    "ring-cta-client": dict(validate=1, batch=2, prevalidate=1),
+    "ring-warp-serverwb": dict(validate=1, batch=1, writeback=1, prevalidate=1),
+    "ring-lane-serverwb": dict(validate=1, batch=0, writeback=1, prevalidate=1),
+    "ringlane-warp-client": dict(validate=2, batch=1, prevalidate=1),
+    "ringlane-cta-client": dict(validate=2, batch=2, prevalidate=1),
+}
+
+
+def variants_section(cg, local):
+    """The engine's commit variants (the reference's sh / gb / ts storage forms map to the stamp
+    and ring protocols and the cluster form; vanilla / batchedAtrInsert / clientWriteback /
+    collabValidation to lane / warp / CTA batches, server write-back and the collaborative ring
+    scan) on the uniform bank (2^18 transactions) and the Zipf bank (2^15): committed tx/s
+    (device time) and abort rate per cell, 2 client warps per CTA, depth 8, host buffers."""
+    out = {"workload": "2^20 accounts r4/w2, 20% read-only scans of 32; uniform 2^18 txn, "
+                       "Zipf(0.99) 2^15 txn; 2 client warps x 152 CTAs (clusters: 4 warps)"}
+    for dist, n in (("uniform", 1 << 18), ("zipf", 1 << 15)):
+        s, bs = generate_batches(dist, n, 2, pinned=False)
+        rows = {}
+        for name, cell in VARIANT_CELLS.items():
+            cw = 4 if cell.get("batch") == 3 and cell.get("cluster_size", 2) <= 8 else 2
+            ctas = 152 if cell.get("batch") != 3 else 0
+            try:
+                with cg.Bank(n_accounts=N_ACCOUNTS, version_depth=8, client_warps=cw, ctas=ctas,
+                             max_txn=n, log_commits=0, device=local, max_reads=4, **cell) as bank:
+                    bank.load()
+                    bank.run(bs[0])  # warm-up
+                    st = bank.run(bs[1])
+                    rows[name] = {"tx_s": n / (st.kernel_ms * 1e-3), "abort_rate": st.abort_rate}
+            except Exception as e:
+                rows[name] = {"error": f"{type(e).__name__}: {e}"}
+            if time.perf_counter() - T_START > 900:
+                break
+        out[dist] = rows
+    return out
 
 
 def memcd_section(cg, local, n_batches=40):
@@ -498,21 +635,38 @@ def workload_name(args):
             f"of 32; 2^24-txn stream in batches of {args.batch}")
 
 
+def oracle_batches(args, count):
+    """The same batches from the oracle's own generator (so this arm loads no library of the
+    product)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as orc
+    dist_id = {"uniform": 0, "zipf": 1, "hotspot": 2}[args.dist]
+    d = dict(WORKLOAD)
+    w = orc.Workload(seed=d["seed"], n_accounts=N_ACCOUNTS, n_txn=args.batch * count,
+                     pr_read_pct=d["pr_read_pct"], ro_reads=d["ro_reads"],
+                     up_reads=d["up_reads"], kind=1, amt_lo=d["amt_lo"], amt_hi=d["amt_hi"],
+                     dist=dist_id, zipf_theta=d["zipf_theta"], hot_frac=0.01, hot_prob=0.3,
+                     shift_every=1 << 20)
+    op, off, addr = orc.generate(w)
+    b = args.batch
+    return [(op[i * b:(i + 1) * b], off[i * b:(i + 1) * b], addr) for i in range(count)]
+
+
 def run_reference(args, rank, world):
     """Reference arm: the path's CPU execution (oracle port, striped locks, all host threads)."""
     if rank != 0:
         return
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as orc
-    s, bs = generate_batches(args.dist, args.batch, args.warmup + args.steps, pinned=False)
+    bs = oracle_batches(args, args.warmup + args.steps)
     vals = np.full(N_ACCOUNTS, 1000, np.int32)
     threads = orc.cpu_threads()
     t, commits = 0.0, 0
-    for i, b in enumerate(bs):
-        vals, ns = orc.locked(b.op, b.off, b.addr, N_ACCOUNTS, vals, threads)
+    for i, (op, off, addr) in enumerate(bs):
+        vals, ns = orc.locked(op, off, addr, N_ACCOUNTS, vals, threads)
         if i >= args.warmup:
             t += ns * 1e-9
-            commits += b.n_txn
+            commits += op.shape[0]
     v = commits / t
     print(json.dumps({
         "impl": "reference", "metric": "committed tx/s", "value": v, "unit": "committed tx/s",
@@ -535,19 +689,21 @@ def run_case(args, local):
 
     import csmv_gb300 as cg
     torch.cuda.set_device(local)
-    if args.case in ("engine", "serial", "flow", "sched"):
+    n = args.case_txn
+    if args.case in ("engine", "group", "serial", "flow", "sched"):
         dist = "uniform" if args.case == "engine" else "zipf"
-        n = (1 << 15) if args.case == "serial" else (1 << 18)
         s, bs = generate_batches(dist, n, 2, pinned=False)
         addr = torch.from_numpy(s.addr.view(np.int32)).cuda()
         dev = [DevBatch(torch, b) for b in bs]
-        bank = new_bank(cg, args, local, n)
-        if args.case == "sched":
-            sched = cg.Scheduler(n_accounts=N_ACCOUNTS, max_txn=n, device=local, **SCHED)
-            for d in dev:
+        over = PLAIN if args.case == "engine" else {}
+        bank = new_bank(cg, args, local, n, log_commits=0, **over)
+        if args.case in ("sched", "group"):
+            sched = cg.Scheduler(n_accounts=N_ACCOUNTS, max_txn=n, device=local,
+                                 **dict(SCHED, probe_every=1))
+            for d in dev:  # a warm-up chunk, then the profiled one
                 r = sched.run(bank, d.stream(cg, addr, s.addr.shape[0]))
             sched.close()
-            out = {"case": "sched", "commits": r.commits}
+            out = {"case": args.case, "commits": r.commits, "planned_ms": r.planned.kernel_ms}
         else:
             run = {"engine": bank.run_device, "serial": bank.run_serial_device,
                    "flow": bank.run_flow_device}[args.case]
@@ -556,7 +712,6 @@ def run_case(args, local):
             out = {"case": args.case, "commits": st.commits, "kernel_ms": st.kernel_ms}
         bank.close()
     elif args.case == "mlp":
-        n = 1 << 18
         rng = np.random.default_rng(0)
         x = (rng.random((n, 64)) < 0.2).astype(np.float32)
         bits = (x.view(np.uint32) >> 16).astype(np.uint16).view(np.int16)  # 0/1 exact in bf16
@@ -606,43 +761,62 @@ def main():
         sample = cg.Stream(np.ascontiguousarray(host[0].op[:1 << 16]),
                            np.ascontiguousarray(host[0].off[:1 << 16]), host[0].addr)
         best, trials = cg.autotune(sample, repeats=2, n_accounts=N_ACCOUNTS, init_value=1000,
-                                   device=local)
+                                   device=local, **ENGINE)
         args.client_warps, args.ctas, args.depth = best.client_warps, best.ctas, best.version_depth
         tuned = {"client_warps": best.client_warps, "ctas": best.ctas,
                  "version_depth": best.version_depth, "candidates": len(trials),
                  "sample_txn": 1 << 16}
-    barrier(world)
-    progress("plain arm")
-    plain, info = run_plain(cg, dev, addr_dev, n_addr, args, local, warm, timed)
+    atomics = cg.measure_atomics(local)
     barrier(world)
     progress("learned arm")
     with ClockSampler(local) as clk:
         learned = run_learned(torch, cg, dev, addr_dev, n_addr, args, local, warm, timed)
     barrier(world)
-    progress("e2e")
     t_learned = reduce_max(learned["wall"], world)
     value = learned["commits"] * world / t_learned
-    t_plain = reduce_max(plain["ms"] * 1e-3, world)
-    e_commits, e_wall, h2d = e2e_learned(torch, cg, host, np.asarray(s.addr), args, local, warm,
-                                         timed)
+    progress("e2e")
+    e_commits, e_wall, h2d, d2h = e2e_learned(torch, cg, host, np.asarray(s.addr), args, local,
+                                              warm, timed)
     e2e = e_commits * world / reduce_max(e_wall, world)
+    progress("comparison arms")
+    n_cmp = min(warm + timed, 4)
+    group_stream, info = run_engine(cg, dev, addr_dev, n_addr, args, local, list(range(n_cmp)),
+                                    log_commits=0)
+    plain, _ = run_engine(cg, dev, addr_dev, n_addr, args, local, list(range(min(n_cmp, 3))),
+                          log_commits=0, **PLAIN)
     if rank != 0:
         return
     pk, pk_kind = peaks()
-    # roofline of the dominant part of the learned step, the dataflow lane (its execution
-    # kernel holds nearly all of the lane's device time): algorithmic bytes of the transfers it
-    # committed over the lane's device time
-    s_ms = learned["serial_ms"]
-    achieved = learned["serial_txn"] * B_UPDATE / (s_ms * 1e-3) / 1e9 if s_ms > 0 else 0.0
+    # roofline of the engine on this workload (the bounds of the survey's measurement row):
+    #  - throughput bound min(BW_eff / B_tx, R_atomic / A_tx): HBM bytes of a transaction's
+    #    versioned reads and writes, and the atomics a committed transfer needs (a lock CAS per
+    #    written account, plus the group's timestamp draw and completion bits per 32)
+    #  - chain bound: the busiest account's lock passes through L_max rounds of the plan, each
+    #    with at least TRIPS_PER_HOLD dependent L2 round trips of cas_chain_ns each
+    i_last, perm = learned["last_plan"]
+    b = host[i_last]
+    probe_n = b.n_txn - len(perm)
+    order = np.concatenate([np.arange(probe_n), perm.astype(np.int64)])
+    l_max, hot_acct, upd_rounds = plan_lock_rounds(b.op, b.off, b.addr, order)
+    l_plain, _, _ = plan_lock_rounds(b.op, b.off, b.addr, np.arange(b.n_txn))
+    steps_t = timed
+    per_step_txn = learned["commits"] / steps_t
+    frac_upd = 0.8
+    a_tx = 2.0 * frac_upd + 3.0 / 32.0
+    b_tx = frac_upd * B_UPDATE + (1 - frac_upd) * B_RO
+    bound_atomic = atomics["spread_per_s"] / a_tx
+    bound_hbm = pk["hbm_gbs"] * 1e9 / b_tx
+    bound_tp = min(bound_atomic, bound_hbm)
+    chain_s = l_max * TRIPS_PER_HOLD * atomics["cas_chain_ns"] * 1e-9
+    bound_chain = per_step_txn / chain_s
+    achieved_atomic = value * a_tx
     traffic = None
     tr = ROOT / "profiles" / "traffic.json"
     if tr.exists():
         try:
-            traffic = json.loads(tr.read_text()).get("flow_exec_kernel_bytes_per_launch")
+            traffic = json.loads(tr.read_text()).get("bank_kernel_learned_bytes_per_launch")
         except Exception:
             traffic = None
-    plain_gbs = (plain["upd"] * B_UPDATE + plain["ro"] * B_RO) / (plain["ms"] * 1e-3) / 1e9
-    l_abort = learned["aborts"] / max(1, learned["aborts"] + learned["commits"])
     line = {
         "metric": "committed tx/s", "value": value, "unit": "committed tx/s", "n_gpus": world,
         "steps": timed, "warmup": warm, "ms_per_step": t_learned / timed * 1e3,
@@ -650,32 +824,53 @@ def main():
         "data": "synthetic (seeded generator with the configured shapes)",
         "config": {"workload": workload_name(args), "l2": "inputs larger than L2 (28 MB/batch)",
                    "ctas": info["ctas"], "threads_per_cta": info["threads_per_cta"],
-                   "version_depth": args.depth, "autotuned": tuned, "scheduler": SCHED,
-                   "parallelism": f"replicas x{world}"},
-        "abort_rate": l_abort,
-        "learned": {"tx_s": value, "abort_rate": l_abort,
-                    "dataflow_lane_txn_per_step": learned["serial_txn"] // timed,
-                    "dataflow_lane_ms_per_step": learned["serial_ms"] / timed,
+                   "version_depth": args.depth, "engine": ENGINE, "autotuned": tuned,
+                   "scheduler": SCHED, "parallelism": f"replicas x{world}"},
+        "abort_rate": learned["abort_rate"],
+        "learned": {"tx_s": value, "abort_rate": learned["abort_rate"],
+                    "engine_validated": "every transaction: locks, server timestamps, validation",
+                    "flagged_per_step": learned["flagged"] / timed,
+                    "aborts_by_kind": {"lock_wait_gave_up": learned["ww"],
+                                       "read_validation": learned["rw"],
+                                       "data_age": learned["age"]},
                     "plan_ms_per_step": learned["plan_ms"] / timed,
-                    "train_ms_per_step": learned["train_ms"] / timed},
-        "plain": {"tx_s": plain["commits"] * world / t_plain,
-                  "abort_rate": plain["aborts"] / max(1, plain["aborts"] + plain["commits"]),
-                  "roofline_frac_of_measured_hbm": plain_gbs / pk["hbm_gbs"]},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
-                     "kernel": "flow_exec_kernel (dataflow lane)", "peak_source": pk_kind,
-                     "bytes_per_txn": B_UPDATE},
+                    "train_ms_per_step": learned["train_ms"] / timed,
+                    "engine_ms_per_step": learned["engine_ms"] / timed,
+                    "device_ms_per_step": learned["device_ms"] / timed},
+        "plain": {"tx_s": plain["tx_s"] * world, "abort_rate": plain["abort_rate"],
+                  "method": "reference commit method: per-transaction validation, pre-validation, "
+                            "CTA-batched timestamps", "steps": plain["steps"]},
+        "group_stream": {"tx_s": group_stream["tx_s"] * world,
+                         "abort_rate": group_stream["abort_rate"], "steps": group_stream["steps"],
+                         "method": "group commit in stream order, no scheduler"},
+        "roofline": {"bound": "l2_atomic", "achieved": achieved_atomic,
+                     "peak": atomics["spread_per_s"], "unit": "atomic/s",
+                     "frac": achieved_atomic / atomics["spread_per_s"], "traffic": traffic,
+                     "peak_source": "measured by csmv_measure_atomics in this run",
+                     "kernel": "bank_kernel (group commit)", "atomics_per_txn": a_tx,
+                     "throughput_bound_tx_s": bound_tp,
+                     "throughput_frac": value / bound_tp,
+                     "hbm": {"bytes_per_txn": b_tx, "achieved_gbs": value * b_tx / 1e9,
+                             "peak_gbs": pk["hbm_gbs"], "frac": value * b_tx / 1e9 / pk["hbm_gbs"],
+                             "peak_source": pk_kind},
+                     "chain": {"busiest_account": hot_acct, "rounds_locking_it": l_max,
+                               "rounds_locking_it_stream_order": l_plain,
+                               "update_rounds": upd_rounds, "trips_per_hold": TRIPS_PER_HOLD,
+                               "cas_round_trip_ns": atomics["cas_chain_ns"],
+                               "bound_tx_s": bound_chain, "frac": value / bound_chain}},
+        "atomics": atomics,
         "e2e": {"value": e2e, "unit": "committed tx/s", "h2d_bytes_per_step": h2d,
-                # per engine or lane run: statistics (80 B) + commit-order words (768 B); up to
-                # three runs per step, the scheduler's 16 B of plan sizes and loss, and the
-                # dataflow lane's 8 B of access count and widest transfer
-                "d2h_bytes_per_step": 3 * (80 + 768) + 16 + 8},
+                "d2h_bytes_per_step": d2h},
         "gpu_launches": learned["launches"],
         "clocks": clk.summary(),
     }
     if not args.no_extras:
-        sections = [("hotspot", lambda: hotspot_section(torch, cg, local)),
+        sections = [("hotspot", lambda: hotspot_section(torch, cg, args, local)),
                     ("uniform", lambda: uniform_section(torch, cg, args, local)),
+                    ("c1", lambda: c1_section(cg, local)),
+                    ("dataflow_lane", lambda: dataflow_section(torch, cg, dev, addr_dev, n_addr,
+                                                               args, local)),
+                    ("variants", lambda: variants_section(cg, local)),
                     ("memcd", lambda: memcd_section(cg, local)),
                     ("serving", lambda: serve_section(cg, local))]
         for name, fn in sections:
@@ -688,6 +883,19 @@ def main():
         progress("cpu baseline")
         line["cpu_baseline"] = cpu_baseline(host)
     print(json.dumps(line))
+
+
+def dataflow_section(torch, cg, dev, addr_dev, n_addr, args, local):
+    """The earlier learned path, kept as a labelled comparison: transfers the scheduler flags are
+    deferred to the dataflow lane, which executes them in stream order WITHOUT locks, server
+    timestamps or validation (exact by construction, not CSMV); the rest go through the engine."""
+    timed = min(3, len(dev) - 1)
+    res = run_learned(torch, cg, dev, addr_dev, n_addr, args, local, 1, timed,
+                      sched_cfg=FLOW, bank_over=dict(flow_warps=8, log_commits=0))
+    return {"tx_s": res["tx_s"], "abort_rate": res["abort_rate"],
+            "lane_txn_per_step": res["serial_txn"] / timed,
+            "lane_ms_per_step": res["serial_ms"] / timed,
+            "validated": "no: the lane's transactions bypass the engine's validation"}
 
 
 if __name__ == "__main__":

@@ -479,6 +479,14 @@ class Bank:
                "csmv_bank_read_groups")
         return out
 
+    def results(self, n_txn: int):
+        """Per-transaction outcomes and read-only results of the last run (no commit log)."""
+        outcome = np.empty(n_txn, np.uint32)
+        result = np.empty(n_txn, np.int32)
+        _check(lib().csmv_bank_read_log(self._h, None, 0, _ptr(outcome), _ptr(result), n_txn),
+               "csmv_bank_read_log")
+        return outcome, result
+
     def device_info(self) -> dict:
         a, b, c_, d = C.c_int(), C.c_int(), C.c_int(), C.c_size_t()
         _check(lib().csmv_bank_device_info(self._h, C.byref(a), C.byref(b), C.byref(c_),
