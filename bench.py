@@ -303,6 +303,22 @@ def run_learned(torch, cg, dev, addr_dev, n_addr, args, local, warm, timed, sche
     return res
 
 
+def tune_learned(torch, cg, dev, addr_dev, n_addr, args, local):
+    """Client warps per CTA x versions per account for the learned arm: each candidate runs the
+    whole arm (probe, plan, group commit) on batch 0 (warm-up) and batch 1 (timed); the fastest
+    is kept in args. The grid stays one CTA per SM."""
+    trials = []
+    for cw, depth in ((1, 8), (2, 8), (1, 4), (2, 4)):
+        args.client_warps, args.depth = cw, depth
+        r = run_learned(torch, cg, dev, addr_dev, n_addr, args, local, 1, 1)
+        trials.append({"client_warps": cw, "version_depth": depth, "tx_s": r["tx_s"]})
+    best = max(trials, key=lambda t: t["tx_s"])
+    args.client_warps, args.depth = best["client_warps"], best["version_depth"]
+    return {"client_warps": best["client_warps"], "ctas": args.ctas,
+            "version_depth": best["version_depth"], "trials": trials,
+            "sample": "the learned arm on batches 0 (warm-up) and 1"}
+
+
 def e2e_learned(torch, cg, host, s_addr, args, local, warm, timed):
     """Host buffers through the public calls: each step copies the batch's op/off arrays and its
     range of the address array from pinned host memory, runs the scheduler's probe and planned
@@ -353,7 +369,7 @@ def hotspot_section(torch, cg, args, local):
     """Learned vs plain on the shifting hotspot: 8 batches of 2^18 transactions. Three arms: plain
     (the reference's commit method, stream order), group commit in stream order, and the learned
     scheduler with group commit; tx/s on the host clock with planning and training included."""
-    chunk, count = 1 << 18, 8
+    chunk, count = 1 << 20, 6
     s, bs = generate_batches("hotspot", chunk, count, pinned=False, seed=3, pr_read_pct=10,
                              ro_reads=8, up_reads=2, hot_frac=0.01, hot_prob=0.3,
                              shift_every=1 << 20)
@@ -369,7 +385,7 @@ def hotspot_section(torch, cg, args, local):
             if learned else None
         c = a = 0
         t = 0.0
-        for d in dev:
+        for j, d in enumerate(dev):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             if sched is None:
@@ -379,13 +395,17 @@ def hotspot_section(torch, cg, args, local):
                 r = sched.run(bank, d.stream(cg, addr, s.addr.shape[0]))
                 c, a = c + r.commits, a + r.aborts
             torch.cuda.synchronize()
+            if j == 0:  # warm-up
+                c = a = 0
+                continue
             t += time.perf_counter() - t0
         if sched is not None:
             sched.close()
         bank.close()
         out[arm] = {"tx_s": c / t, "abort_rate": a / (a + c)}
     out["workload"] = ("2^20 accounts, 1% hot set drawing 30% of the accesses, moving every 2^20 "
-                       "txn; 90% 2-account transfers, 10% read-only sums of 8; 8 batches of 2^18")
+                       "txn; 90% 2-account transfers, 10% read-only sums of 8; batches of 2^20, "
+                       "one warm-up and 5 timed")
     return out
 
 
@@ -460,13 +480,17 @@ def variants_section(cg, local):
                 with cg.Bank(n_accounts=N_ACCOUNTS, version_depth=8, client_warps=cw, ctas=ctas,
                              max_txn=n, log_commits=0, device=local, max_reads=4, **cell) as bank:
                     bank.load()
-                    bank.run(bs[0])  # warm-up
-                    st = bank.run(bs[1])
-                    rows[name] = {"tx_s": n / (st.kernel_ms * 1e-3), "abort_rate": st.abort_rate}
+                    # warm-up on 2^12 transactions; the timed run is sized to about 0.3 s of
+                    # this cell's rate (the slow ring-scan cells run a shorter prefix)
+                    st = bank.run(cg.Stream(bs[0].op[:4096], bs[0].off[:4096], bs[0].addr))
+                    rate = 4096 / max(st.kernel_ms * 1e-3, 1e-6)
+                    m = int(min(n, max(4096, rate * 0.3))) // 32 * 32
+                    st = bank.run(cg.Stream(np.ascontiguousarray(bs[1].op[:m]),
+                                            np.ascontiguousarray(bs[1].off[:m]), bs[1].addr))
+                    rows[name] = {"tx_s": m / (st.kernel_ms * 1e-3), "abort_rate": st.abort_rate,
+                                  "txn": m}
             except Exception as e:
                 rows[name] = {"error": f"{type(e).__name__}: {e}"}
-            if time.perf_counter() - T_START > 900:
-                break
         out[dist] = rows
     return out
 
@@ -756,16 +780,9 @@ def main():
     dev = [DevBatch(torch, b) for b in host]
 
     tuned = None
-    if not args.no_tune:  # the engine's launch shape for this workload, measured on a sample
-        progress("autotune")
-        sample = cg.Stream(np.ascontiguousarray(host[0].op[:1 << 16]),
-                           np.ascontiguousarray(host[0].off[:1 << 16]), host[0].addr)
-        best, trials = cg.autotune(sample, repeats=2, n_accounts=N_ACCOUNTS, init_value=1000,
-                                   device=local, **ENGINE)
-        args.client_warps, args.ctas, args.depth = best.client_warps, best.ctas, best.version_depth
-        tuned = {"client_warps": best.client_warps, "ctas": best.ctas,
-                 "version_depth": best.version_depth, "candidates": len(trials),
-                 "sample_txn": 1 << 16}
+    if not args.no_tune:  # the learned arm's launch shape, measured on the first two batches
+        progress("tune")
+        tuned = tune_learned(torch, cg, dev, addr_dev, n_addr, args, local)
     atomics = cg.measure_atomics(local)
     barrier(world)
     progress("learned arm")

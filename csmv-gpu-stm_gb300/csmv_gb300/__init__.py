@@ -51,7 +51,7 @@ class BankStream(C.Structure):
     _fields_ = [("n_txn", C.c_uint32), ("op", C.c_void_p), ("off", C.c_void_p),
                 ("addr", C.c_void_p), ("n_addr", C.c_uint64), ("txn_aborts", C.c_void_p),
                 ("split_round", C.c_uint32), ("deferred_warps", C.c_uint32),
-                ("backoff", C.c_void_p), ("txn_waits", C.c_void_p)]
+                ("backoff", C.c_void_p), ("txn_waits", C.c_void_p), ("lock_last", C.c_void_p)]
 
 
 class BankConfig(C.Structure):
@@ -118,7 +118,7 @@ class TuneResult(C.Structure):
 class ServeConfig(C.Structure):
     _fields_ = [(n, C.c_uint32) for n in ("n_sets", "client_warps", "ctas", "arena_requests",
                                           "max_inflight_sets", "idle_timeout_ms")] + [
-        ("device", C.c_int32)]
+        ("device", C.c_int32), ("log_cap", C.c_uint32)]
 
 
 class SchedConfig(C.Structure):
@@ -128,7 +128,8 @@ class SchedConfig(C.Structure):
                 ("lr", C.c_float), ("threshold", C.c_float), ("defer_threshold", C.c_float),
                 ("deferred_warps", C.c_uint32), ("serial_lane", C.c_uint32),
                 ("seed", C.c_uint64), ("device", C.c_int32), ("plan", C.c_uint32),
-                ("hot_count", C.c_uint32), ("score", C.c_uint32), ("backoff_ns", C.c_uint32)]
+                ("hot_count", C.c_uint32), ("score", C.c_uint32), ("backoff_ns", C.c_uint32),
+                ("hot_last", C.c_uint32)]
 
 
 class SchedReport(C.Structure):
@@ -212,6 +213,10 @@ def lib() -> C.CDLL:
         "csmv_serve_submit": (I32, [P, C.POINTER(MemcdBatch), C.POINTER(C.c_uint64)]),
         "csmv_serve_poll": (I32, [P, C.c_uint64, C.POINTER(C.c_uint32), P, P,
                                   C.POINTER(C.c_uint64)]),
+        "csmv_serve_poll_logged": (I32, [P, C.c_uint64, C.POINTER(C.c_uint32), P, P, P,
+                                         C.POINTER(C.c_uint64)]),
+        "csmv_serve_read_log": (I32, [P, P, C.c_uint32, C.POINTER(C.c_uint32),
+                                      C.POINTER(C.c_uint32)]),
         "csmv_serve_stop": (I32, [P, C.POINTER(Stats)]),
         "csmv_serve_read_table": (I32, [P, P, P]),
         "csmv_serve_destroy": (None, [P]),
@@ -408,11 +413,12 @@ class Bank:
 
     def run(self, stream: Stream, txn_aborts: np.ndarray | None = None, split_round: int = 0,
             deferred_warps: int = 0, backoff: np.ndarray | None = None,
-            txn_waits: np.ndarray | None = None) -> Stats:
+            txn_waits: np.ndarray | None = None, lock_last: np.ndarray | None = None) -> Stats:
         """Host buffers in: copies the stream to the device inside the call. txn_aborts (uint32
         [n_txn]) receives each transaction's failed attempts; split_round/deferred_warps set
         up the deferred queue; backoff (uint32 [n_txn], ns) bounds each transaction's pause
-        before a retry (csmv_bank_stream)."""
+        before a retry; lock_last (uint8 [n_accounts]) gives group commit's heat classes
+        (csmv_bank_stream)."""
         st = Stats()
         s = stream.c_struct()
         if txn_aborts is not None:
@@ -424,6 +430,9 @@ class Bank:
         if txn_waits is not None:
             assert txn_waits.dtype == np.uint32 and txn_waits.shape[0] >= stream.n_txn
             s.txn_waits = _ptr(txn_waits)
+        if lock_last is not None:
+            assert lock_last.dtype == np.uint8 and lock_last.shape[0] == self.cfg.n_accounts
+            s.lock_last = _ptr(lock_last)
         s.split_round, s.deferred_warps = split_round, deferred_warps
         rc = lib().csmv_bank_run(self._h, C.byref(s), C.byref(st))
         self.last_stats = st
@@ -691,20 +700,36 @@ class Server:
         self._sizes[bid.value] = req.n_req
         return bid.value
 
-    def poll(self, batch_id: int, results: bool = True):
-        """None while running; else (found, val_out, device_ns) (arrays None if not asked)."""
+    def poll(self, batch_id: int, results: bool = True, outcome: bool = False):
+        """None while running; else (found, val_out, device_ns) (arrays None if not asked), and
+        with outcome=True (log_cap > 0) (found, val_out, outcome, device_ns)."""
         n = self._sizes[batch_id]
         done = C.c_uint32()
         ns = C.c_uint64()
         found = np.empty(n, np.uint32) if results else None
         out = np.empty((n, 8), np.uint32) if results else None
-        _check(lib().csmv_serve_poll(self._h, batch_id, C.byref(done),
-                                     _ptr(found) if results else None,
-                                     _ptr(out) if results else None, C.byref(ns)),
-               "csmv_serve_poll")
+        oc = np.empty(n, np.uint32) if outcome else None
+        _check(lib().csmv_serve_poll_logged(self._h, batch_id, C.byref(done),
+                                            _ptr(found) if results else None,
+                                            _ptr(out) if results else None,
+                                            _ptr(oc) if outcome else None, C.byref(ns)),
+               "csmv_serve_poll_logged")
         if not done.value:
             return None
+        if outcome:
+            return found, out, oc, ns.value
         return found, out, ns.value
+
+    def log(self):
+        """(log_txn, base_ts) of the last session (log_cap > 0): log_txn[k] is the arena index of
+        the request that committed with timestamp base_ts + k + 1 (HOLE for a hole)."""
+        used, base = C.c_uint32(), C.c_uint32()
+        _check(lib().csmv_serve_read_log(self._h, None, 0, C.byref(used), C.byref(base)),
+               "csmv_serve_read_log")
+        log = np.empty(max(1, used.value), np.uint32)
+        _check(lib().csmv_serve_read_log(self._h, _ptr(log), log.shape[0], C.byref(used),
+                                         C.byref(base)), "csmv_serve_read_log")
+        return log[:used.value], base.value
 
     def stop(self) -> Stats:
         st = Stats()

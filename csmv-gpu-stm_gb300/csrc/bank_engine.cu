@@ -88,6 +88,7 @@ static csmv_status validate_config(const csmv_bank_config* c) {
   };
   if (!c) return bad("null");
   if (c->n_accounts < 2) return bad("n_accounts < 2");
+  if (c->n_accounts >= 0x80000000u) return bad("n_accounts >= 2^31");
   if (!pick_kernel(c->version_depth)) return bad("version_depth must be 2, 4, 8 or 16");
   if (c->ring_size < 64 || (c->ring_size & (c->ring_size - 1))) return bad("ring_size");
   if (c->client_warps < 1 || c->client_warps > (uint32_t)kMaxClientWarps) return bad("client_warps");
@@ -131,6 +132,7 @@ static void free_all(csmv_bank_t* h) {
   cudaFree(h->d_aborts);
   cudaFree(h->d_backoff);
   cudaFree(h->d_waits);
+  cudaFree(h->d_lock_last);
   cudaFree(h->grp);
   cudaFree(h->tk);
   flow_scratch_free(h->flow);
@@ -288,7 +290,16 @@ csmv_status csmv::check_stream(const csmv_bank_t* h, const csmv_bank_stream* s) 
     set_error("stream: split_round must be <= n_txn/32, with deferred_warps > 0");
     return CSMV_ERR_INVALID_ARG;
   }
+  if (s->lock_last && !(h->cfg.prevalidate == 3 && h->cfg.validate == CSMV_VALIDATE_STAMP)) {
+    set_error("stream: lock_last orders the locks of group commit (prevalidate 3, stamp protocol)");
+    return CSMV_ERR_INVALID_ARG;
+  }
   return CSMV_OK;
+}
+
+bool csmv::bank_group_commit(const csmv_bank_t* h, uint32_t* n_accounts) {
+  *n_accounts = h->cfg.n_accounts;
+  return h->cfg.prevalidate == 3 && h->cfg.validate == CSMV_VALIDATE_STAMP;
 }
 
 BankParams csmv::bank_params(const csmv_bank_t* h, const uint32_t* op, const uint32_t* off,
@@ -321,7 +332,7 @@ BankParams csmv::bank_params(const csmv_bank_t* h, const uint32_t* op, const uin
   p.prevalidate = c.prevalidate;
   p.spin_log2 = c.spin_limit_log2;
   p.txn_aborts = txn_aborts;
-  p.grp = (c.log_commits && c.prevalidate == 3 && c.validate == CSMV_VALIDATE_STAMP) ? h->grp : nullptr;
+  p.grp = (c.log_commits && c.prevalidate >= 2 && c.validate == CSMV_VALIDATE_STAMP) ? h->grp : nullptr;
   p.tk = h->tk;
   return p;
 }
@@ -382,12 +393,14 @@ csmv_status csmv::bank_end_run(csmv_bank_t* h, uint32_t n_txn, csmv_stats* out) 
 static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* off,
                           const uint32_t* addr, uint32_t n_txn, uint32_t* txn_aborts,
                           uint32_t split_round, uint32_t deferred_warps, const uint32_t* backoff,
-                          uint32_t* txn_waits, csmv_stats* out, bool serial = false) {
+                          uint32_t* txn_waits, const uint8_t* lock_last, csmv_stats* out,
+                          bool serial = false) {
   const csmv_bank_config& c = h->cfg;
   BankParams p = bank_params(h, op, off, addr, n_txn, txn_aborts);
   p.split_round = split_round;
   p.deferred_warps = deferred_warps;
   p.backoff = backoff;
+  p.lock_last = serial ? nullptr : lock_last;
   p.txn_waits = txn_waits;
   if (txn_waits && (serial || c.prevalidate != 3))  // only group commit waits on locks
     CSMV_CUDA(cudaMemsetAsync(txn_waits, 0, (size_t)n_txn * 4, h->stream));
@@ -435,7 +448,7 @@ extern "C" csmv_status csmv_bank_run_device(csmv_bank_t* h, const csmv_bank_stre
   CSMV_CUDA(cudaSetDevice(h->cfg.device));
   auto t0 = std::chrono::steady_clock::now();
   st = launch(h, s->op, s->off, s->addr, s->n_txn, s->txn_aborts, s->split_round,
-              s->deferred_warps, s->backoff, s->txn_waits, out);
+              s->deferred_warps, s->backoff, s->txn_waits, s->lock_last, out);
   if (out)
     out->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return st;
@@ -457,7 +470,7 @@ extern "C" csmv_status csmv_bank_run_serial_device(csmv_bank_t* h, const csmv_ba
   CSMV_CUDA(cudaSetDevice(h->cfg.device));
   auto t0 = std::chrono::steady_clock::now();
   st = launch(h, s->op, s->off, s->addr, s->n_txn, s->txn_aborts, 0, 0, nullptr, s->txn_waits,
-              out, true);
+              nullptr, out, true);
   if (out)
     out->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return st;
@@ -486,9 +499,14 @@ extern "C" csmv_status csmv_bank_run(csmv_bank_t* h, const csmv_bank_stream* s, 
   if (s->backoff)
     CSMV_CUDA(cudaMemcpyAsync(h->d_backoff, s->backoff, (size_t)s->n_txn * 4,
                               cudaMemcpyHostToDevice, h->stream));
+  if (s->lock_last) {
+    if (!h->d_lock_last) CSMV_CUDA(cudaMalloc(&h->d_lock_last, h->cfg.n_accounts));
+    CSMV_CUDA(cudaMemcpyAsync(h->d_lock_last, s->lock_last, h->cfg.n_accounts,
+                              cudaMemcpyHostToDevice, h->stream));
+  }
   st = launch(h, h->d_op, h->d_off, h->d_addr, s->n_txn, s->txn_aborts ? h->d_aborts : nullptr,
               s->split_round, s->deferred_warps, s->backoff ? h->d_backoff : nullptr,
-              s->txn_waits ? h->d_waits : nullptr, out);
+              s->txn_waits ? h->d_waits : nullptr, s->lock_last ? h->d_lock_last : nullptr, out);
   if (st == CSMV_OK && (s->txn_aborts || s->txn_waits)) {
     if (s->txn_aborts)
       CSMV_CUDA(cudaMemcpyAsync(s->txn_aborts, h->d_aborts, (size_t)s->n_txn * 4,

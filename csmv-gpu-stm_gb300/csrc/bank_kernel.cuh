@@ -104,6 +104,9 @@ struct BankParams {
                             // lock another warp held (group commit)
   uint32_t* tk;             // group commit: per account {next ticket, ticket served} of its
                             // lock's wait queue
+  const uint8_t* lock_last;  // group commit, optional [n_items]: heat class of each account
+                             // (0 = none); classed accounts are locked after all others, the
+                             // hottest last
   const uint32_t* backoff;  // optional [n_rounds*32]: longest pause (ns) before a retry of each
                             // transaction (a scheduler's per-transaction backoff)
 };
@@ -373,54 +376,69 @@ __device__ __forceinline__ bool group_cas_lock(unsigned long long* cw, uint32_t 
   return false;
 }
 
-// Waits for account x's lock and takes it, with the account's version slots (ed) and latest value
-// (v) read as the lock is taken. Waiters queue first-come first-served on the account's ticket
-// pair (tk[2x] = next ticket, tk[2x + 1] = ticket being served): a warp takes a ticket, waits
-// until it is served, then takes the lock as soon as its holder releases it and serves the next
-// ticket - so only the head of the queue polls the commit word, and a waiter far from the
+// Lock queues. Waiters for account x queue first-come first-served on the account's ticket pair
+// (tk[2x] = next ticket, tk[2x + 1] = ticket being served): a warp takes a ticket, waits until it
+// is served (its turn), then takes the lock as soon as its holder releases it, and serves the
+// next ticket - so only the head of the queue polls the commit word, and a waiter far from the
 // account's L2 slice is not overtaken forever by nearer ones (a plain polling race hands a hot
 // lock to whoever sees the release first). A round's fast path (group_cas_lock) may still take a
-// free lock ahead of the queue. The poll that finds the lock free is an acquire load, so the
-// slots loaded after it hold the version of the stamp it saw, and a CAS that succeeds at that
-// stamp proves them current (*stale stays false). A waiter never leaves the queue while its run
-// is healthy (the tickets behind it would wait forever): the waits are bounded only by the
-// device error word and by 2^spin_log2 polls, after which the run fails with ERR_WAIT_TURN.
-template <int DEPTH>
-__device__ __forceinline__ bool group_wait_lock(const BankParams& p, uint32_t x, uint32_t me,
-                                                uint32_t& stamp, bool& stale,
-                                                SlotEditor<DEPTH>& ed, int32_t& v) {
+// free lock ahead of the queue. A waiter never leaves the queue while its run is healthy (the
+// tickets behind it would wait forever): the waits are bounded only by the device error word and
+// by 2^spin_log2 polls, after which the run fails with ERR_WAIT_TURN.
+__device__ __forceinline__ bool group_take_turn(const BankParams& p, uint32_t x) {
   uint32_t* next = p.tk + 2u * (size_t)x;
   uint32_t* serving = next + 1;
   const uint32_t mine = atomicAdd(next, 1u);
   const uint64_t limit = 1ull << min(p.spin_log2, 22u);  // at most a few seconds
-  bool turn = false;
   for (uint64_t it = 0; it < limit; it++) {
     const uint32_t now = ld_acquire_gpu(serving);
-    if (now == mine) {
-      turn = true;
-      break;
-    }
+    if (now == mine) return true;
     if ((it & 63u) == 63u && ld_relaxed_gpu(&p.gs->error) != 0u) return false;
     __nanosleep(min(64u * (mine - now), 1024u));  // farther back in the queue: poll less often
   }
-  bool got = false;
-  for (uint64_t it = 0; turn && it < limit; it++) {
+  raise_error(&p.gs->error, ERR_WAIT_TURN);
+  return false;
+}
+
+__device__ __forceinline__ void group_pass_turn(const BankParams& p, uint32_t x) {
+  atomicAdd(p.tk + 2u * (size_t)x + 1u, 1u);
+}
+
+// At the head of x's queue: waits for the holder's release and takes the lock, with the account's
+// version slots (ed) and latest value (v) read as it is taken. The poll that finds the lock free
+// is an acquire load, so the slots loaded after it hold the version of the stamp it saw, and a
+// CAS that succeeds at that stamp proves them current (*stale stays false).
+template <int DEPTH>
+__device__ __forceinline__ bool group_lock_at_turn(const BankParams& p, uint32_t x, uint32_t me,
+                                                   uint32_t& stamp, bool& stale,
+                                                   SlotEditor<DEPTH>& ed, int32_t& v) {
+  const uint64_t limit = 1ull << min(p.spin_log2, 22u);
+  for (uint64_t it = 0; it < limit; it++) {
     const unsigned long long w = ld_acquire_gpu(&p.cw[x]);
     if ((w >> 32) == 0ull) {
       ed.load(p.slots + (size_t)x * DEPTH);
       if (atomicCAS(&p.cw[x], w, w | ((unsigned long long)me << 32)) == w) {
         stamp = (uint32_t)w;
         stale = !ed.find(stamp, v);
-        got = true;
-        break;
+        return true;
       }
       continue;  // a fast-path CAS took it first: poll again
     }
     if ((it & 63u) == 63u && ld_relaxed_gpu(&p.gs->error) != 0u) break;
     __nanosleep(32);
   }
-  if (turn) atomicAdd(serving, 1u);  // the next ticket's turn (also when this wait failed)
-  if (!got) raise_error(&p.gs->error, ERR_WAIT_TURN);
+  raise_error(&p.gs->error, ERR_WAIT_TURN);
+  return false;
+}
+
+// Queue for x's lock and take it (the turn is served on, also when the wait failed).
+template <int DEPTH>
+__device__ __forceinline__ bool group_wait_lock(const BankParams& p, uint32_t x, uint32_t me,
+                                                uint32_t& stamp, bool& stale,
+                                                SlotEditor<DEPTH>& ed, int32_t& v) {
+  if (!group_take_turn(p, x)) return false;
+  const bool got = group_lock_at_turn<DEPTH>(p, x, me, stamp, stale, ed, v);
+  group_pass_turn(p, x);
   return got;
 }
 
@@ -475,8 +493,32 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
   const bool lead0 = act && (uint32_t)(__ffs(gx.wmask[s0]) - 1) == lane;
   const bool lead1 = act && s1 != s0 && (uint32_t)(__ffs(gx.wmask[s1]) - 1) == lane;
 
-  // 2. locks, ascending account order, waiting (bounded) for locks held elsewhere. A leader
-  //    keeps the account's version slots from its read: the write-back edits them in registers.
+  // 2. locks, waiting (bounded) for locks held elsewhere, in one total order: accounts with no
+  //    heat class (lock_last 0) ascending, then the classed (hot) ones by class and account, the
+  //    hottest last. A group first tries every lock at once; when one is held elsewhere it
+  //    settles the smallest missing lock while holding only smaller ones, queueing on a cold
+  //    account's tickets. A group with hot accounts that did not get every lock at once
+  //    releases all and queues, holding nothing, for its LAST lock in the order (its hottest
+  //    account); at the head of that queue it takes its other locks - cold ones queued, hot
+  //    ones by polling - and the hottest last, so a hot lock is held only for the commit
+  //    itself, and the next group in line takes its other locks while the current holder
+  //    commits. Waits follow the order turns < cold locks < hot locks, a group holds at most
+  //    one turn, and a hot lock is held only by a group that holds every smaller lock it needs
+  //    or is committing: no cycle of waits. A leader keeps the account's version slots from its
+  //    read: the write-back edits them in registers.
+  const uint32_t c0 = (lead0 && p.lock_last != nullptr) ? p.lock_last[a[0]] : 0u;
+  const uint32_t c1 = (lead1 && p.lock_last != nullptr) ? p.lock_last[a[1]] : 0u;
+  // order key: (tier | class, account); tier bit 31 set for hot accounts
+  const uint32_t kh0 = c0 ? 0x80000000u | c0 : 0u, kh1 = c1 ? 0x80000000u | c1 : 0u;
+  auto key_min = [&](bool m0, bool m1, uint32_t& fh, uint32_t& fl) {  // smallest key of a set
+    const uint32_t h = min(m0 ? kh0 : 0xFFFFFFFFu, m1 ? kh1 : 0xFFFFFFFFu);
+    fh = __reduce_min_sync(FULL, h);
+    fl = __reduce_min_sync(FULL, min((m0 && kh0 == fh) ? a[0] : kGrpEmpty,
+                                     (m1 && kh1 == fh) ? a[1] : kGrpEmpty));
+  };
+  auto above = [](uint32_t h, uint32_t l, uint32_t fh, uint32_t fl) {
+    return h > fh || (h == fh && l > fl);
+  };
   uint32_t st0 = 0, st1 = 0;
   int32_t bv0 = 0, bv1 = 0;
   SlotEditor<DEPTH> ed0, ed1;
@@ -497,31 +539,53 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
   if (lead1 && !h1) gx.busy[s1] = 1u;
   __syncwarp();
   waited = act && (gx.busy[s0] | gx.busy[s1]) != 0u;
-  bool all = false;
-  for (uint32_t it = 0; it <= 64u; it++) {  // each pass settles the smallest account still missing
-    const uint32_t m0 = (lead0 && !h0) ? a[0] : kGrpEmpty, m1 = (lead1 && !h1) ? a[1] : kGrpEmpty;
-    const uint32_t f = __reduce_min_sync(FULL, min(m0, m1));
-    if (f == kGrpEmpty) {
+  bool all = false, ok = true;
+  int turn = -1;  // which of my accounts' queue turn this lane holds (the group holds at most one)
+  if (__any_sync(FULL, (lead0 && !h0) || (lead1 && !h1)) && __any_sync(FULL, c0 || c1)) {
+    if (h0) st_relaxed_gpu(&p.cw[a[0]], (unsigned long long)st0);
+    if (h1) st_relaxed_gpu(&p.cw[a[1]], (unsigned long long)st1);
+    h0 = h1 = false;
+    // the group's last lock: the largest key among its hot accounts
+    const uint32_t qh = __reduce_max_sync(FULL, max(kh0, kh1));
+    const uint32_t ql = __reduce_max_sync(FULL, max((c0 && kh0 == qh) ? a[0] : 0u,
+                                                    (c1 && kh1 == qh) ? a[1] : 0u));
+    bool r = true;
+    if (c0 && kh0 == qh && a[0] == ql) {
+      r = group_take_turn(p, a[0]);
+      if (r) turn = 0;
+    } else if (c1 && kh1 == qh && a[1] == ql) {
+      r = group_take_turn(p, a[1]);
+      if (r) turn = 1;
+    }
+    ok = !__any_sync(FULL, !r);
+  }
+  for (uint32_t it = 0; ok && it <= 64u; it++) {  // each pass settles the smallest missing lock
+    uint32_t fh, fl;
+    key_min(lead0 && !h0, lead1 && !h1, fh, fl);
+    if (fl == kGrpEmpty) {
       all = true;
       break;
     }
-    if (h0 && a[0] > f) {  // hold nothing above the lock being waited for
+    if (h0 && above(kh0, a[0], fh, fl)) {  // hold nothing above the lock being waited for
       st_relaxed_gpu(&p.cw[a[0]], (unsigned long long)st0);
       h0 = false;
     }
-    if (h1 && a[1] > f) {
+    if (h1 && above(kh1, a[1], fh, fl)) {
       st_relaxed_gpu(&p.cw[a[1]], (unsigned long long)st1);
       h1 = false;
     }
-    bool ok = true;
-    if (lead0 && !h0 && a[0] == f)
-      ok = h0 = group_wait_lock<DEPTH>(p, a[0], me, st0, stale0, ed0, bv0);
-    else if (lead1 && !h1 && a[1] == f)
-      ok = h1 = group_wait_lock<DEPTH>(p, a[1], me, st1, stale1, ed1, bv1);
-    if (__any_sync(FULL, !ok)) break;
-    if (lead0 && !h0 && a[0] > f) h0 = group_cas_lock(p.cw, a[0], me, st0, stale0);
-    if (lead1 && !h1 && a[1] > f) h1 = group_cas_lock(p.cw, a[1], me, st1, stale1);
+    bool r = true;
+    if (lead0 && !h0 && kh0 == fh && a[0] == fl)
+      r = h0 = c0 ? group_lock_at_turn<DEPTH>(p, a[0], me, st0, stale0, ed0, bv0)
+                  : group_wait_lock<DEPTH>(p, a[0], me, st0, stale0, ed0, bv0);
+    else if (lead1 && !h1 && kh1 == fh && a[1] == fl)
+      r = h1 = c1 ? group_lock_at_turn<DEPTH>(p, a[1], me, st1, stale1, ed1, bv1)
+                  : group_wait_lock<DEPTH>(p, a[1], me, st1, stale1, ed1, bv1);
+    if (__any_sync(FULL, !r)) break;
+    if (lead0 && !h0 && above(kh0, a[0], fh, fl)) h0 = group_cas_lock(p.cw, a[0], me, st0, stale0);
+    if (lead1 && !h1 && above(kh1, a[1], fh, fl)) h1 = group_cas_lock(p.cw, a[1], me, st1, stale1);
   }
+  if (turn >= 0) group_pass_turn(p, turn == 0 ? a[0] : a[1]);  // the next in line starts now
   if (!all) {  // a wait ran out: release everything, the round retries later
     if (h0) st_relaxed_gpu(&p.cw[a[0]], (unsigned long long)st0);
     if (h1) st_relaxed_gpu(&p.cw[a[1]], (unsigned long long)st1);
@@ -926,8 +990,11 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
         }
         int32_t w0, w1;
         const bool has_w = okr && transfer_writes<MAXR>(op, nr, v, w0, w1);
-        const bool part = okr && (has_w || fwd != 0);      // a link of the chain: needs a timestamp
-        const bool ro_cand = okr && !has_w && fwd == 0;    // read-only outcome
+        // every transfer of the round is a link with a timestamp, also one that writes nothing:
+        // a no-write transfer serialised at the stamps it read could fall inside a chain, whose
+        // intermediate states are never installed
+        const bool part = okr;
+        const bool ro_cand = false;
         const bool snap_ok = recheck(ro_cand);
         const bool ro_fail = ro_cand && !snap_ok;
         // lock leaders: the lowest lane writing each address takes its lock
@@ -1044,8 +1111,11 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
             p.outcome[t] = my_ts;
             p.result[t] = 0;
           }
-          // write-back by the lock leaders: every committed link's version of the item, in
-          // timestamp order, then the stamp of the last one and the unlock
+          // write-back by the lock leaders: ONE version per item, the last committed link's,
+          // then its stamp and the unlock. The chain's timestamps are published to the clock
+          // as one range, so no snapshot falls between them and the intermediate versions are
+          // never read; installing them would also let one store evict two versions, and a
+          // concurrent snapshot read could then see the older victim without the younger one.
           const uint32_t hwm = __ballot_sync(0xFFFFFFFFu, has_w && commit);
 #pragma unroll
           for (int k = 0; k < 2; k++) {
@@ -1054,17 +1124,21 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
             SlotEditor<DEPTH> ed;
             if (lead) ed.load(item);
             uint32_t last = 0;
+            int32_t lv = 0;
             for (uint32_t m = hwm; m; m &= m - 1) {
               const uint32_t i = __ffs(m) - 1;
               const uint32_t x0 = __shfl_sync(0xFFFFFFFFu, a[0], i), x1 = __shfl_sync(0xFFFFFFFFu, a[1], i);
               const int32_t y0 = __shfl_sync(0xFFFFFFFFu, w0, i), y1 = __shfl_sync(0xFFFFFFFFu, w1, i);
               const uint32_t ti = __shfl_sync(0xFFFFFFFFu, my_ts, i);
               if (lead && (x0 == a[k] || x1 == a[k])) {
-                ed.insert(ti, x0 == a[k] ? y0 : y1);
+                lv = x1 == a[k] ? y1 : y0;  // a transfer writes a1 last
                 last = ti;
               }
             }
-            if (lead && last) ed.store(item);
+            if (lead && last) {
+              ed.insert(last, lv);
+              ed.store(item);
+            }
             __threadfence();
             if (lead) {
               if (last)
@@ -1074,7 +1148,13 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
             }
           }
           __syncwarp();
-          if (lane == 0) complete_range(p.done, p.done_mask, p.gs, base + 1, base + __popc(cand));
+          if (lane == 0) {
+            if (p.log && p.grp) {  // the chain's end, for the replay's one-version-per-group rule
+              const uint32_t li = base + __popc(cand) - 1u - p.log_base;
+              if (li < p.log_cap) atomicOr(&p.grp[li >> 5], 1u << (li & 31u));
+            }
+            complete_range(p.done, p.done_mask, p.gs, base + 1, base + __popc(cand));
+          }
         } else {
           // no links: leaders release whatever they locked
 #pragma unroll

@@ -27,4 +27,8 @@ inline csmv_status cuda_status(cudaError_t e, const char* what) {
 // Checks that `device` exists and is an sm_103 part; returns the SM count.
 csmv_status check_device(int device, int* n_sms);
 
+// The bank's account count; true when it commits in groups (prevalidate 3, stamp protocol), the
+// mode that takes a stream's lock_last classes (bank_engine.cu).
+bool bank_group_commit(const csmv_bank_t* h, uint32_t* n_accounts);
+
 }  // namespace csmv

@@ -397,7 +397,13 @@ struct csmv_serve_t {
   ServeHostCtl* ctl = nullptr;
   ServeBatchDesc* desc = nullptr;
   uint32_t *h_kind = nullptr, *h_key = nullptr, *h_val = nullptr, *h_found = nullptr,
-           *h_out = nullptr;
+           *h_out = nullptr, *h_outcome = nullptr;
+  // commit log (log_cap > 0): the kernel's parameters are updated per session (its base ts)
+  uint32_t* log_txn = nullptr;
+  cudaGraphNode_t knode = nullptr;
+  MemcdParams kp{};
+  ServeParams ksp{};
+  uint32_t base_ts = 0, end_ts = 0;
   // host bookkeeping
   bool running = false;
   uint64_t submitted = 0, retired = 0, arena_head = 0, arena_tail = 0, inflight_sets = 0;
@@ -420,9 +426,10 @@ static void serve_free(csmv_serve_t* h) {
   if (h->exec) cudaGraphExecDestroy(h->exec);
   if (h->graph) cudaGraphDestroy(h->graph);
   void* dptr[] = {h->tag, h->rec, h->cw, h->done, h->gs, h->stats, h->dummy_log,
-                  h->dev, h->rq, h->remaining, h->tick};
+                  h->dev, h->rq, h->remaining, h->tick, h->log_txn};
   for (void* p : dptr) cudaFree(p);
-  void* hptr[] = {h->ctl, h->desc, h->h_kind, h->h_key, h->h_val, h->h_found, h->h_out};
+  void* hptr[] = {h->ctl, h->desc, h->h_kind, h->h_key, h->h_val, h->h_found, h->h_out,
+                  h->h_outcome};
   for (void* p : hptr)
     if (p) cudaFreeHost(p);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -495,6 +502,12 @@ extern "C" csmv_status csmv_serve_create(const csmv_serve_config* cfg, csmv_serv
   for (auto& a : hallocs)
     if ((st = cuda_status(cudaHostAlloc(a.p, a.bytes, cudaHostAllocMapped), "cudaHostAlloc")) != CSMV_OK)
       return fail(st);
+  if (cfg->log_cap) {
+    if ((st = cuda_status(cudaMalloc(&h->log_txn, (size_t)cfg->log_cap * 4), "cudaMalloc")) != CSMV_OK ||
+        (st = cuda_status(cudaHostAlloc(&h->h_outcome, (size_t)A * 4, cudaHostAllocMapped),
+                          "cudaHostAlloc")) != CSMV_OK)
+      return fail(st);
+  }
   std::memset(h->ctl, 0, sizeof(ServeHostCtl));
   std::memset(h->desc, 0, kServeSlots * sizeof(ServeBatchDesc));
   if ((st = cuda_status(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream")) != CSMV_OK)
@@ -536,6 +549,16 @@ extern "C" csmv_status csmv_serve_create(const csmv_serve_config* cfg, csmv_serv
   p.log = 0;
   p.log_base = 0;
   p.log_cap = 1;
+  if (cfg->log_cap) {  // the base timestamp is set per session (csmv_serve_start)
+    p.log_txn = h->log_txn;
+    p.outcome = dev_ptr_of(h->h_outcome);
+    p.log = 1;
+    p.log_cap = cfg->log_cap;
+    if (!p.outcome) {
+      set_error("cudaHostGetDevicePointer failed");
+      return fail(CSMV_ERR_CUDA);
+    }
+  }
   p.stats = h->stats;
   p.nc = cfg->client_warps;
   p.batch = CSMV_BATCH_CTA;
@@ -563,6 +586,23 @@ extern "C" csmv_status csmv_serve_create(const csmv_serve_config* cfg, csmv_serv
   if ((st = cuda_status(e, "capture of the serving graph")) != CSMV_OK) return fail(st);
   if ((st = cuda_status(cudaGraphInstantiate(&h->exec, h->graph, 0), "cudaGraphInstantiate")) != CSMV_OK)
     return fail(st);
+  h->kp = p;
+  h->ksp = sp;
+  if (cfg->log_cap) {  // the kernel node, whose parameters each session updates
+    cudaGraphNode_t nodes[8];
+    size_t n_nodes = 8;
+    if ((st = cuda_status(cudaGraphGetNodes(h->graph, nodes, &n_nodes), "cudaGraphGetNodes")) != CSMV_OK)
+      return fail(st);
+    for (size_t i = 0; i < n_nodes; i++) {
+      cudaGraphNodeType ty;
+      if (cudaGraphNodeGetType(nodes[i], &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel)
+        h->knode = nodes[i];
+    }
+    if (!h->knode) {
+      set_error("serving graph without a kernel node");
+      return fail(CSMV_ERR_CUDA);
+    }
+  }
   *out = h;
   return CSMV_OK;
 }
@@ -578,6 +618,21 @@ extern "C" csmv_status csmv_serve_start(csmv_serve_t* h) {
   std::memset(h->desc, 0, kServeSlots * sizeof(ServeBatchDesc));
   std::atomic_thread_fence(std::memory_order_seq_cst);
   h->submitted = h->retired = h->arena_head = h->arena_tail = h->inflight_sets = 0;
+  if (h->cfg.log_cap) {  // this session's log starts after the last timestamp drawn so far
+    GlobalSync gs;
+    CSMV_CUDA(cudaMemcpy(&gs, h->gs, sizeof(gs), cudaMemcpyDeviceToHost));
+    h->base_ts = h->end_ts = gs.ts_next;
+    CSMV_CUDA(cudaMemset(h->log_txn, 0xFF, (size_t)h->cfg.log_cap * 4));
+    h->kp.log_base = h->base_ts;
+    void* args[] = {&h->kp, &h->ksp};
+    cudaKernelNodeParams kn{};
+    kn.func = (void*)memcd_serve_kernel;
+    kn.gridDim = dim3(h->ctas);
+    kn.blockDim = dim3(h->threads);
+    kn.sharedMemBytes = 0;
+    kn.kernelParams = args;
+    CSMV_CUDA(cudaGraphExecKernelNodeSetParams(h->exec, h->knode, &kn));
+  }
   CSMV_CUDA(cudaGraphLaunch(h->exec, h->stream));
   h->running = true;
   return CSMV_OK;
@@ -658,7 +713,17 @@ extern "C" csmv_status csmv_serve_submit(csmv_serve_t* h, const csmv_memcd_batch
 extern "C" csmv_status csmv_serve_poll(csmv_serve_t* h, uint64_t batch_id, uint32_t* done,
                                        uint32_t* host_found, uint32_t* host_val_out,
                                        uint64_t* device_ns) {
+  return csmv_serve_poll_logged(h, batch_id, done, host_found, host_val_out, nullptr, device_ns);
+}
+
+extern "C" csmv_status csmv_serve_poll_logged(csmv_serve_t* h, uint64_t batch_id, uint32_t* done,
+                                              uint32_t* host_found, uint32_t* host_val_out,
+                                              uint32_t* host_outcome, uint64_t* device_ns) {
   if (!h || !done) return CSMV_ERR_INVALID_ARG;
+  if (host_outcome && !h->cfg.log_cap) {
+    set_error("outcomes are kept only with log_cap > 0");
+    return CSMV_ERR_STATE;
+  }
   *done = 0;
   if (batch_id >= h->submitted) {
     set_error("batch %llu not submitted", (unsigned long long)batch_id);
@@ -688,6 +753,10 @@ extern "C" csmv_status csmv_serve_poll(csmv_serve_t* h, uint64_t batch_id, uint3
     std::memcpy(host_val_out, h->h_out + (size_t)first * 8, (size_t)n1 * 32);
     if (n2) std::memcpy(host_val_out + (size_t)n1 * 8, h->h_out, (size_t)n2 * 32);
   }
+  if (host_outcome) {
+    std::memcpy(host_outcome, h->h_outcome + first, (size_t)n1 * 4);
+    if (n2) std::memcpy(host_outcome + n1, h->h_outcome, (size_t)n2 * 4);
+  }
   if (device_ns) *device_ns = d.done_ns > d.admit_ns ? d.done_ns - d.admit_ns : 0;
   *done = 1;
   return CSMV_OK;
@@ -710,6 +779,7 @@ extern "C" csmv_status csmv_serve_stop(csmv_serve_t* h, csmv_stats* out) {
   CSMV_CUDA(cudaMemcpy(st, h->stats, sizeof(st), cudaMemcpyDeviceToHost));
   CSMV_CUDA(cudaMemcpy(&gs, h->gs, sizeof(gs), cudaMemcpyDeviceToHost));
   serve_retire(h);
+  h->end_ts = gs.ts_next;
   if (out) {
     std::memset(out, 0, sizeof(*out));
     out->commits_update = st[ST_COMMIT_UPDATE];
@@ -726,6 +796,35 @@ extern "C" csmv_status csmv_serve_stop(csmv_serve_t* h, csmv_stats* out) {
   if (gs.error) {
     set_error("serving kernel ended with device error %u (4: idle timeout)", gs.error);
     return CSMV_ERR_TIMEOUT;
+  }
+  return CSMV_OK;
+}
+
+extern "C" csmv_status csmv_serve_read_log(csmv_serve_t* h, uint32_t* host_log_txn, uint32_t n_log,
+                                           uint32_t* n_used, uint32_t* base_ts) {
+  if (!h) return CSMV_ERR_INVALID_ARG;
+  if (!h->cfg.log_cap) {
+    set_error("serving handle was created with log_cap = 0");
+    return CSMV_ERR_STATE;
+  }
+  if (h->running) {
+    set_error("stop the serving session first");
+    return CSMV_ERR_STATE;
+  }
+  CSMV_CUDA(cudaSetDevice(h->cfg.device));
+  const uint32_t used = h->end_ts - h->base_ts;
+  if (n_used) *n_used = used;
+  if (base_ts) *base_ts = h->base_ts;
+  if (used > h->cfg.log_cap) {
+    set_error("the session drew %u timestamps, the log holds %u", used, h->cfg.log_cap);
+    return CSMV_ERR_CAPACITY;
+  }
+  if (host_log_txn) {
+    if (n_log < used) {
+      set_error("log buffer holds %u entries, the session used %u timestamps", n_log, used);
+      return CSMV_ERR_CAPACITY;
+    }
+    CSMV_CUDA(cudaMemcpy(host_log_txn, h->log_txn, (size_t)used * 4, cudaMemcpyDeviceToHost));
   }
   return CSMV_OK;
 }

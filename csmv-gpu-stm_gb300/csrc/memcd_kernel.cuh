@@ -477,14 +477,17 @@ __global__ void __launch_bounds__(512, 1) memcd_kernel(MemcdParams p) {
 // Requests live in a ring ("arena") of pinned, mapped host memory that the kernel reads and
 // writes in place (coherent over the C2C link of a Grace-Blackwell node): request i of a batch
 // that starts at arena index f is request (f + i) mod arena size. The host publishes a batch by
-// filling its descriptor and then bumping ctl->submitted (release). Any client warp that finds
-// the round queue empty takes the admission lock, turns newly published batches into rounds of
-// 32 requests appended to the device round queue, and releases the queue tail; warps claim
-// rounds in order and run them with the cache's commit protocol, so rounds of different batches
-// overlap on the device. After a round, the warp makes its results visible to the host and
-// counts the round off its batch; the batch's last round stamps done_ns and sets done (release).
-// The kernel returns once ctl->stop is set and every published batch has completed, or when the
-// host has published nothing for idle_ns (error ERR_WAIT_REQUEST).
+// filling its descriptor and then bumping ctl->submitted (release). ONE warp (the first client
+// warp of CTA 0) is the admitter: it alone polls the host's control words, turns newly
+// published batches into rounds of 32 requests appended to the device round queue, and releases
+// the queue tail; it runs no rounds. Every other client warp takes a ticket (the next round
+// index, one atomic add) and polls the queue tail in device memory until its round exists, then
+// runs it with the cache's commit protocol, so rounds of different batches overlap on the device
+// and idle warps put no traffic on the host link. After a round, the warp makes its results
+// visible to the host and counts the round off its batch; the batch's last round stamps done_ns
+// and sets done (release). Once ctl->stop is set and every published batch is admitted, or when
+// the host has published nothing and every round is done for idle_ns (error ERR_WAIT_REQUEST),
+// the admitter raises dev->quit; a warp leaves when quit is set and its ticket is past the tail.
 // ---------------------------------------------------------------------------------------------
 constexpr uint32_t kServeSlots = 1024;  // batch descriptors in flight at most
 
@@ -502,10 +505,11 @@ struct ServeBatchDesc {   // mapped host memory, one per in-flight batch (slot =
 };
 
 struct alignas(128) ServeDev {  // device memory
-  alignas(128) uint32_t admitted;  // batches turned into rounds
-  alignas(128) uint32_t q_head;    // rounds claimed
-  alignas(128) uint32_t q_tail;    // rounds appended
-  alignas(128) uint32_t lock;      // admission
+  alignas(128) uint32_t admitted;     // batches turned into rounds
+  alignas(128) uint32_t q_head;       // round tickets taken
+  alignas(128) uint32_t q_tail;       // rounds appended
+  alignas(128) uint32_t rounds_done;  // rounds completed
+  alignas(128) uint32_t quit;         // no round will be appended any more
 };
 
 struct ServeParams {
@@ -520,50 +524,72 @@ struct ServeParams {
   unsigned long long idle_ns;
 };
 
-// Admission, warp-collective (called by a warp whose claim found the queue empty).
-__device__ void serve_admit(const ServeParams& s) {
+// The admitter's loop, warp-collective: the only reader of the host's control words.
+__device__ void serve_admitter(const MemcdParams& p, const ServeParams& s) {
   const uint32_t lane = lane_id();
-  uint32_t locked = 0;
-  if (lane == 0) locked = atomicCAS(&s.dev->lock, 0u, 1u) == 0u ? 1u : 0u;
-  if (!__shfl_sync(0xFFFFFFFFu, locked, 0)) return;
-  uint32_t sub = 0, adm = 0, qt = 0;
-  if (lane == 0) {
-    sub = ld_acquire_sys(&s.ctl->submitted);
-    adm = ld_relaxed_gpu(&s.dev->admitted);
-    qt = ld_relaxed_gpu(&s.dev->q_tail);
-  }
-  sub = __shfl_sync(0xFFFFFFFFu, sub, 0);
-  adm = __shfl_sync(0xFFFFFFFFu, adm, 0);
-  qt = __shfl_sync(0xFFFFFFFFu, qt, 0);
-  for (uint32_t guard = 0; adm < sub && guard < kServeSlots; guard++, adm++) {
-    const uint32_t slot = adm % kServeSlots;
-    uint32_t first = 0, n = 0, tk = 0;
+  uint32_t adm = 0, qt = 0, last_sub = 0;
+  unsigned long long idle_since = globaltimer_ns();
+  for (;;) {
+    uint32_t sub = 0, stop = 0, err = 0, done = 0;
     if (lane == 0) {
-      const volatile ServeBatchDesc* d = s.desc + slot;
-      first = d->first;
-      n = d->n_req;
-      tk = d->tick;
+      sub = ld_acquire_sys(&s.ctl->submitted);
+      stop = ld_acquire_sys(&s.ctl->stop);
+      err = ld_relaxed_gpu(&p.gs->error);
+      done = ld_relaxed_gpu(&s.dev->rounds_done);
     }
-    first = __shfl_sync(0xFFFFFFFFu, first, 0);
-    n = __shfl_sync(0xFFFFFFFFu, n, 0);
-    tk = __shfl_sync(0xFFFFFFFFu, tk, 0);
-    const uint32_t rounds = n / 32u;
-    for (uint32_t i = lane; i < rounds; i += 32)
-      s.rq[(qt + i) & s.q_mask] = make_uint2((first + 32u * i) & s.arena_mask, slot);
-    if (lane == 0) {
-      s.remaining[slot] = rounds;
-      s.tick[slot] = tk;
-      s.desc[slot].admit_ns = globaltimer_ns();
+    sub = __shfl_sync(0xFFFFFFFFu, sub, 0);
+    stop = __shfl_sync(0xFFFFFFFFu, stop, 0);
+    err = __shfl_sync(0xFFFFFFFFu, err, 0);
+    done = __shfl_sync(0xFFFFFFFFu, done, 0);
+    if (err) {
+      if (lane == 0) st_release_sys(&s.ctl->error, err);  // the host sees it without waiting
+      break;
     }
-    qt += rounds;
+    const bool fresh = adm < sub;
+    for (uint32_t guard = 0; adm < sub && guard < kServeSlots; guard++, adm++) {
+      const uint32_t slot = adm % kServeSlots;
+      uint32_t first = 0, n = 0, tk = 0;
+      if (lane == 0) {
+        const volatile ServeBatchDesc* d = s.desc + slot;
+        first = d->first;
+        n = d->n_req;
+        tk = d->tick;
+      }
+      first = __shfl_sync(0xFFFFFFFFu, first, 0);
+      n = __shfl_sync(0xFFFFFFFFu, n, 0);
+      tk = __shfl_sync(0xFFFFFFFFu, tk, 0);
+      const uint32_t rounds = n / 32u;
+      for (uint32_t i = lane; i < rounds; i += 32)
+        s.rq[(qt + i) & s.q_mask] = make_uint2((first + 32u * i) & s.arena_mask, slot);
+      if (lane == 0) {
+        s.remaining[slot] = rounds;
+        s.tick[slot] = tk;
+        s.desc[slot].admit_ns = globaltimer_ns();
+      }
+      qt += rounds;
+    }
+    __syncwarp();
+    if (fresh && lane == 0) {
+      st_relaxed_gpu(&s.dev->admitted, adm);
+      __threadfence();
+      st_release_gpu(&s.dev->q_tail, qt);  // rounds, counts and ticks before the tail
+    }
+    const unsigned long long now = globaltimer_ns();
+    if (sub != last_sub || done != qt) {  // the host published, or rounds are running: not idle
+      last_sub = sub;
+      idle_since = now;
+    }
+    if (stop && adm == sub) break;
+    if (now - idle_since > s.idle_ns) {
+      if (lane == 0) {
+        raise_error(&p.gs->error, ERR_WAIT_REQUEST);
+        st_release_sys(&s.ctl->error, ERR_WAIT_REQUEST);
+      }
+      break;
+    }
+    if (!fresh) __nanosleep(256);
   }
-  __syncwarp();
-  if (lane == 0) {
-    st_relaxed_gpu(&s.dev->admitted, adm);
-    __threadfence();
-    st_release_gpu(&s.dev->q_tail, qt);  // rounds, counts and ticks before the tail
-    st_release_gpu(&s.dev->lock, 0u);
-  }
+  if (lane == 0) st_release_gpu(&s.dev->quit, 1u);
 }
 
 __device__ void serve_client(const MemcdParams& p, const ServeParams& s, MemcdShared& sm,
@@ -572,69 +598,54 @@ __device__ void serve_client(const MemcdParams& p, const ServeParams& s, MemcdSh
   const uint32_t lane = lane_id();
   const uint32_t me = blockIdx.x * p.nc + w + 1;
   uint32_t seq = 0;
-  unsigned long long idle_since = 0;  // since when the host has published nothing new
-  uint32_t last_sub = 0xFFFFFFFFu;
-  for (;;) {
-    uint32_t got = 0u, first = 0u, slot = 0u;
-    if (lane == 0) {
-      for (uint32_t attempt = 0; attempt < 64u; attempt++) {
-        const uint32_t h = ld_relaxed_gpu(&s.dev->q_head), t = ld_acquire_gpu(&s.dev->q_tail);
-        if (h >= t) break;
-        if (atomicCAS(&s.dev->q_head, h, h + 1u) == h) {
-          const uint2 e = s.rq[h & s.q_mask];
-          first = e.x;
-          slot = e.y;
-          got = 1u;
-          break;
-        }
-      }
-    }
-    got = __shfl_sync(0xFFFFFFFFu, got, 0);
-    if (!got) {
-      serve_admit(s);
-      uint32_t leave = 0;
+  if (blockIdx.x == 0 && w == 0) {
+    serve_admitter(p, s);
+  } else {
+    for (;;) {
+      uint32_t state = 0u, first = 0u, slot = 0u;  // 1: a round, 2: leave
       if (lane == 0) {
-        const uint32_t h = ld_relaxed_gpu(&s.dev->q_head), t = ld_acquire_gpu(&s.dev->q_tail);
-        const uint32_t stop = ld_acquire_sys(&s.ctl->stop);
-        const uint32_t sub = ld_acquire_sys(&s.ctl->submitted);
-        const uint32_t adm = ld_relaxed_gpu(&s.dev->admitted);
-        const unsigned long long now = globaltimer_ns();
-        if (sub != last_sub || h < t) {  // the host published, or work is queued: not idle
-          last_sub = sub;
-          idle_since = now;
-        }
-        const uint32_t err = ld_relaxed_gpu(&p.gs->error);
-        if (err) {
-          st_release_sys(&s.ctl->error, err);  // the host sees it without waiting for the end
-          leave = 1;
-        } else if (stop && adm == sub && h >= t) {
-          leave = 1;
-        } else if (now - idle_since > s.idle_ns) {
-          raise_error(&p.gs->error, ERR_WAIT_REQUEST);
-          st_release_sys(&s.ctl->error, ERR_WAIT_REQUEST);
-          leave = 1;
+        const uint32_t ticket = atomicAdd(&s.dev->q_head, 1u);
+        uint32_t nap = 64;
+        for (;;) {
+          if (ticket < ld_acquire_gpu(&s.dev->q_tail)) {
+            const uint2 e = s.rq[ticket & s.q_mask];
+            first = e.x;
+            slot = e.y;
+            state = 1u;
+            break;
+          }
+          if (ld_acquire_gpu(&s.dev->quit) && ticket >= ld_acquire_gpu(&s.dev->q_tail)) {
+            state = 2u;  // nothing more will be appended
+            break;
+          }
+          if (ld_relaxed_gpu(&p.gs->error)) {
+            state = 2u;
+            break;
+          }
+          __nanosleep(nap);
+          nap = min(nap * 2u, 2048u);
         }
       }
-      if (__shfl_sync(0xFFFFFFFFu, leave, 0)) break;
-      __nanosleep(200);
-      continue;
-    }
-    first = __shfl_sync(0xFFFFFFFFu, first, 0);
-    slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
-    uint32_t tk = 0;
-    if (lane == 0) tk = ld_relaxed_gpu(&s.tick[slot]);
-    tk = __shfl_sync(0xFFFFFFFFu, tk, 0);
-    if (!memcd_round(p, sm, ms, me, (first + lane) & s.arena_mask, seq, tk)) {
-      if (lane == 0) st_release_sys(&s.ctl->error, max(1u, ld_relaxed_gpu(&p.gs->error)));
-      break;
-    }
-    __syncwarp();
-    if (lane == 0) {
-      __threadfence_system();  // this round's results reach the host before its batch completes
-      if (atomicSub(&s.remaining[slot], 1u) == 1u) {
-        s.desc[slot].done_ns = globaltimer_ns();
-        __threadfence_system();
-        st_release_sys(&s.desc[slot].done, 1u);
+      state = __shfl_sync(0xFFFFFFFFu, state, 0);
+      if (state == 2u) break;
+      first = __shfl_sync(0xFFFFFFFFu, first, 0);
+      slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+      uint32_t tk = 0;
+      if (lane == 0) tk = ld_relaxed_gpu(&s.tick[slot]);
+      tk = __shfl_sync(0xFFFFFFFFu, tk, 0);
+      if (!memcd_round(p, sm, ms, me, (first + lane) & s.arena_mask, seq, tk)) {
+        if (lane == 0) st_release_sys(&s.ctl->error, max(1u, ld_relaxed_gpu(&p.gs->error)));
+        break;
+      }
+      __syncwarp();
+      if (lane == 0) {
+        __threadfence_system();  // this round's results reach the host before its batch completes
+        if (atomicSub(&s.remaining[slot], 1u) == 1u) {
+          s.desc[slot].done_ns = globaltimer_ns();
+          __threadfence_system();
+          st_release_sys(&s.desc[slot].done, 1u);
+        }
+        atomicAdd(&s.dev->rounds_done, 1u);
       }
     }
   }

@@ -47,6 +47,8 @@ struct csmv_sched_t {
   uint32_t *hidx = nullptr, *key_start = nullptr, *tile_sum = nullptr, *tile_off = nullptr;
   uint32_t *rank = nullptr, *cold_pos = nullptr, *sorted = nullptr, *rbucket = nullptr;
   uint32_t *round_order = nullptr, *bo = nullptr, *bo2 = nullptr, *max_count = nullptr;
+  uint8_t* lock_last = nullptr;  // heat classes of the bank's accounts (hot_last)
+  uint32_t lock_last_n = 0;
   uint64_t chunks = 0;
   // the current chunk
   uint32_t n = 0, probe_rounds = 0, split_round = 0, planned = 0, serial_rounds = 0;
@@ -72,6 +74,7 @@ extern "C" void csmv_sched_config_default(csmv_sched_config* c) {
   c->hot_count = 0;
   c->score = 0;
   c->backoff_ns = 2048;
+  c->hot_last = 1;
 }
 
 static void free_all(csmv_sched_t* s) {
@@ -80,7 +83,7 @@ static void free_all(csmv_sched_t* s) {
                   s->bucket_fill, s->order, s->perm, s->op2, s->off2, s->ro_flag, s->ro_scan,
                   s->ro_list, s->n_flagged, s->waits, s->hidx, s->key_start, s->tile_sum,
                   s->tile_off, s->rank, s->cold_pos, s->sorted, s->rbucket, s->round_order,
-                  s->bo, s->bo2, s->max_count};
+                  s->bo, s->bo2, s->max_count, s->lock_last};
   for (void* b : bufs) cudaFree(b);
   for (auto& e : s->ev)
     if (e) cudaEventDestroy(e);
@@ -212,6 +215,7 @@ extern "C" csmv_status csmv_sched_probe(csmv_sched_t* s, csmv_bank_t* bank,
   ps.txn_aborts = s->aborts;
   ps.txn_waits = s->waits;
   ps.backoff = nullptr;
+  ps.lock_last = nullptr;
   ps.split_round = 0;
   ps.deferred_warps = 0;
   csmv_stats bst;
@@ -275,7 +279,7 @@ extern "C" csmv_status csmv_sched_plan_run(csmv_sched_t* s, csmv_bank_t* bank,
   uint32_t flagged = 0, deferred_rounds = 0;
   const uint32_t* run_op = d->op + t0;
   const uint32_t* run_off = d->off + t0;
-  bool with_backoff = false;
+  bool with_backoff = false, with_classes = false;
   if (U > 0 && s->cfg.plan == 1) {
     // grouped plan: hot accounts, keys by the two hottest accounts touched, counting sort,
     // rounds of 32 consecutive sorted transfers spread by hot account
@@ -324,6 +328,20 @@ extern "C" csmv_status csmv_sched_plan_run(csmv_sched_t* s, csmv_bank_t* bank,
                                                              s->ro_list, s->order, s->perm,
                                                              s->op2, s->off2);
     SCHED_LAUNCH_CHECK("emit");
+    uint32_t bank_n = 0;
+    if (s->cfg.hot_last && bank_group_commit(bank, &bank_n)) {
+      if (s->lock_last_n < bank_n) {
+        cudaFree(s->lock_last);
+        s->lock_last = nullptr;
+        s->lock_last_n = 0;
+        CSMV_CUDA(cudaMalloc(&s->lock_last, bank_n));
+        s->lock_last_n = bank_n;
+      }
+      sched_lock_last_kernel<<<grid_for(s, bank_n), 256, 0, s->stream>>>(bank_n, s->sketch, hot,
+                                                                         s->lock_last);
+      SCHED_LAUNCH_CHECK("lock classes");
+      with_classes = true;
+    }
     if (s->cfg.backoff_ns) {
       sched_plan_backoff_kernel<<<grid_for(s, n1), 256, 0, s->stream>>>(n1, t0, s->perm, s->bo,
                                                                        s->bo2);
@@ -384,6 +402,7 @@ extern "C" csmv_status csmv_sched_plan_run(csmv_sched_t* s, csmv_bank_t* bank,
   rs.txn_aborts = nullptr;
   rs.txn_waits = nullptr;
   rs.backoff = with_backoff ? s->bo2 : nullptr;
+  rs.lock_last = with_classes ? s->lock_last : nullptr;
   rs.split_round = s->split_round;
   rs.deferred_warps = s->split_round ? s->cfg.deferred_warps : 0;
   if (s->cfg.serial_lane && s->split_round) {  // the deferred rounds wait for the serial lane
@@ -424,6 +443,7 @@ extern "C" csmv_status csmv_sched_serial_run(csmv_sched_t* s, csmv_bank_t* bank,
   rs.txn_aborts = nullptr;
   rs.txn_waits = nullptr;
   rs.backoff = nullptr;
+  rs.lock_last = nullptr;
   rs.split_round = rs.deferred_warps = 0;
   csmv_stats bst;
   csmv_status st = s->cfg.serial_lane == 2 ? csmv_bank_run_flow_device(bank, &rs, &bst)

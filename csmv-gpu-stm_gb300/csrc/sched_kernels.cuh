@@ -311,6 +311,24 @@ __global__ void sched_hot_flags_kernel(const uint32_t* sketch, uint32_t hot_coun
     flag[i] = sketch[i] >= hot_count ? 1u : 0u;
 }
 
+// Heat class of every account of the bank for the engine's lock order: 0 below hot_count, else
+// 1 + 4 log2(count / hot_count) (quarter octaves, from the count's two bits below its leading
+// one), at most 255. Accounts sharing a sketch slot share its class; any class is a valid order.
+__global__ void sched_lock_last_kernel(uint32_t n_accounts, const uint32_t* sketch,
+                                       uint32_t hot_count, uint8_t* cls) {
+  for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n_accounts; x += gridDim.x * blockDim.x) {
+    const uint32_t c = sketch[sketch_slot(x)];
+    uint32_t k = 0;
+    if (c >= hot_count) {
+      const uint32_t q = c / max(hot_count, 1u);  // >= 1
+      const uint32_t l = 31u - __clz(q);
+      const uint32_t frac = l >= 2u ? (q >> (l - 2u)) & 3u : (l == 1u ? (q & 1u) << 1 : 0u);
+      k = min(255u, 1u + 4u * l + frac);
+    }
+    cls[x] = (uint8_t)k;
+  }
+}
+
 // score: 0 = the network's predicted probability p[t - t0]; 1 = the raw sketch-count score
 // (count of the transfer's most-accessed account / the chunk's largest count, no network).
 // backoff (ns) per transaction: 0 below a score of 1/4, else score x backoff_ns.

@@ -96,6 +96,13 @@ typedef struct csmv_bank_stream {
                               transaction's commit group found one of its write locks held by
                               another warp and waited for it (group commit), else 0 - a
                               conflict the engine resolved by waiting instead of aborting   */
+  const uint8_t* lock_last; /* optional [n_accounts of the bank] (same memory kind as op; group
+                              commit only): heat class of each account, 0 = none. Group commit
+                              takes the locks of classed accounts after all others, by class
+                              and account (the hottest last); a group that cannot take every
+                              lock at once queues, holding nothing, for its hottest account and
+                              takes its other locks at the head of that queue, so a hot lock is
+                              held only while its group commits (a scheduler's hot accounts) */
 } csmv_bank_stream;
 
 /* Account-choice distributions for the workload generator. */
@@ -450,6 +457,9 @@ typedef struct csmv_serve_config {
   uint32_t max_inflight_sets;  /* SET requests in flight at most (admission)                    */
   uint32_t idle_timeout_ms;    /* the kernel returns (error) after this long without work       */
   int32_t device;
+  uint32_t log_cap;            /* > 0: each session logs its commits (commit ts -> arena index
+                                  of the request, for its first log_cap timestamps) and every
+                                  request's outcome, for a replay by a checker; 0 = off       */
 } csmv_serve_config;
 typedef struct csmv_serve_t csmv_serve_t;
 void csmv_serve_config_default(csmv_serve_config* cfg);
@@ -468,6 +478,16 @@ csmv_status csmv_serve_submit(csmv_serve_t* s, const csmv_memcd_batch* host_batc
  * collected keep their slots, so admission stalls until they are polled. */
 csmv_status csmv_serve_poll(csmv_serve_t* s, uint64_t batch_id, uint32_t* done,
                             uint32_t* host_found, uint32_t* host_val_out, uint64_t* device_ns);
+/* As csmv_serve_poll, also copying each request's outcome to host_outcome [n] (log_cap > 0):
+ * the commit timestamp of a SET, the snapshot | 2^31 of a GET. */
+csmv_status csmv_serve_poll_logged(csmv_serve_t* s, uint64_t batch_id, uint32_t* done,
+                                   uint32_t* host_found, uint32_t* host_val_out,
+                                   uint32_t* host_outcome, uint64_t* device_ns);
+/* After csmv_serve_stop (log_cap > 0): host_log_txn[k] = arena index of the request that
+ * committed with timestamp *base_ts + k + 1 (0xFFFFFFFF: a hole), for the *n_used timestamps of
+ * the session (CSMV_ERR_CAPACITY when n_log is smaller). */
+csmv_status csmv_serve_read_log(csmv_serve_t* s, uint32_t* host_log_txn, uint32_t n_log,
+                                uint32_t* n_used, uint32_t* base_ts);
 /* Ends the session once every published batch is served; statistics of the session. */
 csmv_status csmv_serve_stop(csmv_serve_t* s, csmv_stats* out);
 /* Version store between sessions (layout as csmv_memcd_read_table). */
@@ -546,6 +566,10 @@ typedef struct csmv_sched_config {
                                  count / the chunk's largest), no network - the ablation      */
   uint32_t backoff_ns;        /* per-transaction retry backoff: score x backoff_ns for scores
                                  >= 1/4, else 0 (0 = no backoff array)                          */
+  uint32_t hot_last;          /* plan 1 on a group-commit bank: 1 (default) passes the plan's
+                                 hot accounts to the engine as heat classes (the stream's
+                                 lock_last, 1 + 4 log2(count / hot_count) capped at 255), so
+                                 they are locked last and queued for; 0 = plain account order */
 } csmv_sched_config;
 
 typedef struct csmv_sched_report {

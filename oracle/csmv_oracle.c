@@ -741,7 +741,8 @@ int orc_bank_sim_1warp(uint32_t n_txn, const uint32_t* op, const uint32_t* off,
             n_w++;
           }
           has[l] = nw > 0;
-          if (nw > 0 || fwd) {
+          (void)fwd;
+          if ((op[t] & 3u) != 0) { /* every transfer is a link, also one that writes nothing */
             links |= 1u << l;
           } else {
             outcome[t] = nowrite_snap(t, op, off, addr, slots, depth, locks, snap) | SNAP_FLAG;
@@ -752,6 +753,11 @@ int orc_bank_sim_1warp(uint32_t n_txn, const uint32_t* op, const uint32_t* off,
               st->commits_nowrite++;
           }
         }
+        /* the chain's links take consecutive timestamps; each written account gets one
+         * version, its last link's (the chain is published to the clock as one range) */
+        uint32_t ga[64], gts[64];
+        int32_t gv[64];
+        int gn = 0;
         for (int l = 0; l < 32; l++) {
           if (!((links >> l) & 1)) continue;
           uint32_t t = g * 32 + l, ts = ++clock;
@@ -759,13 +765,18 @@ int orc_bank_sim_1warp(uint32_t n_txn, const uint32_t* op, const uint32_t* off,
           outcome[t] = ts;
           result[t] = 0;
           if (has[l]) {
-            for (int k = 0; k < 2; k++)
-              orc_packed_writeback(slots + (uint64_t)ws_a[l][k] * depth, depth, ts, ws_v[l][k]);
+            for (int k = 0; k < 2; k++) {
+              ga[gn] = ws_a[l][k];
+              gts[gn] = ts;
+              gv[gn] = ws_v[l][k];
+              gn++;
+            }
             st->commits_update++;
           } else {
             st->commits_nowrite++;
           }
         }
+        flush_group(slots, depth, ga, gts, gv, &gn);
         free(round_val);
         pending = 0;
         continue;

@@ -1,12 +1,14 @@
 """GPU tests of the cache's serving loop (csmv_serve_*): results equal the batch engine's, a
 batch's results are the same served alone and in a mix of overlapping batches (exact: GET
-results are integers), and admission holds batches back until room frees up."""
+results are integers), overlapping batches that share hot keys replay exactly in the oracle
+from the session's commit log, and admission holds batches back until room frees up."""
 import time
 
 import numpy as np
 import pytest
 
 import csmv_gb300 as cg
+import oracle as orc
 
 pytestmark = pytest.mark.gpu
 
@@ -101,3 +103,53 @@ def test_admission_holds_batches_until_room_frees():
         st = srv.stop()
     assert refused > 0 and len(ids) >= 2 and st.error == 0
     assert st.commits_readonly + st.commits_update == 2048 * len(ids)
+
+
+def test_overlapping_batches_sharing_hot_keys_replay_exactly():
+    """Batches that GET and SET the SAME hot keys (Zipf over a small key set, inserts and
+    evictions included) are served overlapped; the session's commit log and every request's
+    outcome replay exactly in the oracle from the table the session started with: each SET's
+    installed entry and each GET's result equal the serial replay in commit order."""
+    n_sets = 1 << 10
+    n_b, per = 24, 2048
+    with cg.Server(n_sets=n_sets, client_warps=4, arena_requests=1 << 16,
+                   max_inflight_sets=1 << 15, log_cap=1 << 17) as srv:
+        srv.start()  # a session of fills, then the table it leaves is the replay's start
+        fill = cg.memcd_generate(cg.memcd_workload(1 << 13, 8192, seed=21, get_pct=0))
+        _wait(srv, srv.submit(fill, tick=1))
+        srv.stop()
+        table0 = srv.table()
+        reqs = [cg.memcd_generate(cg.memcd_workload(1 << 13, per, seed=100 + i,
+                                                    get_pct=60 + (i % 4) * 10,
+                                                    dist=cg.DIST_ZIPF, zipf_theta=0.99))
+                for i in range(n_b)]
+        srv.start()
+        ids = [srv.submit(r, tick=2) for r in reqs]
+        assert all(b is not None for b in ids)
+        overlapped = sum(srv.poll(b, results=False) is None for b in ids[1:])
+        res = [_poll_logged(srv, b) for b in ids]
+        st = srv.stop()
+        log_txn, base = srv.log()
+        tags, recs = srv.table()
+    assert st.error == 0
+    assert overlapped > 0, "the batches did not overlap"
+    kind = np.concatenate([r.kind for r in reqs])
+    key = np.concatenate([r.key for r in reqs])
+    val = np.concatenate([r.val for r in reqs])
+    found = np.concatenate([x[0] for x in res])
+    val_out = np.concatenate([x[1] for x in res])
+    outcome = np.concatenate([x[2] for x in res])
+    n_set = int(np.count_nonzero(kind == cg.MEMCD_SET))
+    assert st.commits_update == n_set and st.commits_readonly == kind.shape[0] - n_set
+    orc.memcd_check(kind, key, val, 2, n_sets, table0, base, log_txn, outcome, found, val_out,
+                    tags, recs)
+
+
+def _poll_logged(srv, bid, timeout=30.0):
+    t0 = time.time()
+    while True:
+        r = srv.poll(bid, outcome=True)
+        if r is not None:
+            return r
+        assert time.time() - t0 < timeout, "batch did not complete"
+        time.sleep(0.0002)

@@ -243,7 +243,10 @@ def test_one_warp_model_is_exact(prevalidate, locks):
     init = np.full(40, 100, np.int32)
     slots, log, outcome, result, st = orc.sim_1warp(op, off, addr, 40, init, 4, prevalidate, locks)
     assert st.commits_update + st.commits_readonly + st.commits_nowrite == len(op)
-    assert orc.check(op, off, addr, 40, init, 4, st.final_ts, log, outcome, result, slots) is None
+    # a chain (prevalidate 2) installs one version per account: its round is a commit group
+    g = round_groups(op, log[:st.final_ts]) if prevalidate == 2 else None
+    assert orc.check(op, off, addr, 40, init, 4, st.final_ts, log, outcome, result, slots,
+                     groups=g) is None
     if prevalidate == 2:  # the chain commits every transaction on its first attempt
         assert st.aborts_prevalid + st.aborts_read_write + st.aborts_write_write == 0
         assert st.rounds == len(op) // 32
