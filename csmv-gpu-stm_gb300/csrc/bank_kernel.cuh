@@ -315,7 +315,10 @@ static __device__ void complete_range(uint32_t* done, uint32_t done_mask, Global
   for (uint32_t attempt = 0; attempt < 4096; attempt++) {
     const uint32_t c = ld_acquire_gpu(&gs->clock);
     uint32_t n = c;
-    for (uint32_t words = 0; words < 64; words++) {  // bounded scan per attempt
+    // scan to the first incomplete timestamp, never a fixed number of words: a scan cut short
+    // could end inside a range and publish a clock no snapshot may take (at most the whole
+    // bitmap, which holds every timestamp in flight)
+    for (uint32_t words = 0; words <= done_mask; words++) {
       const uint32_t t = n + 1, bit = t & 31u;
       const uint32_t w = ld_acquire_gpu(&done[(t >> 5) & done_mask]) >> bit;
       const uint32_t ones = (w == 0xFFFFFFFFu) ? 32u : (uint32_t)(__ffs(~w) - 1);
