@@ -543,7 +543,7 @@ def serve_section(cg, local, loads=(0.1, 0.25, 0.5, 0.75, 1.0), per_load_s=1.5):
 
     with cg.Server(n_sets=1 << 20, client_warps=4, arena_requests=1 << 19,
                    max_inflight_sets=1 << 16, idle_timeout_ms=5000, device=local) as srv:
-        srv.start()
+        srv.start()  # a session of fills; the measured session starts from the table it leaves
         fill = cg.memcd_generate(cg.memcd_workload(1 << 22, 1 << 16, seed=5, get_pct=0))
         t_end = time.perf_counter() + 30
         for _ in range(8):
@@ -553,7 +553,9 @@ def serve_section(cg, local, loads=(0.1, 0.25, 0.5, 0.75, 1.0), per_load_s=1.5):
                 deadline_check(t_end, "fill")
             while srv.poll(b, results=False) is None:
                 deadline_check(t_end, "fill")
+        srv.stop()
         progress("serving: table filled")
+        srv.start()
         # closed loop: keep the ring full
         inflight, n_done, t0 = [], 0, time.perf_counter()
         t_end = t0 + 30
@@ -578,7 +580,7 @@ def serve_section(cg, local, loads=(0.1, 0.25, 0.5, 0.75, 1.0), per_load_s=1.5):
             n_b = max(20, int(rate * per_load_s))
             arrivals = np.cumsum(rng.exponential(1.0 / rate, n_b))
             reqs = [draw() for _ in range(n_b)]
-            lat, pending, inflight = [], 0, []
+            lat, dev_ns, pending, inflight = [], [], 0, []
             served = 0
             t0 = time.perf_counter()
             t_end = t0 + per_load_s * 4 + 10
@@ -593,22 +595,27 @@ def serve_section(cg, local, loads=(0.1, 0.25, 0.5, 0.75, 1.0), per_load_s=1.5):
                 i = 0
                 while i < len(inflight):
                     b, arr, n = inflight[i]
-                    if srv.poll(b, results=False) is not None:
+                    r = srv.poll(b, results=False)
+                    if r is not None:
                         lat.append(time.perf_counter() - t0 - arr)
+                        dev_ns.append(r[2])
                         served += n
                         inflight.pop(i)
                     else:
                         i += 1
             span = time.perf_counter() - t0
             lat = np.array(lat) * 1e3
+            dms = np.array(dev_ns) * 1e-6
             rows.append({"offered_frac": load, "offered_req_s": load * peak,
                          "achieved_req_s": served / span, "p50_ms": float(np.percentile(lat, 50)),
-                         "p99_ms": float(np.percentile(lat, 99)), "batches": n_b})
+                         "p99_ms": float(np.percentile(lat, 99)), "batches": n_b,
+                         "device_p50_ms": float(np.percentile(dms, 50)),
+                         "device_p99_ms": float(np.percentile(dms, 99))})
             replay.append((arrivals, reqs))
             progress(f"serving: load {load}: p50 {rows[-1]['p50_ms']:.3f} ms")
         st = srv.stop()
         out["loads"] = rows
-        out["abort_rate"] = st.aborts / max(1, st.aborts + st.commits)
+        out["abort_rate"] = st.aborts / max(1, st.aborts + st.commits)  # the measured session
     # the plain form at equal offered load: the same arrivals, one batch call at a time
     # (csmv_memcd_run with host buffers); a batch that arrives while another runs waits
     with cg.Memcd(n_sets=1 << 20, client_warps=4, max_req=1 << 16, log_commits=0,
