@@ -447,12 +447,10 @@ __device__ __forceinline__ bool group_wait_lock(const BankParams& p, uint32_t x,
 
 // One attempt of a transfer round as a commit group, warp-collective. Every active lane's
 // transfer may write its two accounts; the warp locks each such account once (its lowest writer
-// lane does), in ascending account order, waiting for a lock held elsewhere while it holds only
-// locks on smaller accounts (no cycle of waits is possible; a warp queued for a hot account
-// holds nothing, so the locks it needs next are free when its turn comes). Every access of this
-// mode to a commit word is a full 8-byte access. The locked accounts' latest values
-// are read under the locks; the commit server then gives the group consecutive timestamps in
-// lane order; every read of an account the group does not lock (a foreign read) is validated
+// lane does), in one total order (step 2), waiting for a lock held elsewhere while it holds only
+// smaller ones (no cycle of waits is possible). Every access of this mode to a commit word is a
+// full 8-byte access. The locked accounts' latest values are read under the locks; the group
+// then draws consecutive timestamps in lane order (one atomicAdd); every read of an account the group does not lock (a foreign read) is validated
 // against its commit word, as the stamp protocol validates any transaction; the lanes that pass
 // run in lane order as a chain through the locked accounts (each reads the value left by the
 // nearest lower lane that wrote it, else the locked value), so a dependent transfer never
@@ -623,13 +621,15 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
   const uint32_t inc = __ballot_sync(FULL, act);
   __syncwarp();
 
-  // 4. post the group to the commit server; the foreign reads run while it draws
-  seq++;
-  if (lane == 0) {
-    ms.snap = 0u;
-    ms.cand = inc;
-    mail_release<CLUSTER>(&ms.req, seq);
-  }
+  // 4. the group draws its consecutive timestamps itself: one atomicAdd on the timestamp cursor,
+  //    with SC fences on both sides as the commit server draws (the ready marks above are
+  //    ordered before the draw, the draw before the validation loads below); a group commits
+  //    with the lock of its hottest account held, so the server's mailbox round trip would sit
+  //    on that lock's critical path. The foreign reads are issued while the draw is in flight.
+  __syncwarp();
+  __threadfence();
+  uint32_t drawn = 0u;
+  if (lane == 0) drawn = atomicAdd(&p.gs->ts_next, __popc(inc));
   int32_t fv[MAXR];
   uint32_t fst[MAXR];
   bool fok = true;
@@ -639,19 +639,10 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
     fst[k] = 0u;
     if (act && k < (int)nr && rsl[k] < 0) fok &= read_latest<DEPTH>(vs, p.cw, a[k], fst[k], fv[k]);
   }
-  bool ok_wait = true;
-  if (lane == 0)
-    ok_wait = bounded_wait([&] { return mail_acquire<CLUSTER>(&ms.rep) == seq; }, &p.gs->error,
-                           ERR_WAIT_REPLY, p.spin_log2);
-  ok_wait = __shfl_sync(FULL, ok_wait, 0);
-  if (!ok_wait) {
-    failed = true;
-    return 0u;
-  }
-  (void)mail_acquire<CLUSTER>(&ms.rep);
-  const uint32_t base = ms.base, n_ts = __popc(inc);
+  const uint32_t base = __shfl_sync(FULL, drawn, 0), n_ts = __popc(inc);
   const uint32_t my_ts = base + 1u + __popc(inc & lanemask_lt());
-  fence_acq_rel_gpu();
+  __threadfence();
+  if (lane == 0) stat_add(sm.stat, ST_SECTIONS, 1);
 
   // 5. the group's first timestamp in its locks, then validation of the foreign reads: the stamp
   //    read must still be the latest, and a lock of a holder ordered before us (or whose
@@ -691,14 +682,82 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
   }
   const uint32_t fin = __ballot_sync(FULL, valid);
 
-  // 6. the chain, in lane order through the locked accounts
+  // 6. the chain, in lane order through the locked accounts. The value a lane reads from a locked
+  //    account is the value read under the lock plus the amounts every lower writer of it moved
+  //    (modular int32 sums: the same as applying them one after another). All lanes first solve
+  //    that triangular system together, by fixed-point iteration (each pass recomputes every
+  //    lane's amount and funds check from the previous pass's; a pass that changes nothing is
+  //    the lane-order solution, which is unique); a round that has not settled after a few
+  //    passes, or a transfer writing one account twice, runs the chain one level at a time.
+  uint32_t hw = 0u;
+  bool has_w = false, chained = false;
+  if (!__any_sync(FULL, valid && a[0] == a[1])) {
+    uint32_t mdeb[MAXR], mcre[MAXR];  // lower lanes debiting / crediting each read's account
+#pragma unroll
+    for (int k = 0; k < MAXR; k++) {
+      mdeb[k] = mcre[k] = 0u;
+      if (!valid || k >= (int)nr || rsl[k] < 0) continue;
+      for (uint32_t m = gx.wmask[rsl[k]] & fin & lanemask_lt(); m; m &= m - 1u) {
+        const uint32_t j = __ffs(m) - 1u;
+        if (gx.wa0[j] == a[k])
+          mdeb[k] |= 1u << j;
+        else
+          mcre[k] |= 1u << j;
+      }
+    }
+    uint32_t amt = 0u;
+    int32_t v[MAXR];
+    gx.out1[lane] = 0;
+    __syncwarp();
+    for (uint32_t pass = 0; pass < 6u; pass++) {
+#pragma unroll
+      for (int k = 0; k < MAXR; k++) {
+        v[k] = 0;
+        if (k >= (int)nr) continue;
+        if (rsl[k] < 0) {
+          v[k] = fv[k];
+          continue;
+        }
+        uint32_t x = (uint32_t)gx.base[rsl[k]];
+        for (uint32_t m = mcre[k] & hw; m; m &= m - 1u) x += (uint32_t)gx.out1[__ffs(m) - 1u];
+        for (uint32_t m = mdeb[k] & hw; m; m &= m - 1u) x -= (uint32_t)gx.out1[__ffs(m) - 1u];
+        v[k] = (int32_t)x;
+      }
+      uint32_t acc = CSMV_OP_AMT0(op) - 1u;
+#pragma unroll
+      for (int k = 2; k < MAXR; k++)
+        if (k < (int)nr) acc += (uint32_t)v[k];
+      const uint32_t a2 = valid ? 1u + acc % CSMV_OP_AMOD(op) : 0u;
+      const bool w2 = valid && (CSMV_OP_KIND(op) == CSMV_KIND_TRANSFER_ALWAYS || v[0] >= (int32_t)a2);
+      const bool changed = valid && (pass == 0u || a2 != amt || w2 != has_w);
+      __syncwarp();
+      gx.out1[lane] = (int32_t)a2;
+      amt = a2;
+      has_w = w2;
+      hw = __ballot_sync(FULL, has_w);
+      if (!__any_sync(FULL, changed)) {
+        chained = true;
+        break;
+      }
+    }
+    __syncwarp();
+    if (chained) {  // v holds the settled reads: the writes of each lane
+      gx.out0[lane] = (int32_t)((uint32_t)v[0] - amt);
+      gx.out1[lane] = (int32_t)((uint32_t)v[1] + amt);
+    }
+    __syncwarp();
+  }
   uint32_t dep = 0u;
 #pragma unroll
   for (int k = 0; k < MAXR; k++)
     if (valid && rsl[k] >= 0) dep |= gx.wmask[rsl[k]];
   dep &= fin & lanemask_lt();
-  uint32_t done = ~fin, hw = 0u;
-  bool computed = !valid, has_w = false;
+  uint32_t done = chained ? FULL : ~fin;
+  bool computed = !valid;
+  if (!chained) {
+    hw = 0u;
+    has_w = false;
+  }
   for (uint32_t it = 0; it < 33u && done != FULL; it++) {
     const bool ready = !computed && (dep & ~done) == 0u;
     if (ready) {
