@@ -366,9 +366,10 @@ def e2e_learned(torch, cg, host, s_addr, args, local, warm, timed):
 
 
 def hotspot_section(torch, cg, args, local):
-    """Learned vs plain on the shifting hotspot: 8 batches of 2^18 transactions. Three arms: plain
-    (the reference's commit method, stream order), group commit in stream order, and the learned
-    scheduler with group commit; tx/s on the host clock with planning and training included."""
+    """Learned vs plain on the shifting hotspot: batches of 2^20 transactions. Arms: plain (the
+    reference's commit method, stream order), group commit in stream order, the learned
+    scheduler with group commit, and two ablations of it (the raw sketch-count score instead of
+    the network; no backoff); tx/s on the host clock with planning and training included."""
     chunk, count = 1 << 20, 6
     s, bs = generate_batches("hotspot", chunk, count, pinned=False, seed=3, pr_read_pct=10,
                              ro_reads=8, up_reads=2, hot_frac=0.01, hot_prob=0.3,
@@ -377,12 +378,13 @@ def hotspot_section(torch, cg, args, local):
     dev = [DevBatch(torch, b) for b in bs]
     out = {}
     for arm, over, learned in (("plain", PLAIN, False), ("group_stream", ENGINE, False),
-                               ("learned", ENGINE, True)):
+                               ("learned", ENGINE, {}), ("learned_sketch_score", ENGINE, {"score": 1}),
+                               ("learned_no_backoff", ENGINE, {"backoff_ns": 0})):
         bank = cg.Bank(n_accounts=N_ACCOUNTS, version_depth=8, client_warps=2, ctas=152,
                        max_txn=chunk, log_commits=0, device=local, **over)
         bank.load()
-        sched = cg.Scheduler(n_accounts=N_ACCOUNTS, max_txn=chunk, device=local, plan=1) \
-            if learned else None
+        sched = cg.Scheduler(n_accounts=N_ACCOUNTS, max_txn=chunk, device=local, plan=1,
+                             **learned) if learned is not False else None
         c = a = 0
         t = 0.0
         for j, d in enumerate(dev):
@@ -808,6 +810,15 @@ def main():
                                     log_commits=0)
     plain, _ = run_engine(cg, dev, addr_dev, n_addr, args, local, list(range(min(n_cmp, 3))),
                           log_commits=0, **PLAIN)
+    # ablations of the learned arm, one warm-up and two timed batches each: the raw sketch-count
+    # score instead of the network, no backoff, no heat classes (plain account lock order)
+    ablations = {}
+    for name, over in (("sketch_score", dict(score=1)), ("no_backoff", dict(backoff_ns=0)),
+                       ("no_heat_classes", dict(hot_last=0))):
+        r = run_learned(torch, cg, dev, addr_dev, n_addr, args, local, 1, 2,
+                        sched_cfg=dict(SCHED, **over))
+        ablations[name] = {"tx_s": r["tx_s"], "abort_rate": r["abort_rate"],
+                           "flagged_per_step": r["flagged"] / 2}
     if rank != 0:
         return
     pk, pk_kind = peaks()
@@ -867,6 +878,7 @@ def main():
         "group_stream": {"tx_s": group_stream["tx_s"] * world,
                          "abort_rate": group_stream["abort_rate"], "steps": group_stream["steps"],
                          "method": "group commit in stream order, no scheduler"},
+        "ablations": ablations,
         "roofline": {"bound": "l2_atomic", "achieved": achieved_atomic,
                      "peak": atomics["spread_per_s"], "unit": "atomic/s",
                      "frac": achieved_atomic / atomics["spread_per_s"], "traffic": traffic,

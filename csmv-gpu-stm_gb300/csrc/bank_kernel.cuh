@@ -164,6 +164,12 @@ struct GroupScratch {
   int32_t base[kGrpSlots];    // its latest committed value, read under the warp's lock
   int32_t out0[32], out1[32]; // per lane: value written to its debit / credit account
   uint32_t wa0[32], wa1[32];  // per lane: its debit / credit account
+  // the chain walk's inputs per lane: table slots of its accounts, the part of its amount sum
+  // read outside the table, the slots of its other table reads, and its amount divisor
+  uint32_t cs[32];            // slot of a0 | slot of a1 << 8 | table reads << 16 | always << 24
+  uint32_t facc[32];
+  unsigned long long tr[32];  // up to 8 slots, one byte each
+  uint32_t md[32], mm[32];    // divisor and its multiply-shift magic
 };
 
 __host__ __device__ constexpr size_t group_scratch_offset(size_t cta_bytes) {
@@ -434,6 +440,21 @@ __device__ __forceinline__ bool group_lock_at_turn(const BankParams& p, uint32_t
   return false;
 }
 
+// One look at x's lock: when it is free, the slots are read and the lock taken by a CAS at the
+// stamp seen (as group_lock_at_turn does, without waiting).
+template <int DEPTH>
+__device__ __forceinline__ bool group_try_lock(const BankParams& p, uint32_t x, uint32_t me,
+                                               uint32_t& stamp, bool& stale,
+                                               SlotEditor<DEPTH>& ed, int32_t& v) {
+  const unsigned long long w = ld_acquire_gpu(&p.cw[x]);
+  if ((w >> 32) != 0ull) return false;
+  ed.load(p.slots + (size_t)x * DEPTH);
+  if (atomicCAS(&p.cw[x], w, w | ((unsigned long long)me << 32)) != w) return false;
+  stamp = (uint32_t)w;
+  stale = !ed.find(stamp, v);
+  return true;
+}
+
 // Queue for x's lock and take it (the turn is served on, also when the wait failed).
 template <int DEPTH>
 __device__ __forceinline__ bool group_wait_lock(const BankParams& p, uint32_t x, uint32_t me,
@@ -449,8 +470,8 @@ __device__ __forceinline__ bool group_wait_lock(const BankParams& p, uint32_t x,
 // transfer may write its two accounts; the warp locks each such account once (its lowest writer
 // lane does), in one total order (step 2), waiting for a lock held elsewhere while it holds only
 // smaller ones (no cycle of waits is possible). Every access of this mode to a commit word is a
-// full 8-byte access. The locked accounts' latest values are read under the locks; the group
-// then draws consecutive timestamps in lane order (one atomicAdd); every read of an account the group does not lock (a foreign read) is validated
+// full 8-byte access. The locked accounts' latest values are read under the locks; the commit
+// server then gives the group consecutive timestamps in lane order; every read of an account the group does not lock (a foreign read) is validated
 // against its commit word, as the stamp protocol validates any transaction; the lanes that pass
 // run in lane order as a chain through the locked accounts (each reads the value left by the
 // nearest lower lane that wrote it, else the locked value), so a dependent transfer never
@@ -465,11 +486,13 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
                                   MailSlot<MAXR, MAXW>& ms, GroupScratch& gx, uint32_t me,
                                   uint32_t t, uint32_t op, uint32_t nr,
                                   const uint32_t (&a)[MAXR], bool act, uint32_t& seq,
-                                  bool& gave_up, bool& failed, bool& waited) {
+                                  bool patient, bool& gave_up, bool& failed, bool& waited,
+                                  bool& sat_out) {
   constexpr uint32_t FULL = 0xFFFFFFFFu;
   const uint32_t lane = lane_id();
   const VersionStore vs{p.slots, p.n_items};
   gave_up = false;
+  sat_out = false;
   // 1. the accounts the round may write, with their writer lanes
   for (uint32_t i = lane; i < (uint32_t)kGrpSlots; i += 32) {
     gx.key[i] = kGrpEmpty;
@@ -543,6 +566,13 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
   bool all = false, ok = true;
   int turn = -1;  // which of my accounts' queue turn this lane holds (the group holds at most one)
   if (__any_sync(FULL, (lead0 && !h0) || (lead1 && !h1)) && __any_sync(FULL, c0 || c1)) {
+    // hot path: release all, queue (holding nothing) for the group's hottest account, and at
+    // the head of its queue take the other locks by CAS whenever they look free (never waiting
+    // for them) until the hottest lock itself is free, then take it. The lanes whose other
+    // accounts are still held elsewhere then sit this attempt out. A round that sat out twice
+    // running is patient: at the head it waits for its other locks in order, the hottest last.
+    // Every waiting group holds only locks below the one it waits for (a head's held locks are
+    // below its queued one), so keys rise along any chain of waits: no cycle.
     if (h0) st_relaxed_gpu(&p.cw[a[0]], (unsigned long long)st0);
     if (h1) st_relaxed_gpu(&p.cw[a[1]], (unsigned long long)st1);
     h0 = h1 = false;
@@ -559,77 +589,108 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
       if (r) turn = 1;
     }
     ok = !__any_sync(FULL, !r);
+    const uint64_t limit = 1ull << min(p.spin_log2, 22u);
+    for (uint64_t it = 0; ok && !patient && it < limit; it++) {
+      if (lead0 && !h0 && turn != 0 && (ld_relaxed_gpu(&p.cw[a[0]]) >> 32) == 0ull)
+        h0 = group_cas_lock(p.cw, a[0], me, st0, stale0);
+      if (lead1 && !h1 && turn != 1 && (ld_relaxed_gpu(&p.cw[a[1]]) >> 32) == 0ull)
+        h1 = group_cas_lock(p.cw, a[1], me, st1, stale1);
+      if (turn == 0 && !h0) h0 = group_try_lock<DEPTH>(p, a[0], me, st0, stale0, ed0, bv0);
+      if (turn == 1 && !h1) h1 = group_try_lock<DEPTH>(p, a[1], me, st1, stale1, ed1, bv1);
+      if (__any_sync(FULL, (turn == 0 && h0) || (turn == 1 && h1))) {
+        all = true;
+        break;
+      }
+      if ((it & 63u) == 63u && __any_sync(FULL, lane == 0 && ld_relaxed_gpu(&p.gs->error) != 0u))
+        break;
+      __nanosleep(32);
+    }
+    if (ok && !patient && !all && lane == 0) raise_error(&p.gs->error, ERR_WAIT_TURN);
   }
-  for (uint32_t it = 0; ok && it <= 64u; it++) {  // each pass settles the smallest missing lock
-    uint32_t fh, fl;
-    key_min(lead0 && !h0, lead1 && !h1, fh, fl);
-    if (fl == kGrpEmpty) {
-      all = true;
-      break;
+  if (ok && !all) {
+    for (uint32_t it = 0; it <= 64u; it++) {  // each pass settles the smallest missing lock
+      uint32_t fh, fl;
+      key_min(lead0 && !h0, lead1 && !h1, fh, fl);
+      if (fl == kGrpEmpty) {
+        all = true;
+        break;
+      }
+      if (h0 && above(kh0, a[0], fh, fl)) {  // hold nothing above the lock being waited for
+        st_relaxed_gpu(&p.cw[a[0]], (unsigned long long)st0);
+        h0 = false;
+      }
+      if (h1 && above(kh1, a[1], fh, fl)) {
+        st_relaxed_gpu(&p.cw[a[1]], (unsigned long long)st1);
+        h1 = false;
+      }
+      bool r = true;  // a hot lock is polled (its queue's turn is this group's or another's)
+      if (lead0 && !h0 && kh0 == fh && a[0] == fl)
+        r = h0 = c0 ? group_lock_at_turn<DEPTH>(p, a[0], me, st0, stale0, ed0, bv0)
+                    : group_wait_lock<DEPTH>(p, a[0], me, st0, stale0, ed0, bv0);
+      else if (lead1 && !h1 && kh1 == fh && a[1] == fl)
+        r = h1 = c1 ? group_lock_at_turn<DEPTH>(p, a[1], me, st1, stale1, ed1, bv1)
+                    : group_wait_lock<DEPTH>(p, a[1], me, st1, stale1, ed1, bv1);
+      if (__any_sync(FULL, !r)) break;
+      if (lead0 && !h0 && above(kh0, a[0], fh, fl)) h0 = group_cas_lock(p.cw, a[0], me, st0, stale0);
+      if (lead1 && !h1 && above(kh1, a[1], fh, fl)) h1 = group_cas_lock(p.cw, a[1], me, st1, stale1);
     }
-    if (h0 && above(kh0, a[0], fh, fl)) {  // hold nothing above the lock being waited for
-      st_relaxed_gpu(&p.cw[a[0]], (unsigned long long)st0);
-      h0 = false;
-    }
-    if (h1 && above(kh1, a[1], fh, fl)) {
-      st_relaxed_gpu(&p.cw[a[1]], (unsigned long long)st1);
-      h1 = false;
-    }
-    bool r = true;
-    if (lead0 && !h0 && kh0 == fh && a[0] == fl)
-      r = h0 = c0 ? group_lock_at_turn<DEPTH>(p, a[0], me, st0, stale0, ed0, bv0)
-                  : group_wait_lock<DEPTH>(p, a[0], me, st0, stale0, ed0, bv0);
-    else if (lead1 && !h1 && kh1 == fh && a[1] == fl)
-      r = h1 = c1 ? group_lock_at_turn<DEPTH>(p, a[1], me, st1, stale1, ed1, bv1)
-                  : group_wait_lock<DEPTH>(p, a[1], me, st1, stale1, ed1, bv1);
-    if (__any_sync(FULL, !r)) break;
-    if (lead0 && !h0 && above(kh0, a[0], fh, fl)) h0 = group_cas_lock(p.cw, a[0], me, st0, stale0);
-    if (lead1 && !h1 && above(kh1, a[1], fh, fl)) h1 = group_cas_lock(p.cw, a[1], me, st1, stale1);
   }
   if (turn >= 0) group_pass_turn(p, turn == 0 ? a[0] : a[1]);  // the next in line starts now
-  if (!all) {  // a wait ran out: release everything, the round retries later
+  // the accounts held; a lane sits the attempt out when one of its own is not (hot path only)
+  const bool own0 = lead0 && h0, own1 = lead1 && h1;
+  if (lead0) gx.busy[s0] = own0 ? 0u : 1u;
+  if (lead1) gx.busy[s1] = own1 ? 0u : 1u;
+  __syncwarp();
+  const bool in = act && all && gx.busy[s0] == 0u && gx.busy[s1] == 0u;
+  if (in) {  // a read of a table account this group does not hold becomes a foreign read
+#pragma unroll
+    for (int k = 2; k < MAXR; k++)
+      if (rsl[k] >= 0 && gx.busy[rsl[k]] != 0u) rsl[k] = -1;
+  }
+  const uint32_t inc = __ballot_sync(FULL, in);
+  const uint32_t actm = __ballot_sync(FULL, act);
+  sat_out = all && actm != inc;
+  if (!all || inc == 0u) {  // a wait ran out, or no lane can commit now: release, retry later
     if (h0) st_relaxed_gpu(&p.cw[a[0]], (unsigned long long)st0);
     if (h1) st_relaxed_gpu(&p.cw[a[1]], (unsigned long long)st1);
-    gave_up = true;
+    gave_up = !all;
+    if (all && lane == 0) stat_add(sm.stat, ST_ABORT_WRITE_WRITE, __popc(actm));
     return 0u;
   }
   // 3. latest values of the locked accounts whose slots were read before their stamp moved (the
   //    stamp cannot move while the lock is held), then the ready marks: every lock of the group
   //    is held and its timestamps are drawn next (the server's fence orders these marks before
   //    its draw: the mailbox hand-off carries them to it)
-  if (__any_sync(FULL, (lead0 && stale0) || (lead1 && stale1))) {
+  if (__any_sync(FULL, (own0 && stale0) || (own1 && stale1))) {
     fence_acq_rel_gpu();  // the previous holders' versions are visible before they are read
     bool lost = false;
-    if (lead0 && stale0) {
+    if (own0 && stale0) {
       ed0.load(p.slots + (size_t)a[0] * DEPTH);
       lost |= !ed0.find(st0, bv0);
     }
-    if (lead1 && stale1) {
+    if (own1 && stale1) {
       ed1.load(p.slots + (size_t)a[1] * DEPTH);
       lost |= !ed1.find(st1, bv1);
     }
     if (lost) raise_error(&p.gs->error, ERR_DATA);  // the latest version must be present
   }
-  if (lead0) {
+  if (own0) {
     gx.base[s0] = bv0;
     st_relaxed_gpu(&p.cw[a[0]], lock_word(st0, me | kReadyFlag));
   }
-  if (lead1) {
+  if (own1) {
     gx.base[s1] = bv1;
     st_relaxed_gpu(&p.cw[a[1]], lock_word(st1, me | kReadyFlag));
   }
-  const uint32_t inc = __ballot_sync(FULL, act);
   __syncwarp();
 
-  // 4. the group draws its consecutive timestamps itself: one atomicAdd on the timestamp cursor,
-  //    with SC fences on both sides as the commit server draws (the ready marks above are
-  //    ordered before the draw, the draw before the validation loads below); a group commits
-  //    with the lock of its hottest account held, so the server's mailbox round trip would sit
-  //    on that lock's critical path. The foreign reads are issued while the draw is in flight.
-  __syncwarp();
-  __threadfence();
-  uint32_t drawn = 0u;
-  if (lane == 0) drawn = atomicAdd(&p.gs->ts_next, __popc(inc));
+  // 4. post the group to the commit server; the foreign reads run while it draws
+  seq++;
+  if (lane == 0) {
+    ms.snap = 0u;
+    ms.cand = inc;
+    mail_release<CLUSTER>(&ms.req, seq);
+  }
   int32_t fv[MAXR];
   uint32_t fst[MAXR];
   bool fok = true;
@@ -637,20 +698,29 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
   for (int k = 0; k < MAXR; k++) {
     fv[k] = 0;
     fst[k] = 0u;
-    if (act && k < (int)nr && rsl[k] < 0) fok &= read_latest<DEPTH>(vs, p.cw, a[k], fst[k], fv[k]);
+    if (in && k < (int)nr && rsl[k] < 0) fok &= read_latest<DEPTH>(vs, p.cw, a[k], fst[k], fv[k]);
   }
-  const uint32_t base = __shfl_sync(FULL, drawn, 0), n_ts = __popc(inc);
+  bool ok_wait = true;
+  if (lane == 0)
+    ok_wait = bounded_wait([&] { return mail_acquire<CLUSTER>(&ms.rep) == seq; }, &p.gs->error,
+                           ERR_WAIT_REPLY, p.spin_log2);
+  ok_wait = __shfl_sync(FULL, ok_wait, 0);
+  if (!ok_wait) {
+    failed = true;
+    return 0u;
+  }
+  (void)mail_acquire<CLUSTER>(&ms.rep);
+  const uint32_t base = ms.base, n_ts = __popc(inc);
   const uint32_t my_ts = base + 1u + __popc(inc & lanemask_lt());
-  __threadfence();
-  if (lane == 0) stat_add(sm.stat, ST_SECTIONS, 1);
+  fence_acq_rel_gpu();
 
   // 5. the group's first timestamp in its locks, then validation of the foreign reads: the stamp
   //    read must still be the latest, and a lock of a holder ordered before us (or whose
   //    timestamps are being drawn) must be resolved first. Waits point only to earlier
   //    timestamps or to holders already drawing: no cycles.
-  if (lead0) st_relaxed_gpu(&p.cw[a[0]], lock_word(st0, kPendingFlag | (base + 1u)));
-  if (lead1) st_relaxed_gpu(&p.cw[a[1]], lock_word(st1, kPendingFlag | (base + 1u)));
-  bool valid = act && fok;
+  if (own0) st_relaxed_gpu(&p.cw[a[0]], lock_word(st0, kPendingFlag | (base + 1u)));
+  if (own1) st_relaxed_gpu(&p.cw[a[1]], lock_word(st1, kPendingFlag | (base + 1u)));
+  bool valid = in && fok;
   if (valid) {
     unsigned long long word[MAXR];
 #pragma unroll
@@ -682,112 +752,58 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
   }
   const uint32_t fin = __ballot_sync(FULL, valid);
 
-  // 6. the chain, in lane order through the locked accounts. The value a lane reads from a locked
-  //    account is the value read under the lock plus the amounts every lower writer of it moved
-  //    (modular int32 sums: the same as applying them one after another). All lanes first solve
-  //    that triangular system together, by fixed-point iteration (each pass recomputes every
-  //    lane's amount and funds check from the previous pass's; a pass that changes nothing is
-  //    the lane-order solution, which is unique); a round that has not settled after a few
-  //    passes, or a transfer writing one account twice, runs the chain one level at a time.
-  uint32_t hw = 0u;
-  bool has_w = false, chained = false;
-  if (!__any_sync(FULL, valid && a[0] == a[1])) {
-    uint32_t mdeb[MAXR], mcre[MAXR];  // lower lanes debiting / crediting each read's account
+  // 6. the chain, in lane order through the locked accounts: each lane stages what its transfer
+  //    needs (table slots, the part of its amount read outside the table, its divisor), and
+  //    lane 0 walks the lanes that passed in lane order over the table's values in shared
+  //    memory, which it updates as it goes (a transfer writes a1 last), recording each writer's
+  //    outputs - a dependent chain of shared-memory accesses, not of warp-wide steps.
+  if (valid) {
+    uint32_t facc = CSMV_OP_AMT0(op) - 1u, ntr = 0u;
+    unsigned long long tr = ~0ull;
 #pragma unroll
-    for (int k = 0; k < MAXR; k++) {
-      mdeb[k] = mcre[k] = 0u;
-      if (!valid || k >= (int)nr || rsl[k] < 0) continue;
-      for (uint32_t m = gx.wmask[rsl[k]] & fin & lanemask_lt(); m; m &= m - 1u) {
-        const uint32_t j = __ffs(m) - 1u;
-        if (gx.wa0[j] == a[k])
-          mdeb[k] |= 1u << j;
-        else
-          mcre[k] |= 1u << j;
+    for (int k = 2; k < MAXR; k++) {
+      if (k >= (int)nr) continue;
+      if (rsl[k] < 0) {
+        facc += (uint32_t)fv[k];
+      } else {
+        tr = (tr & ~(0xFFull << (8u * ntr))) | ((unsigned long long)rsl[k] << (8u * ntr));
+        ntr++;
       }
     }
-    uint32_t amt = 0u;
-    int32_t v[MAXR];
-    gx.out1[lane] = 0;
-    __syncwarp();
-    for (uint32_t pass = 0; pass < 6u; pass++) {
-#pragma unroll
-      for (int k = 0; k < MAXR; k++) {
-        v[k] = 0;
-        if (k >= (int)nr) continue;
-        if (rsl[k] < 0) {
-          v[k] = fv[k];
-          continue;
-        }
-        uint32_t x = (uint32_t)gx.base[rsl[k]];
-        for (uint32_t m = mcre[k] & hw; m; m &= m - 1u) x += (uint32_t)gx.out1[__ffs(m) - 1u];
-        for (uint32_t m = mdeb[k] & hw; m; m &= m - 1u) x -= (uint32_t)gx.out1[__ffs(m) - 1u];
-        v[k] = (int32_t)x;
-      }
-      uint32_t acc = CSMV_OP_AMT0(op) - 1u;
-#pragma unroll
-      for (int k = 2; k < MAXR; k++)
-        if (k < (int)nr) acc += (uint32_t)v[k];
-      const uint32_t a2 = valid ? 1u + acc % CSMV_OP_AMOD(op) : 0u;
-      const bool w2 = valid && (CSMV_OP_KIND(op) == CSMV_KIND_TRANSFER_ALWAYS || v[0] >= (int32_t)a2);
-      const bool changed = valid && (pass == 0u || a2 != amt || w2 != has_w);
-      __syncwarp();
-      gx.out1[lane] = (int32_t)a2;
-      amt = a2;
-      has_w = w2;
-      hw = __ballot_sync(FULL, has_w);
-      if (!__any_sync(FULL, changed)) {
-        chained = true;
-        break;
-      }
-    }
-    __syncwarp();
-    if (chained) {  // v holds the settled reads: the writes of each lane
-      gx.out0[lane] = (int32_t)((uint32_t)v[0] - amt);
-      gx.out1[lane] = (int32_t)((uint32_t)v[1] + amt);
-    }
-    __syncwarp();
+    const uint32_t d = CSMV_OP_AMOD(op);
+    gx.cs[lane] = (uint32_t)s0 | ((uint32_t)s1 << 8) | (ntr << 16) |
+                  ((CSMV_OP_KIND(op) == CSMV_KIND_TRANSFER_ALWAYS ? 1u : 0u) << 24);
+    gx.facc[lane] = facc;
+    gx.tr[lane] = tr;
+    gx.md[lane] = d;
+    gx.mm[lane] = 0xFFFFFFFFu / d;
   }
-  uint32_t dep = 0u;
-#pragma unroll
-  for (int k = 0; k < MAXR; k++)
-    if (valid && rsl[k] >= 0) dep |= gx.wmask[rsl[k]];
-  dep &= fin & lanemask_lt();
-  uint32_t done = chained ? FULL : ~fin;
-  bool computed = !valid;
-  if (!chained) {
-    hw = 0u;
-    has_w = false;
-  }
-  for (uint32_t it = 0; it < 33u && done != FULL; it++) {
-    const bool ready = !computed && (dep & ~done) == 0u;
-    if (ready) {
-      int32_t v[MAXR];
-#pragma unroll
-      for (int k = 0; k < MAXR; k++) {
-        v[k] = 0;
-        if (k >= (int)nr) continue;
-        if (rsl[k] < 0) {
-          v[k] = fv[k];
-        } else {
-          const uint32_t wr = gx.wmask[rsl[k]] & hw & lanemask_lt();
-          if (wr) {
-            const uint32_t j = 31u - __clz(wr);
-            v[k] = gx.wa1[j] == a[k] ? gx.out1[j] : gx.out0[j];  // a transfer writes a1 last
-          } else {
-            v[k] = gx.base[rsl[k]];
-          }
-        }
+  __syncwarp();
+  uint32_t hwm = 0u;
+  if (lane == 0) {
+    for (uint32_t m = fin; m; m &= m - 1u) {
+      const uint32_t j = __ffs(m) - 1u;
+      const uint32_t cs = gx.cs[j], x0 = cs & 0xFFu, x1 = (cs >> 8) & 0xFFu, n = (cs >> 16) & 0xFFu;
+      const int32_t v0 = gx.base[x0], v1 = gx.base[x1];
+      uint32_t acc = gx.facc[j];
+      const unsigned long long tr = gx.tr[j];
+      for (uint32_t q = 0; q < n; q++) acc += (uint32_t)gx.base[(tr >> (8u * q)) & 0xFFu];
+      const uint32_t d = gx.md[j];
+      uint32_t r = acc - __umulhi(acc, gx.mm[j]) * d;  // acc mod d (one correction suffices)
+      if (r >= d) r -= d;
+      const uint32_t amt = 1u + r;
+      if ((cs >> 24) != 0u || v0 >= (int32_t)amt) {
+        const int32_t w0 = (int32_t)((uint32_t)v0 - amt), w1 = (int32_t)((uint32_t)v1 + amt);
+        gx.base[x0] = w0;
+        gx.base[x1] = w1;
+        gx.out0[j] = w0;
+        gx.out1[j] = w1;
+        hwm |= 1u << j;
       }
-      int32_t w0 = 0, w1 = 0;
-      has_w = transfer_writes<MAXR>(op, nr, v, w0, w1);
-      gx.out0[lane] = w0;
-      gx.out1[lane] = w1;
-      computed = true;
     }
-    done |= __ballot_sync(FULL, ready);
-    hw |= __ballot_sync(FULL, ready && has_w);
-    __syncwarp();
   }
+  const uint32_t hw = __shfl_sync(FULL, hwm, 0);
+  __syncwarp();
 
   // 7. one version per locked account (its last writer's), then the stamp (a release store: the
   //    version is visible first) and the unlock
@@ -802,13 +818,13 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
     return ts;
   };
   uint32_t pub0 = 0u, pub1 = 0u;
-  if (lead0) pub0 = install(s0, a[0], ed0);
-  if (lead1) pub1 = install(s1, a[1], ed1);
-  if (lead0) st_release_gpu(&p.cw[a[0]], (unsigned long long)(pub0 ? pub0 : st0));
-  if (lead1) st_release_gpu(&p.cw[a[1]], (unsigned long long)(pub1 ? pub1 : st1));
+  if (own0) pub0 = install(s0, a[0], ed0);
+  if (own1) pub1 = install(s1, a[1], ed1);
+  if (own0) st_release_gpu(&p.cw[a[0]], (unsigned long long)(pub0 ? pub0 : st0));
+  if (own1) st_release_gpu(&p.cw[a[1]], (unsigned long long)(pub1 ? pub1 : st1));
 
   // 8. log, outcomes, the group's end, completion
-  if (p.log && act) {
+  if (p.log && in) {
     const uint32_t li = my_ts - 1u - p.log_base;
     if (li < p.log_cap)
       p.log_txn[li] = valid ? t : kHole;
@@ -829,6 +845,7 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
     stat_add(sm.stat, ST_COMMIT_UPDATE, __popc(hw));
     stat_add(sm.stat, ST_COMMIT_NOWRITE, __popc(fin & ~hw));
     stat_add(sm.stat, ST_ABORT_READ_WRITE, __popc(inc & ~fin));
+    stat_add(sm.stat, ST_ABORT_WRITE_WRITE, __popc(actm & ~inc));  // sat out: a lock was held
   }
   return fin;
 }
@@ -894,7 +911,7 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
     }
 
     uint32_t pending = 0xFFFFFFFFu;
-    uint32_t attempts = 0, lock_fails = 0, tries = 0, stuck = 0;
+    uint32_t attempts = 0, lock_fails = 0, tries = 0, stuck = 0, sat_outs = 0;
     if (p.txn_waits) p.txn_waits[t] = 0u;
     while (pending) {
       if (lane == 0) atomicAdd(&sm.stat[ST_ROUNDS], 1ull);
@@ -949,9 +966,11 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
       }
 
       if (stamp && p.prevalidate == 3) {  // group commit of the round's transfers
-        bool gave_up = false, waited = false;
+        bool gave_up = false, waited = false, sat = false;
         const uint32_t fin = group_attempt<DEPTH, MAXR, MAXW, CLUSTER>(
-            p, sm, ms, *gx, me, t, op, nr, a, mine, seq, gave_up, failed, waited);
+            p, sm, ms, *gx, me, t, op, nr, a, mine, seq, sat_outs >= 2u, gave_up, failed,
+            waited, sat);
+        sat_outs = sat ? sat_outs + 1u : 0u;
         if (failed) break;
         if (p.txn_waits && waited) p.txn_waits[t] = 1u;
         if (lane == 0 && gave_up) stat_add(sm.stat, ST_ABORT_WRITE_WRITE, __popc(pending));
