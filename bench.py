@@ -865,7 +865,7 @@ def main():
         "learned": {"tx_s": value, "abort_rate": learned["abort_rate"],
                     "engine_validated": "every transaction: locks, server timestamps, validation",
                     "flagged_per_step": learned["flagged"] / timed,
-                    "aborts_by_kind": {"lock_wait_gave_up": learned["ww"],
+                    "aborts_by_kind": {"write_write_lock_held": learned["ww"],
                                        "read_validation": learned["rw"],
                                        "data_age": learned["age"]},
                     "plan_ms_per_step": learned["plan_ms"] / timed,

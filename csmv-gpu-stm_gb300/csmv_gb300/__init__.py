@@ -108,11 +108,16 @@ class MemcdConfig(C.Structure):
 
 class TuneTrial(C.Structure):
     _fields_ = [(n, C.c_uint32) for n in ("client_warps", "ctas", "version_depth", "runs")] + [
-        ("status", C.c_int32), ("tx_per_s", C.c_double), ("abort_rate", C.c_double)]
+        ("status", C.c_int32), ("tx_per_s", C.c_double), ("abort_rate", C.c_double),
+        ("prevalidate", C.c_uint32), ("max_reads", C.c_uint32)]
 
 
 class TuneResult(C.Structure):
     _fields_ = [("best", BankConfig), ("n_trials", C.c_uint32), ("trials", TuneTrial * 64)]
+
+
+class MemcdTuneResult(C.Structure):
+    _fields_ = [("best", MemcdConfig), ("n_trials", C.c_uint32), ("trials", TuneTrial * 64)]
 
 
 class ServeConfig(C.Structure):
@@ -207,6 +212,8 @@ def lib() -> C.CDLL:
         "csmv_mlp_destroy": (None, [P]),
         "csmv_bank_autotune": (I32, [C.POINTER(BankConfig), C.POINTER(BankStream), P, U32,
                                      C.POINTER(TuneResult)]),
+        "csmv_memcd_autotune": (I32, [C.POINTER(MemcdConfig), C.POINTER(MemcdBatch),
+                                      C.POINTER(MemcdBatch), U32, C.POINTER(MemcdTuneResult)]),
         "csmv_serve_config_default": (None, [C.POINTER(ServeConfig)]),
         "csmv_serve_create": (I32, [C.POINTER(ServeConfig), C.POINTER(P)]),
         "csmv_serve_start": (I32, [P]),
@@ -892,6 +899,23 @@ def autotune(stream: Stream, repeats: int = 3, init: np.ndarray | None = None, *
         init_p = _ptr(init)
     _check(lib().csmv_bank_autotune(C.byref(cfg), C.byref(s), init_p, repeats, C.byref(res)),
            "csmv_bank_autotune")
+    trials = [{n: getattr(t, n) for n, _ in TuneTrial._fields_} for t in res.trials[:res.n_trials]]
+    return res.best, trials
+
+
+def memcd_autotune(sample: Requests, fill: Requests | None = None, repeats: int = 3,
+                   tick: int = 2, **base):
+    """Pick the cache's launch shape (csmv_memcd_autotune): `fill` runs first on each fresh
+    candidate (tick 1), then `sample` is timed. Returns (best MemcdConfig, trial dicts; tx_per_s
+    is requests/s)."""
+    cfg = memcd_config(**base)
+    res = MemcdTuneResult()
+    def batch(r, t):
+        return MemcdBatch(r.n_req, t, _ptr(r.kind), _ptr(r.key), _ptr(r.val), None, None)
+    fb = batch(fill, 1) if fill is not None else None
+    sb = batch(sample, tick)
+    _check(lib().csmv_memcd_autotune(C.byref(cfg), C.byref(fb) if fb is not None else None,
+                                     C.byref(sb), repeats, C.byref(res)), "csmv_memcd_autotune")
     trials = [{n: getattr(t, n) for n, _ in TuneTrial._fields_} for t in res.trials[:res.n_trials]]
     return res.best, trials
 

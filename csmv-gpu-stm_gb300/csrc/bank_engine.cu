@@ -665,19 +665,34 @@ extern "C" csmv_status csmv_bank_autotune(const csmv_bank_config* base,
   int n_sms = 0;
   csmv_status st = check_device(base->device, &n_sms);
   if (st != CSMV_OK) return st;
+  // commit methods and read specialisations worth trying on this sample
+  std::vector<uint32_t> methods{base->prevalidate}, reads{base->max_reads};
+  if (base->validate == CSMV_VALIDATE_STAMP) methods = {1u, 3u};
+  if (host_sample->op) {
+    uint32_t widest = 0;
+    for (uint32_t i = 0; i < host_sample->n_txn; i++) {
+      const uint32_t o = host_sample->op[i];
+      if (CSMV_OP_KIND(o) != CSMV_KIND_READONLY) widest = std::max(widest, CSMV_OP_NREADS(o));
+    }
+    if (widest <= 4u) reads = {0u, 4u};
+  }
   std::vector<Trial> trials;
-  for (uint32_t depth : {4u, 8u})
-    for (uint32_t cw : {1u, 2u, 4u, 8u})
-      for (uint32_t per_sm : {1u, 2u}) {
-        Trial t;
-        t.cfg = *base;
-        t.cfg.version_depth = depth;
-        t.cfg.client_warps = cw;
-        t.cfg.ctas = per_sm * (uint32_t)n_sms;
-        t.cfg.max_txn = std::max(base->max_txn, host_sample->n_txn);
-        t.cfg.log_commits = 0;
-        trials.push_back(t);
-      }
+  for (uint32_t method : methods)
+    for (uint32_t mr : reads)
+      for (uint32_t depth : {4u, 8u})
+        for (uint32_t cw : {1u, 2u, 4u, 8u})
+          for (uint32_t per_sm : {1u, 2u}) {
+            Trial t;
+            t.cfg = *base;
+            t.cfg.prevalidate = method;
+            t.cfg.max_reads = mr;
+            t.cfg.version_depth = depth;
+            t.cfg.client_warps = cw;
+            t.cfg.ctas = per_sm * (uint32_t)n_sms;
+            t.cfg.max_txn = std::max(base->max_txn, host_sample->n_txn);
+            t.cfg.log_commits = 0;
+            trials.push_back(t);
+          }
   for (auto& t : trials) {
     t.st = tune_run(t.cfg, host_sample, host_init, 1, t);
     if (t.st == CSMV_OK) t.best_ms = t.ms.back();
@@ -715,6 +730,8 @@ extern "C" csmv_status csmv_bank_autotune(const csmv_bank_config* base,
     o.status = (int32_t)t.st;
     o.tx_per_s = t.st == CSMV_OK ? host_sample->n_txn / (t.best_ms * 1e-3) : 0.0;
     o.abort_rate = t.abort_rate;
+    o.prevalidate = t.cfg.prevalidate;
+    o.max_reads = t.cfg.max_reads;
   }
   return CSMV_OK;
 }

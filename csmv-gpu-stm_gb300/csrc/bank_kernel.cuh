@@ -752,58 +752,90 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
   }
   const uint32_t fin = __ballot_sync(FULL, valid);
 
-  // 6. the chain, in lane order through the locked accounts: each lane stages what its transfer
-  //    needs (table slots, the part of its amount read outside the table, its divisor), and
-  //    lane 0 walks the lanes that passed in lane order over the table's values in shared
-  //    memory, which it updates as it goes (a transfer writes a1 last), recording each writer's
-  //    outputs - a dependent chain of shared-memory accesses, not of warp-wide steps.
-  if (valid) {
-    uint32_t facc = CSMV_OP_AMT0(op) - 1u, ntr = 0u;
-    unsigned long long tr = ~0ull;
+  // 6. the chain, in lane order through the locked accounts. Every lane first computes its
+  //    transfer from the values read under the locks; that result is final for a lane no lower
+  //    lane writes any of its accounts to (every writer of an account also reads it, so two
+  //    writers of one account are always dependent). When some lanes depend on lower ones, each
+  //    stages what its transfer needs (table slots, the part of its amount sum read outside the
+  //    table, its divisor) and lane 0 walks the lanes in order over the table's values in shared
+  //    memory, applying the independent lanes' writes and recomputing the dependent ones (a
+  //    transfer writes a1 last): a chain of dependent shared-memory accesses.
+  uint32_t dep = 0u;
 #pragma unroll
-    for (int k = 2; k < MAXR; k++) {
-      if (k >= (int)nr) continue;
-      if (rsl[k] < 0) {
-        facc += (uint32_t)fv[k];
-      } else {
-        tr = (tr & ~(0xFFull << (8u * ntr))) | ((unsigned long long)rsl[k] << (8u * ntr));
-        ntr++;
+  for (int k = 0; k < MAXR; k++)
+    if (valid && k < (int)nr && rsl[k] >= 0) dep |= gx.wmask[rsl[k]];
+  dep &= fin & lanemask_lt();
+  bool has_w = false;
+  if (valid) {
+    int32_t v[MAXR];
+#pragma unroll
+    for (int k = 0; k < MAXR; k++) v[k] = (k >= (int)nr) ? 0 : rsl[k] < 0 ? fv[k] : gx.base[rsl[k]];
+    int32_t w0 = 0, w1 = 0;
+    has_w = transfer_writes<MAXR>(op, nr, v, w0, w1);
+    gx.out0[lane] = w0;
+    gx.out1[lane] = w1;
+  }
+  const uint32_t depm = __ballot_sync(FULL, dep != 0u);
+  uint32_t hw = __ballot_sync(FULL, has_w);
+  if (depm) {
+    if (valid) {
+      uint32_t facc = CSMV_OP_AMT0(op) - 1u, ntr = 0u;
+      unsigned long long tr = ~0ull;
+#pragma unroll
+      for (int k = 2; k < MAXR; k++) {
+        if (k >= (int)nr) continue;
+        if (rsl[k] < 0) {
+          facc += (uint32_t)fv[k];
+        } else {
+          tr = (tr & ~(0xFFull << (8u * ntr))) | ((unsigned long long)rsl[k] << (8u * ntr));
+          ntr++;
+        }
+      }
+      const uint32_t d = CSMV_OP_AMOD(op);
+      gx.cs[lane] = (uint32_t)s0 | ((uint32_t)s1 << 8) | (ntr << 16) |
+                    ((CSMV_OP_KIND(op) == CSMV_KIND_TRANSFER_ALWAYS ? 1u : 0u) << 24);
+      gx.facc[lane] = facc;
+      gx.tr[lane] = tr;
+      gx.md[lane] = d;
+      gx.mm[lane] = 0xFFFFFFFFu / d;
+    }
+    __syncwarp();
+    uint32_t hwm = hw & ~depm;
+    if (lane == 0) {
+      for (uint32_t m = fin; m; m &= m - 1u) {
+        const uint32_t j = __ffs(m) - 1u;
+        const uint32_t cs = gx.cs[j], x0 = cs & 0xFFu, x1 = (cs >> 8) & 0xFFu;
+        if (!((depm >> j) & 1u)) {  // independent: its writes, for the lanes above
+          if ((hw >> j) & 1u) {
+            gx.base[x0] = gx.out0[j];
+            gx.base[x1] = gx.out1[j];
+          }
+          continue;
+        }
+        const uint32_t n = (cs >> 16) & 0xFFu;
+        const int32_t v0 = gx.base[x0], v1 = gx.base[x1];
+        uint32_t acc = gx.facc[j];
+        const unsigned long long tr = gx.tr[j];
+        for (uint32_t q = 0; q < n; q++) acc += (uint32_t)gx.base[(tr >> (8u * q)) & 0xFFu];
+        const uint32_t d = gx.md[j];
+        uint32_t r = acc - __umulhi(acc, gx.mm[j]) * d;  // acc mod d (one correction suffices)
+        if (r >= d) r -= d;
+        const uint32_t amt = 1u + r;
+        if ((cs >> 24) != 0u || v0 >= (int32_t)amt) {
+          const int32_t w0 = (int32_t)((uint32_t)v0 - amt), w1 = (int32_t)((uint32_t)v1 + amt);
+          gx.base[x0] = w0;
+          gx.base[x1] = w1;
+          gx.out0[j] = w0;
+          gx.out1[j] = w1;
+          hwm |= 1u << j;
+        } else {
+          hwm &= ~(1u << j);
+        }
       }
     }
-    const uint32_t d = CSMV_OP_AMOD(op);
-    gx.cs[lane] = (uint32_t)s0 | ((uint32_t)s1 << 8) | (ntr << 16) |
-                  ((CSMV_OP_KIND(op) == CSMV_KIND_TRANSFER_ALWAYS ? 1u : 0u) << 24);
-    gx.facc[lane] = facc;
-    gx.tr[lane] = tr;
-    gx.md[lane] = d;
-    gx.mm[lane] = 0xFFFFFFFFu / d;
+    hw = __shfl_sync(FULL, hwm, 0);
+    __syncwarp();
   }
-  __syncwarp();
-  uint32_t hwm = 0u;
-  if (lane == 0) {
-    for (uint32_t m = fin; m; m &= m - 1u) {
-      const uint32_t j = __ffs(m) - 1u;
-      const uint32_t cs = gx.cs[j], x0 = cs & 0xFFu, x1 = (cs >> 8) & 0xFFu, n = (cs >> 16) & 0xFFu;
-      const int32_t v0 = gx.base[x0], v1 = gx.base[x1];
-      uint32_t acc = gx.facc[j];
-      const unsigned long long tr = gx.tr[j];
-      for (uint32_t q = 0; q < n; q++) acc += (uint32_t)gx.base[(tr >> (8u * q)) & 0xFFu];
-      const uint32_t d = gx.md[j];
-      uint32_t r = acc - __umulhi(acc, gx.mm[j]) * d;  // acc mod d (one correction suffices)
-      if (r >= d) r -= d;
-      const uint32_t amt = 1u + r;
-      if ((cs >> 24) != 0u || v0 >= (int32_t)amt) {
-        const int32_t w0 = (int32_t)((uint32_t)v0 - amt), w1 = (int32_t)((uint32_t)v1 + amt);
-        gx.base[x0] = w0;
-        gx.base[x1] = w1;
-        gx.out0[j] = w0;
-        gx.out1[j] = w1;
-        hwm |= 1u << j;
-      }
-    }
-  }
-  const uint32_t hw = __shfl_sync(FULL, hwm, 0);
-  __syncwarp();
 
   // 7. one version per locked account (its last writer's), then the stamp (a release store: the
   //    version is visible first) and the unlock

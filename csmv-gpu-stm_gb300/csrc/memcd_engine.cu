@@ -8,6 +8,7 @@
 //   done  256 KB               completion bitmap, one bit per commit timestamp
 //   logs  8*max_req*4 + max_req*4 B   log_txn[ts-1] (holes included), outcome[req]
 //   io    max_req * (4 + 16 + 32 + 4 + 32) B   request / response staging for host-buffer runs
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <vector>
@@ -307,6 +308,105 @@ extern "C" csmv_status csmv_memcd_run(csmv_memcd_t* h, const csmv_memcd_batch* b
   if (out)
     out->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return st;
+}
+
+// The cache's autotuner: each candidate shape on a fresh cache, fill untimed, the sample timed
+// by its kernel time; successive halving as in the bank's tuner.
+extern "C" csmv_status csmv_memcd_autotune(const csmv_memcd_config* base,
+                                           const csmv_memcd_batch* host_fill,
+                                           const csmv_memcd_batch* host_sample, uint32_t repeats,
+                                           csmv_memcd_tune_result* out) {
+  if (!base || !host_sample || !out || repeats == 0) return CSMV_ERR_INVALID_ARG;
+  std::memset(out, 0, sizeof(*out));
+  int n_sms = 0;
+  csmv_status st = check_device(base->device, &n_sms);
+  if (st != CSMV_OK) return st;
+  struct Cand {
+    csmv_memcd_config cfg;
+    std::vector<double> ms;
+    double med = 1e30, abort_rate = 0;
+    csmv_status st = CSMV_OK;
+  };
+  std::vector<Cand> cands;
+  for (uint32_t cw : {1u, 2u, 4u, 8u})
+    for (uint32_t per_sm : {1u, 2u}) {
+      Cand c;
+      c.cfg = *base;
+      c.cfg.client_warps = cw;
+      c.cfg.ctas = per_sm * (uint32_t)n_sms;
+      c.cfg.log_commits = 0;
+      c.cfg.max_req = std::max(base->max_req, std::max(host_sample->n_req,
+                                                        host_fill ? host_fill->n_req : 0u));
+      cands.push_back(c);
+    }
+  const size_t n = host_sample->n_req;
+  std::vector<uint32_t> found(n);
+  std::vector<uint32_t> vout(n * 8);
+  auto run = [&](Cand& c, uint32_t times) {
+    csmv_memcd_t* h = nullptr;
+    csmv_status s = csmv_memcd_create(&c.cfg, &h);
+    if (s != CSMV_OK) return s;
+    if (host_fill) {
+      csmv_memcd_batch f = *host_fill;
+      std::vector<uint32_t> ff(f.n_req), fv((size_t)f.n_req * 8);
+      f.found = ff.data();
+      f.val_out = fv.data();
+      s = csmv_memcd_run(h, &f, nullptr);
+    }
+    for (uint32_t i = 0; i < times && s == CSMV_OK; i++) {
+      csmv_memcd_batch b = *host_sample;
+      b.found = found.data();
+      b.val_out = vout.data();
+      csmv_stats o;
+      if ((s = csmv_memcd_run(h, &b, &o)) != CSMV_OK) break;
+      c.ms.push_back(o.kernel_ms);
+      const double cm = (double)(o.commits_update + o.commits_readonly);
+      const double ab = (double)(o.aborts_data_age + o.aborts_read_write + o.aborts_prevalid +
+                                 o.aborts_write_write);
+      c.abort_rate = ab / std::max(1.0, ab + cm);
+    }
+    csmv_memcd_destroy(h);
+    return s;
+  };
+  for (auto& c : cands) {
+    c.st = run(c, 1);
+    if (c.st == CSMV_OK) c.med = c.ms.back();
+  }
+  std::vector<size_t> order(cands.size());
+  for (size_t i = 0; i < order.size(); i++) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return cands[a].med < cands[b].med; });
+  const size_t keep = std::max<size_t>(1, cands.size() / 4);
+  for (size_t r = 0; r < keep; r++) {
+    Cand& c = cands[order[r]];
+    if (c.st != CSMV_OK) continue;
+    c.st = run(c, repeats);
+    std::vector<double> m = c.ms;
+    std::sort(m.begin(), m.end());
+    c.med = m[m.size() / 2];
+  }
+  size_t best = order[0];
+  for (size_t r = 0; r < keep; r++)
+    if (cands[order[r]].st == CSMV_OK && cands[order[r]].med < cands[best].med) best = order[r];
+  if (cands[best].st != CSMV_OK) {
+    set_error("memcd autotune: no candidate ran (%s)", csmv_status_str(cands[best].st));
+    return cands[best].st;
+  }
+  out->best = cands[best].cfg;
+  out->best.log_commits = base->log_commits;
+  out->best.max_req = base->max_req;
+  out->n_trials = (uint32_t)cands.size();
+  for (uint32_t i = 0; i < out->n_trials; i++) {
+    const Cand& c = cands[i];
+    csmv_tune_trial& o = out->trials[i];
+    o.client_warps = c.cfg.client_warps;
+    o.ctas = c.cfg.ctas;
+    o.version_depth = kMemcdDepth;
+    o.runs = (uint32_t)c.ms.size();
+    o.status = (int32_t)c.st;
+    o.tx_per_s = c.st == CSMV_OK ? (double)n / (c.med * 1e-3) : 0.0;
+    o.abort_rate = c.abort_rate;
+  }
+  return CSMV_OK;
 }
 
 extern "C" csmv_status csmv_memcd_read_table(csmv_memcd_t* h, uint64_t* host_tags,

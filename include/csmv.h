@@ -608,10 +608,13 @@ void csmv_sched_destroy(csmv_sched_t* s);
 /* ------------------------------------------------------------------------------------------
  * Autotuner (no counterpart in the reference, whose launch shape is fixed on the command line):
  * measures the engine on a sample of the caller's stream over client warps per CTA (1, 2, 4,
- * 8: the block size and the number of mailboxes per commit-server warp), CTAs per SM (1, 2)
- * and versions per account (4, 8), with the rest of *base fixed; every candidate runs once from
- * host_init (NULL: base->init_value), the best quarter `repeats` more times, and the fastest
- * median wins. out->best is *base with the winning shape.
+ * 8: the block size and the number of mailboxes per commit-server warp), CTAs per SM (1, 2),
+ * versions per account (4, 8), and - for the stamp protocol - the commit method (prevalidate
+ * 1: per transaction with pre-validation; 3: group commit) and, when every transfer of the
+ * sample reads at most four accounts, the kernels specialised for it (max_reads 4, else 0);
+ * the rest of *base is fixed. Every candidate runs once from host_init (NULL:
+ * base->init_value), the best quarter `repeats` more times, and the fastest median wins.
+ * out->best is *base with the winning shape and method.
  * ------------------------------------------------------------------------------------------ */
 #define CSMV_TUNE_MAX_TRIALS 64
 typedef struct csmv_tune_trial {
@@ -619,6 +622,7 @@ typedef struct csmv_tune_trial {
   int32_t status;             /* csmv_status of the candidate (e.g. does not fit)           */
   double tx_per_s;            /* committed tx/s of the sample (median over runs)            */
   double abort_rate;
+  uint32_t prevalidate, max_reads;  /* the candidate's commit method and read specialisation */
 } csmv_tune_trial;
 typedef struct csmv_tune_result {
   csmv_bank_config best;
@@ -627,6 +631,20 @@ typedef struct csmv_tune_result {
 } csmv_tune_result;
 csmv_status csmv_bank_autotune(const csmv_bank_config* base, const csmv_bank_stream* host_sample,
                                const int32_t* host_init, uint32_t repeats, csmv_tune_result* out);
+
+/* The cache's autotuner: client warps per CTA (1, 2, 4, 8) x CTAs per SM (1, 2), the rest of
+ * *base fixed (max_req at least the sample's size, logging off). Each candidate is a fresh
+ * cache: host_fill (optional) runs first untimed, then host_sample once; the best quarter runs
+ * the sample `repeats` more times and the fastest median kernel time wins. Trials report
+ * requests/s in tx_per_s and version_depth 2. out->best is *base with the winning shape. */
+typedef struct csmv_memcd_tune_result {
+  csmv_memcd_config best;
+  uint32_t n_trials;
+  csmv_tune_trial trials[CSMV_TUNE_MAX_TRIALS];
+} csmv_memcd_tune_result;
+csmv_status csmv_memcd_autotune(const csmv_memcd_config* base, const csmv_memcd_batch* host_fill,
+                                const csmv_memcd_batch* host_sample, uint32_t repeats,
+                                csmv_memcd_tune_result* out);
 
 /* ------------------------------------------------------------------------------------------
  * L2 atomic rates of the device (no counterpart in the reference): the bounds of the commit
