@@ -346,7 +346,8 @@ extern "C" csmv_status csmv_memcd_autotune(const csmv_memcd_config* base,
     csmv_memcd_t* h = nullptr;
     csmv_status s = csmv_memcd_create(&c.cfg, &h);
     if (s != CSMV_OK) return s;
-    if (host_fill) {
+    s = csmv_memcd_clear(h);
+    if (s == CSMV_OK && host_fill) {
       csmv_memcd_batch f = *host_fill;
       std::vector<uint32_t> ff(f.n_req), fv((size_t)f.n_req * 8);
       f.found = ff.data();

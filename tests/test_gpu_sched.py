@@ -207,3 +207,44 @@ def test_grouped_plan_at_the_bench_shape_replays_exactly():
     assert err is None, err
     upd = (s.op & 3) != 0
     assert 0 < waits[upd].mean() < 1 and not waits[~upd].any()
+
+
+@pytest.mark.parametrize("arm", ["network", "sketch_score", "no_backoff"])
+def test_grouped_plan_ablation_on_shifting_hotspot(arm):
+    """Ablation of the learned arm on the shifting hotspot (1 M accounts, a 1 % hot set drawing
+    30 % of the accesses, moving every 2^20 transactions; four chunks of 2^18): the grouped plan
+    on group commit with the network's score, with the raw sketch-count score instead, or with
+    the network and no backoff. Each arm commits everything, conserves the balance, and keeps
+    its abort rate at least 30 % below the reference's commit method on the same chunks in
+    stream order (the rates of all arms are printed for the record)."""
+    torch = pytest.importorskip("torch")
+    n_acc, chunk, n_chunks = 1 << 20, 1 << 18, 4
+    s, bounds = _hotspot_chunks(n_acc, chunk, n_chunks, 0.3)
+    over = {"network": {}, "sketch_score": {"score": 1}, "no_backoff": {"backoff_ns": 0}}[arm]
+    res = {}
+    for name in ("plain", arm):
+        commits = aborts = 0
+        cfg = dict(prevalidate=1) if name == "plain" else dict(prevalidate=3)
+        with cg.Bank(n_accounts=n_acc, max_txn=chunk, ctas=152, client_warps=2, version_depth=8,
+                     log_commits=0, **cfg) as bank:
+            bank.load()
+            sched = None if name == "plain" else cg.Scheduler(
+                n_accounts=n_acc, max_txn=chunk, plan=1, probe_every=1, **over)
+            for lo, hi in bounds:
+                c = cg.Stream(np.ascontiguousarray(s.op[lo:hi]), np.ascontiguousarray(s.off[lo:hi]),
+                              s.addr)
+                ds, keep = to_device(torch, c)
+                if sched is None:
+                    st = bank.run_device(ds)
+                    commits, aborts = commits + st.commits, aborts + st.aborts
+                else:
+                    r = sched.run(bank, ds)
+                    commits, aborts = commits + r.commits, aborts + r.aborts
+            vals = bank.values()
+            if sched is not None:
+                sched.close()
+        assert commits == chunk * n_chunks
+        assert int(vals.astype(np.int64).sum()) == 1000 * n_acc
+        res[name] = aborts / (aborts + commits)
+    print("abort rates:", res)
+    assert res[arm] <= 0.7 * res["plain"], res
