@@ -59,7 +59,8 @@ class BankConfig(C.Structure):
         (n, C.c_uint32) for n in ("version_depth", "ring_size", "client_warps", "ctas",
                                   "cluster_size", "validate", "writeback", "batch",
                                   "prevalidate", "log_commits", "max_txn", "spin_limit_log2")
-    ] + [("device", C.c_int32), ("flow_warps", C.c_uint32), ("max_reads", C.c_uint32)]
+    ] + [("device", C.c_int32), ("flow_warps", C.c_uint32), ("max_reads", C.c_uint32),
+         ("group_grace", C.c_uint32)]
 
 
 class Stats(C.Structure):

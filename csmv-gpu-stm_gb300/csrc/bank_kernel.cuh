@@ -104,6 +104,7 @@ struct BankParams {
                             // lock another warp held (group commit)
   uint32_t* tk;             // group commit: per account {next ticket, ticket served} of its
                             // lock's wait queue
+  uint32_t grace;            // group commit: polls a head keeps trying its other locks
   const uint8_t* lock_last;  // group commit, optional [n_items]: heat class of each account
                              // (0 = none); classed accounts are locked after all others, the
                              // hottest last
@@ -599,6 +600,17 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
       if (turn == 1 && !h1) h1 = group_try_lock<DEPTH>(p, a[1], me, st1, stale1, ed1, bv1);
       if (__any_sync(FULL, (turn == 0 && h0) || (turn == 1 && h1))) {
         all = true;
+        // a short grace for the other locks still held elsewhere (bounded: no wait cycle can
+        // form, at worst their lanes sit out)
+        for (uint32_t g = 0; g < p.grace &&
+                             __any_sync(FULL, (lead0 && !h0 && turn != 0) || (lead1 && !h1 && turn != 1));
+             g++) {
+          __nanosleep(32);
+          if (lead0 && !h0 && turn != 0 && (ld_relaxed_gpu(&p.cw[a[0]]) >> 32) == 0ull)
+            h0 = group_cas_lock(p.cw, a[0], me, st0, stale0);
+          if (lead1 && !h1 && turn != 1 && (ld_relaxed_gpu(&p.cw[a[1]]) >> 32) == 0ull)
+            h1 = group_cas_lock(p.cw, a[1], me, st1, stale1);
+        }
         break;
       }
       if ((it & 63u) == 63u && __any_sync(FULL, lane == 0 && ld_relaxed_gpu(&p.gs->error) != 0u))
@@ -802,35 +814,60 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
     __syncwarp();
     uint32_t hwm = hw & ~depm;
     if (lane == 0) {
-      for (uint32_t m = fin; m; m &= m - 1u) {
-        const uint32_t j = __ffs(m) - 1u;
-        const uint32_t cs = gx.cs[j], x0 = cs & 0xFFu, x1 = (cs >> 8) & 0xFFu;
+      // software-pipelined: the next lane's staged inputs load while this one computes (only
+      // the table values carry a dependence from one lane to the next)
+      uint32_t m = fin & (0u - (depm & (0u - depm)));  // from the first dependent lane on...
+      const uint32_t below = fin & ~m & hw;              // ...after the writes of those below it
+      for (uint32_t b = below; b; b &= b - 1u) {
+        const uint32_t j = __ffs(b) - 1u, cs = gx.cs[j];
+        gx.base[cs & 0xFFu] = gx.out0[j];
+        gx.base[(cs >> 8) & 0xFFu] = gx.out1[j];
+      }
+      uint32_t j = m ? __ffs(m) - 1u : 0u;
+      uint32_t cs = gx.cs[j], facc = gx.facc[j], d = gx.md[j], mg = gx.mm[j];
+      unsigned long long tr = gx.tr[j];
+      int32_t o0 = gx.out0[j], o1 = gx.out1[j];
+      while (m) {
+        m &= m - 1u;
+        const uint32_t jn = m ? __ffs(m) - 1u : j;
+        const uint32_t csn = gx.cs[jn], faccn = gx.facc[jn], dn = gx.md[jn], mgn = gx.mm[jn];
+        const unsigned long long trn = gx.tr[jn];
+        const int32_t o0n = gx.out0[jn], o1n = gx.out1[jn];
+        const uint32_t x0 = cs & 0xFFu, x1 = (cs >> 8) & 0xFFu;
         if (!((depm >> j) & 1u)) {  // independent: its writes, for the lanes above
           if ((hw >> j) & 1u) {
-            gx.base[x0] = gx.out0[j];
-            gx.base[x1] = gx.out1[j];
+            gx.base[x0] = o0;
+            gx.base[x1] = o1;
           }
-          continue;
-        }
-        const uint32_t n = (cs >> 16) & 0xFFu;
-        const int32_t v0 = gx.base[x0], v1 = gx.base[x1];
-        uint32_t acc = gx.facc[j];
-        const unsigned long long tr = gx.tr[j];
-        for (uint32_t q = 0; q < n; q++) acc += (uint32_t)gx.base[(tr >> (8u * q)) & 0xFFu];
-        const uint32_t d = gx.md[j];
-        uint32_t r = acc - __umulhi(acc, gx.mm[j]) * d;  // acc mod d (one correction suffices)
-        if (r >= d) r -= d;
-        const uint32_t amt = 1u + r;
-        if ((cs >> 24) != 0u || v0 >= (int32_t)amt) {
-          const int32_t w0 = (int32_t)((uint32_t)v0 - amt), w1 = (int32_t)((uint32_t)v1 + amt);
-          gx.base[x0] = w0;
-          gx.base[x1] = w1;
-          gx.out0[j] = w0;
-          gx.out1[j] = w1;
-          hwm |= 1u << j;
         } else {
-          hwm &= ~(1u << j);
+          const uint32_t n = (cs >> 16) & 0xFFu;
+          const int32_t v0 = gx.base[x0], v1 = gx.base[x1];
+          uint32_t acc = facc;
+#pragma unroll
+          for (int q = 0; q < MAXR - 2; q++)
+            if ((uint32_t)q < n) acc += (uint32_t)gx.base[(tr >> (8u * q)) & 0xFFu];
+          uint32_t r = acc - __umulhi(acc, mg) * d;  // acc mod d (one correction suffices)
+          if (r >= d) r -= d;
+          const uint32_t amt = 1u + r;
+          if ((cs >> 24) != 0u || v0 >= (int32_t)amt) {
+            const int32_t w0 = (int32_t)((uint32_t)v0 - amt), w1 = (int32_t)((uint32_t)v1 + amt);
+            gx.base[x0] = w0;
+            gx.base[x1] = w1;
+            gx.out0[j] = w0;
+            gx.out1[j] = w1;
+            hwm |= 1u << j;
+          } else {
+            hwm &= ~(1u << j);
+          }
         }
+        j = jn;
+        cs = csn;
+        facc = faccn;
+        d = dn;
+        mg = mgn;
+        tr = trn;
+        o0 = o0n;
+        o1 = o1n;
       }
     }
     hw = __shfl_sync(FULL, hwm, 0);

@@ -176,13 +176,14 @@ typedef struct csmv_bank_config {
   uint32_t prevalidate;        /* 0 = none; 1 = intra-warp pre-validation (batchedAtrInsert,
                                   API.cu:94-191); 2 = intra-warp chaining (stamp protocol);
                                   3 = group commit (stamp protocol): a warp's round locks every
-                                  account it may write once, waiting in descending account
-                                  order, reads them under the locks, draws the round's
-                                  timestamps from its server, validates every read of an
-                                  account it does not lock, runs the transfers that pass as a
-                                  chain in lane order and installs ONE version per account
-                                  (the last writer's); the clock passes a group's timestamps
-                                  at once, so no snapshot sees its intermediate states        */
+                                  account it may write once, waiting in one total order (the
+                                  stream's heat classes last, first-come first-served queues),
+                                  reads them under the locks, draws the round's timestamps from
+                                  its server, validates every read of an account it does not
+                                  lock, runs the transfers that pass as a chain in lane order
+                                  and installs ONE version per account (the last writer's); the
+                                  clock passes a group's timestamps at once, so no snapshot
+                                  sees its intermediate states                                 */
   uint32_t log_commits;        /* 1 = keep the per-ts commit log and per-txn outcomes         */
   uint32_t max_txn;            /* largest stream a run may carry (sizes the logs)             */
   uint32_t spin_limit_log2;    /* bounded waits give up after 2^this polls (default 24)       */
@@ -192,6 +193,10 @@ typedef struct csmv_bank_config {
                                   4 = up to 4 (a leaner kernel; a transfer with more reads is
                                   malformed, CSMV_ERR_INVALID_ARG). Read-only transactions may
                                   read up to 32 accounts either way                            */
+  uint32_t group_grace;        /* group commit: polls (about 0.1 us each) a hot queue's head
+                                  keeps trying its other locks after taking its hottest one,
+                                  before the lanes whose locks are still held sit the attempt
+                                  out (default 16)                                             */
 } csmv_bank_config;
 
 void csmv_bank_config_default(csmv_bank_config* cfg);
