@@ -543,10 +543,16 @@ def serve_section(cg, local, loads=(0.1, 0.25, 0.5, 0.75, 1.0), per_load_s=1.5):
         if time.perf_counter() > t_end:
             raise TimeoutError(f"serving: {what} exceeded its time budget")
 
-    with cg.Server(n_sets=1 << 20, client_warps=4, arena_requests=1 << 19,
-                   max_inflight_sets=1 << 16, idle_timeout_ms=5000, device=local) as srv:
+    # one launch shape for both forms: the cache autotuner's pick on a 32 K-request sample
+    fill = cg.memcd_generate(cg.memcd_workload(1 << 22, 1 << 16, seed=5, get_pct=0))
+    best, trials = cg.memcd_autotune(cg.requests_slice(pool, 0, 1 << 15), fill, repeats=2,
+                                     n_sets=1 << 20, device=local)
+    shape = dict(client_warps=best.client_warps, ctas=best.ctas)
+    out["tuned"] = dict(shape, candidates=len(trials))
+    progress(f"serving: tuned shape {shape}")
+    with cg.Server(n_sets=1 << 20, arena_requests=1 << 19, max_inflight_sets=1 << 16,
+                   idle_timeout_ms=5000, device=local, **shape) as srv:
         srv.start()  # a session of fills; the measured session starts from the table it leaves
-        fill = cg.memcd_generate(cg.memcd_workload(1 << 22, 1 << 16, seed=5, get_pct=0))
         t_end = time.perf_counter() + 30
         for _ in range(8):
             b = None
@@ -620,12 +626,13 @@ def serve_section(cg, local, loads=(0.1, 0.25, 0.5, 0.75, 1.0), per_load_s=1.5):
         out["abort_rate"] = st.aborts / max(1, st.aborts + st.commits)  # the measured session
     # the plain form at equal offered load: the same arrivals, one batch call at a time
     # (csmv_memcd_run with host buffers); a batch that arrives while another runs waits
-    with cg.Memcd(n_sets=1 << 20, client_warps=4, max_req=1 << 16, log_commits=0,
-                  device=local) as cache:
+    with cg.Memcd(n_sets=1 << 20, max_req=1 << 16, log_commits=0, device=local,
+                  **shape) as cache:
         for _ in range(8):
             cache.run(fill)
+        p_commits = p_aborts = 0
         for row, (arrivals, reqs) in zip(rows, replay):
-            lat, served, t0 = [], 0, time.perf_counter()
+            lat, kms, served, t0 = [], [], 0, time.perf_counter()
             t_end = t0 + per_load_s * 4 + 10
             for arr, req in zip(arrivals, reqs):
                 if time.perf_counter() > t_end:
@@ -633,15 +640,21 @@ def serve_section(cg, local, loads=(0.1, 0.25, 0.5, 0.75, 1.0), per_load_s=1.5):
                     break
                 while time.perf_counter() - t0 < arr:
                     pass
-                cache.run(req)
+                _, _, pst = cache.run(req)
                 lat.append(time.perf_counter() - t0 - arr)
+                kms.append(pst.kernel_ms)
+                p_commits += pst.commits
+                p_aborts += pst.aborts
                 served += req.n_req
             lat = np.array(lat) * 1e3
             row["plain_p50_ms"] = float(np.percentile(lat, 50))
             row["plain_p99_ms"] = float(np.percentile(lat, 99))
+            row["plain_kernel_p50_ms"] = float(np.percentile(kms, 50))
+            row["plain_kernel_p99_ms"] = float(np.percentile(kms, 99))
             row["plain_achieved_req_s"] = served / (time.perf_counter() - t0)
             progress(f"serving: plain form at load {row['offered_frac']}: "
                      f"p99 {row['plain_p99_ms']:.3f} ms")
+        out["plain_abort_rate"] = p_aborts / max(1, p_aborts + p_commits)
     return out
 
 

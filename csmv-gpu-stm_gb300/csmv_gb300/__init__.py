@@ -135,7 +135,7 @@ class SchedConfig(C.Structure):
                 ("deferred_warps", C.c_uint32), ("serial_lane", C.c_uint32),
                 ("seed", C.c_uint64), ("device", C.c_int32), ("plan", C.c_uint32),
                 ("hot_count", C.c_uint32), ("score", C.c_uint32), ("backoff_ns", C.c_uint32),
-                ("hot_last", C.c_uint32)]
+                ("hot_last", C.c_uint32), ("key_written", C.c_uint32)]
 
 
 class SchedReport(C.Structure):

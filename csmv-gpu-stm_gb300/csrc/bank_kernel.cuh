@@ -441,6 +441,19 @@ __device__ __forceinline__ bool group_lock_at_turn(const BankParams& p, uint32_t
   return false;
 }
 
+// x's lock seen free as the word w (an acquire load): its slots are read and the lock taken by a
+// CAS at that stamp (false when another warp took it first).
+template <int DEPTH>
+__device__ __forceinline__ bool group_take_seen(const BankParams& p, uint32_t x, uint32_t me,
+                                                unsigned long long w, uint32_t& stamp, bool& stale,
+                                                SlotEditor<DEPTH>& ed, int32_t& v) {
+  ed.load(p.slots + (size_t)x * DEPTH);
+  if (atomicCAS(&p.cw[x], w, w | ((unsigned long long)me << 32)) != w) return false;
+  stamp = (uint32_t)w;
+  stale = !ed.find(stamp, v);
+  return true;
+}
+
 // One look at x's lock: when it is free, the slots are read and the lock taken by a CAS at the
 // stamp seen (as group_lock_at_turn does, without waiting).
 template <int DEPTH>
@@ -592,12 +605,22 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
     ok = !__any_sync(FULL, !r);
     const uint64_t limit = 1ull << min(p.spin_log2, 22u);
     for (uint64_t it = 0; ok && !patient && it < limit; it++) {
-      if (lead0 && !h0 && turn != 0 && (ld_relaxed_gpu(&p.cw[a[0]]) >> 32) == 0ull)
-        h0 = group_cas_lock(p.cw, a[0], me, st0, stale0);
-      if (lead1 && !h1 && turn != 1 && (ld_relaxed_gpu(&p.cw[a[1]]) >> 32) == 0ull)
-        h1 = group_cas_lock(p.cw, a[1], me, st1, stale1);
-      if (turn == 0 && !h0) h0 = group_try_lock<DEPTH>(p, a[0], me, st0, stale0, ed0, bv0);
-      if (turn == 1 && !h1) h1 = group_try_lock<DEPTH>(p, a[1], me, st1, stale1, ed1, bv1);
+      // one round of loads in flight together: the queued lock's word and the other missing
+      // ones; the queued lock is taken as soon as it is seen free, the others only when the
+      // queued one is still held
+      const bool o0 = lead0 && !h0 && turn != 0, o1 = lead1 && !h1 && turn != 1;
+      unsigned long long wq = ~0ull, w0 = ~0ull, w1 = ~0ull;
+      if (turn == 0) wq = ld_acquire_gpu(&p.cw[a[0]]);
+      if (turn == 1) wq = ld_acquire_gpu(&p.cw[a[1]]);
+      if (o0) w0 = ld_relaxed_gpu(&p.cw[a[0]]);
+      if (o1) w1 = ld_relaxed_gpu(&p.cw[a[1]]);
+      if (__any_sync(FULL, turn >= 0 && (wq >> 32) == 0ull)) {
+        if (turn == 0 && (wq >> 32) == 0ull) h0 = group_take_seen<DEPTH>(p, a[0], me, wq, st0, stale0, ed0, bv0);
+        if (turn == 1 && (wq >> 32) == 0ull) h1 = group_take_seen<DEPTH>(p, a[1], me, wq, st1, stale1, ed1, bv1);
+      } else {
+        if (o0 && (w0 >> 32) == 0ull) h0 = group_cas_lock(p.cw, a[0], me, st0, stale0);
+        if (o1 && (w1 >> 32) == 0ull) h1 = group_cas_lock(p.cw, a[1], me, st1, stale1);
+      }
       if (__any_sync(FULL, (turn == 0 && h0) || (turn == 1 && h1))) {
         all = true;
         // a short grace for the other locks still held elsewhere (bounded: no wait cycle can

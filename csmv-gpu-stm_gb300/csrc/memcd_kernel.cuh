@@ -483,7 +483,8 @@ __global__ void __launch_bounds__(512, 1) memcd_kernel(MemcdParams p) {
 // the queue tail; it runs no rounds. Every other client warp takes a ticket (the next round
 // index, one atomic add) and polls the queue tail in device memory until its round exists, then
 // runs it with the cache's commit protocol, so rounds of different batches overlap on the device
-// and idle warps put no traffic on the host link. After a round, the warp makes its results
+// and idle warps put no traffic on the host link (and little on the queue's line: a warp polls
+// less often the farther its ticket is from the tail). After a round, the warp makes its results
 // visible to the host and counts the round off its batch; the batch's last round stamps done_ns
 // and sets done (release). Once ctl->stop is set and every published batch is admitted, or when
 // the host has published nothing and every round is done for idle_ns (error ERR_WAIT_REQUEST),
@@ -605,9 +606,9 @@ __device__ void serve_client(const MemcdParams& p, const ServeParams& s, MemcdSh
       uint32_t state = 0u, first = 0u, slot = 0u;  // 1: a round, 2: leave
       if (lane == 0) {
         const uint32_t ticket = atomicAdd(&s.dev->q_head, 1u);
-        uint32_t nap = 64;
         for (;;) {
-          if (ticket < ld_acquire_gpu(&s.dev->q_tail)) {
+          const uint32_t tail = ld_acquire_gpu(&s.dev->q_tail);
+          if (ticket < tail) {
             const uint2 e = s.rq[ticket & s.q_mask];
             first = e.x;
             slot = e.y;
@@ -622,8 +623,9 @@ __device__ void serve_client(const MemcdParams& p, const ServeParams& s, MemcdSh
             state = 2u;
             break;
           }
-          __nanosleep(nap);
-          nap = min(nap * 2u, 2048u);
+          // the farther back a ticket is, the more rounds must be appended before it: poll
+          // less often, so idle warps do not crowd the queue's L2 line
+          __nanosleep(min(64u + 32u * (ticket - tail), 8192u));
         }
       }
       state = __shfl_sync(0xFFFFFFFFu, state, 0);

@@ -300,7 +300,7 @@ extern "C" csmv_status csmv_sched_plan_run(csmv_sched_t* s, csmv_bank_t* bank,
     sched_group_keys_kernel<<<grid_for(s, n1), 256, 0, s->stream>>>(
         d->op, d->off, d->addr, t0, n, s->p, s->cfg.threshold, s->cfg.score, s->sketch,
         s->max_count, hot, s->hidx, s->key, s->rank, s->key_count, s->n_flagged, s->bo,
-        s->cfg.backoff_ns);
+        s->cfg.backoff_ns, s->cfg.key_written);
     SCHED_LAUNCH_CHECK("group keys");
     if ((st = scan_multi(s, s->key_count, SK, s->key_start)) != CSMV_OK) return st;
     sched_cold_flags_kernel<<<grid_for(s, n1), 256, 0, s->stream>>>(n1, s->key, s->bucket);

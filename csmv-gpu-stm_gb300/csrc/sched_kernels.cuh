@@ -338,7 +338,8 @@ __global__ void sched_group_keys_kernel(const uint32_t* op, const uint32_t* off,
                                         const uint32_t* sketch, const uint32_t* max_count,
                                         uint32_t hot_count, const uint32_t* hidx, uint32_t* key,
                                         uint32_t* rank, uint32_t* key_count, uint32_t* n_flagged,
-                                        uint32_t* backoff, uint32_t backoff_ns) {
+                                        uint32_t* backoff, uint32_t backoff_ns,
+                                        uint32_t key_written) {
   uint32_t flagged = 0;
   for (uint32_t t = t0 + blockIdx.x * blockDim.x + threadIdx.x; t < t1; t += gridDim.x * blockDim.x) {
     const uint32_t i = t - t0, o = op[t];
@@ -350,9 +351,12 @@ __global__ void sched_group_keys_kernel(const uint32_t* op, const uint32_t* off,
     const uint32_t nr = CSMV_OP_NREADS(o), base = off[t];
     uint32_t c1 = 0, c2 = 0, x1 = kHotNone, x2 = kHotNone, cmax = 0;
     for (uint32_t k = 0; k < nr; k++) {
-      const uint32_t sl = sketch_slot(addr[base + k]), c = sketch[sl];
-      cmax = max(cmax, c);
-      if (c < hot_count) continue;
+      const uint32_t sl = sketch_slot(addr[base + k]), c0 = sketch[sl];
+      cmax = max(cmax, c0);
+      if (c0 < hot_count) continue;
+      // key_written: a written account (k < 2) ranks above every read-only one, so a round's
+      // transfers share the hot account they WRITE (the lock the group must take)
+      const uint32_t c = (key_written && k < 2) ? c0 + 0x40000000u : c0;
       const uint32_t h = min(hidx[sl], kHotNone);
       if (h == x1 || h == x2) continue;  // two accounts hashed to one slot
       if (c > c1 || (c == c1 && h < x1)) {
