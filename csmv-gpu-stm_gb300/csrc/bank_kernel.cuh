@@ -782,7 +782,20 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
         __nanosleep(32);
         wd = ld_relaxed_gpu(&p.cw[a[k]]);
       }
-      valid = settled && (uint32_t)wd == fst[k];
+      if (settled && (uint32_t)wd != fst[k]) {
+        // a version below our timestamp was committed since the read, and no holder ordered
+        // before us remains: that version is the latest as of our timestamp, so it is read
+        // again (the chain below has not used the value yet) instead of aborting
+        uint32_t s2 = 0u;
+        int32_t v2 = 0;
+        if (read_latest<DEPTH>(vs, p.cw, a[k], s2, v2) && s2 == (uint32_t)wd) {
+          fst[k] = s2;
+          fv[k] = v2;
+        } else {
+          settled = false;
+        }
+      }
+      valid = settled;
     }
   }
   const uint32_t fin = __ballot_sync(FULL, valid);

@@ -160,10 +160,11 @@ def _scheduled_chunk_checked(bank, sched, s, ds, n, n_acc, depth):
     return r1, r2
 
 
-@pytest.mark.parametrize("score", [0, 1])
-def test_grouped_plan_replays_exactly(score):
+@pytest.mark.parametrize("score,key_written", [(0, 0), (1, 0), (0, 1)])
+def test_grouped_plan_replays_exactly(score, key_written):
     """Grouped plan (plan 1) in front of group commit on a small contended bank, with the network
-    (score 0) or the raw sketch-count score (score 1) flagging transfers."""
+    (score 0) or the raw sketch-count score (score 1) flagging transfers, and rounds keyed by the
+    hottest accounts touched or (key_written) written."""
     torch = pytest.importorskip("torch")
     n_acc, n = 1 << 14, 1 << 15
     w = c1_workload(n_txn=n, n_accounts=n_acc, dist=cg.DIST_ZIPF, zipf_theta=0.99, seed=10,
@@ -172,7 +173,7 @@ def test_grouped_plan_replays_exactly(score):
     ds, keep = to_device(torch, s)
     with cg.Bank(n_accounts=n_acc, max_txn=n, ctas=16, client_warps=4, prevalidate=3) as bank, \
             cg.Scheduler(n_accounts=n_acc, max_txn=n, plan=1, score=score, threshold=0.05,
-                         train_steps=2) as sched:
+                         train_steps=2, key_written=key_written) as sched:
         bank.load()
         r1, r2 = _scheduled_chunk_checked(bank, sched, s, ds, n, n_acc, 4)
     assert r2.n_flagged > 0
