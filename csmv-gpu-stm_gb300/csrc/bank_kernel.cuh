@@ -782,13 +782,17 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
         __nanosleep(32);
         wd = ld_relaxed_gpu(&p.cw[a[k]]);
       }
-      if (settled && (uint32_t)wd != fst[k]) {
+      // the reads were issued while the timestamps were being drawn, so a version read may even
+      // be newer than ours (a group ordered after us that committed meanwhile): it must be below
+      if (settled && ((uint32_t)wd != fst[k] || fst[k] >= my_ts)) {
         // a version below our timestamp was committed since the read, and no holder ordered
         // before us remains: that version is the latest as of our timestamp, so it is read
-        // again (the chain below has not used the value yet) instead of aborting
+        // again (the chain below has not used the value yet) instead of aborting. A version at
+        // or above our timestamp (a group ordered after us that already committed) is not.
         uint32_t s2 = 0u;
         int32_t v2 = 0;
-        if (read_latest<DEPTH>(vs, p.cw, a[k], s2, v2) && s2 == (uint32_t)wd) {
+        if ((uint32_t)wd < my_ts && read_latest<DEPTH>(vs, p.cw, a[k], s2, v2) &&
+            s2 == (uint32_t)wd) {
           fst[k] = s2;
           fv[k] = v2;
         } else {
