@@ -75,6 +75,7 @@ extern "C" void csmv_sched_config_default(csmv_sched_config* c) {
   c->score = 0;
   c->backoff_ns = 2048;
   c->hot_last = 1;
+  c->key_written = 1;
 }
 
 static void free_all(csmv_sched_t* s) {

@@ -575,9 +575,9 @@ typedef struct csmv_sched_config {
                                  hot accounts to the engine as heat classes (the stream's
                                  lock_last, 1 + 4 log2(count / hot_count) capped at 255), so
                                  they are locked last and queued for; 0 = plain account order */
-  uint32_t key_written;       /* plan 1: 1 = a transfer's group key ranks the hot accounts it
-                                 writes above those it only reads (rounds share the locks they
-                                 take); 0 = the hottest accounts touched, read or written      */
+  uint32_t key_written;       /* plan 1: 1 (default) = a transfer's group key ranks the hot
+                                 accounts it writes above those it only reads (rounds share the
+                                 locks they take); 0 = the hottest accounts touched           */
 } csmv_sched_config;
 
 typedef struct csmv_sched_report {
