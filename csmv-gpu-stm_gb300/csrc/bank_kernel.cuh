@@ -867,12 +867,6 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
       uint32_t cs = gx.cs[j], facc = gx.facc[j], d = gx.md[j], mg = gx.mm[j];
       unsigned long long tr = gx.tr[j];
       int32_t o0 = gx.out0[j], o1 = gx.out1[j];
-      // the last lane's two written slots and values stay in registers: consecutive lanes of
-      // a group mostly share its hot account, whose value then never round-trips through
-      // shared memory between them
-      uint32_t ka = 0xFFFFFFFFu, kb = 0xFFFFFFFFu;
-      int32_t va = 0, vb = 0;
-      auto val = [&](uint32_t x) -> int32_t { return x == kb ? vb : x == ka ? va : gx.base[x]; };
       while (m) {
         m &= m - 1u;
         const uint32_t jn = m ? __ffs(m) - 1u : j;
@@ -884,18 +878,14 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
           if ((hw >> j) & 1u) {
             gx.base[x0] = o0;
             gx.base[x1] = o1;
-            ka = x0;
-            va = o0;
-            kb = x1;
-            vb = o1;
           }
         } else {
           const uint32_t n = (cs >> 16) & 0xFFu;
-          const int32_t v0 = val(x0), v1 = val(x1);
+          const int32_t v0 = gx.base[x0], v1 = gx.base[x1];
           uint32_t acc = facc;
 #pragma unroll
           for (int q = 0; q < MAXR - 2; q++)
-            if ((uint32_t)q < n) acc += (uint32_t)val((uint32_t)(tr >> (8u * q)) & 0xFFu);
+            if ((uint32_t)q < n) acc += (uint32_t)gx.base[(tr >> (8u * q)) & 0xFFu];
           uint32_t r = acc - __umulhi(acc, mg) * d;  // acc mod d (one correction suffices)
           if (r >= d) r -= d;
           const uint32_t amt = 1u + r;
@@ -905,10 +895,6 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
             gx.base[x1] = w1;
             gx.out0[j] = w0;
             gx.out1[j] = w1;
-            ka = x0;
-            va = w0;
-            kb = x1;
-            vb = w1;
             hwm |= 1u << j;
           } else {
             hwm &= ~(1u << j);

@@ -157,9 +157,12 @@ __device__ bool memcd_round(const MemcdParams& p, MemcdShared& sm, MemcdMail& ms
           for (int wy = 0; wy < kWays; wy++) w1[wy] = ld_relaxed_gpu(&p.cw[e0 + wy]);
 #pragma unroll
           for (int wy = 0; wy < kWays; wy++) {
+            // a holder still without a timestamp is waited for (bounded); so, briefly, is one
+            // with a timestamp (a SET about to install: waiting for it costs less than the
+            // retry its timestamp below the snapshot would force)
             for (uint32_t it = 0; it < 512u; it++) {
               const uint32_t own = (uint32_t)(w1[wy] >> 32);
-              if (own == 0u || (own & kPendingFlag)) break;
+              if (own == 0u || ((own & kPendingFlag) && it >= 32u)) break;
               __nanosleep(64);
               w1[wy] = ld_relaxed_gpu(&p.cw[e0 + wy]);
             }
