@@ -51,7 +51,8 @@ class BankStream(C.Structure):
     _fields_ = [("n_txn", C.c_uint32), ("op", C.c_void_p), ("off", C.c_void_p),
                 ("addr", C.c_void_p), ("n_addr", C.c_uint64), ("txn_aborts", C.c_void_p),
                 ("split_round", C.c_uint32), ("deferred_warps", C.c_uint32),
-                ("backoff", C.c_void_p), ("txn_waits", C.c_void_p), ("lock_last", C.c_void_p)]
+                ("backoff", C.c_void_p), ("txn_waits", C.c_void_p), ("lock_last", C.c_void_p),
+                ("lane_start", C.c_void_p)]
 
 
 class BankConfig(C.Structure):
@@ -135,7 +136,7 @@ class SchedConfig(C.Structure):
                 ("deferred_warps", C.c_uint32), ("serial_lane", C.c_uint32),
                 ("seed", C.c_uint64), ("device", C.c_int32), ("plan", C.c_uint32),
                 ("hot_count", C.c_uint32), ("score", C.c_uint32), ("backoff_ns", C.c_uint32),
-                ("hot_last", C.c_uint32), ("key_written", C.c_uint32)]
+                ("hot_last", C.c_uint32), ("key_written", C.c_uint32), ("hot_lanes", C.c_uint32)]
 
 
 class SchedReport(C.Structure):
@@ -421,12 +422,14 @@ class Bank:
 
     def run(self, stream: Stream, txn_aborts: np.ndarray | None = None, split_round: int = 0,
             deferred_warps: int = 0, backoff: np.ndarray | None = None,
-            txn_waits: np.ndarray | None = None, lock_last: np.ndarray | None = None) -> Stats:
+            txn_waits: np.ndarray | None = None, lock_last: np.ndarray | None = None,
+            lane_start: np.ndarray | None = None) -> Stats:
         """Host buffers in: copies the stream to the device inside the call. txn_aborts (uint32
         [n_txn]) receives each transaction's failed attempts; split_round/deferred_warps set
         up the deferred queue; backoff (uint32 [n_txn], ns) bounds each transaction's pause
-        before a retry; lock_last (uint8 [n_accounts]) gives group commit's heat classes
-        (csmv_bank_stream)."""
+        before a retry; lock_last (uint8 [n_accounts]) gives group commit's heat classes;
+        lane_start (uint32 [deferred_warps + 1]) cuts the deferred queue into one lane of rounds
+        per deferred warp (csmv_bank_stream)."""
         st = Stats()
         s = stream.c_struct()
         if txn_aborts is not None:
@@ -441,6 +444,10 @@ class Bank:
         if lock_last is not None:
             assert lock_last.dtype == np.uint8 and lock_last.shape[0] == self.cfg.n_accounts
             s.lock_last = _ptr(lock_last)
+        if lane_start is not None:
+            lane_start = np.ascontiguousarray(lane_start, np.uint32)
+            assert lane_start.shape[0] == deferred_warps + 1
+            s.lane_start = _ptr(lane_start)
         s.split_round, s.deferred_warps = split_round, deferred_warps
         rc = lib().csmv_bank_run(self._h, C.byref(s), C.byref(st))
         self.last_stats = st

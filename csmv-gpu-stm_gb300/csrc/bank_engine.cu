@@ -134,6 +134,7 @@ static void free_all(csmv_bank_t* h) {
   cudaFree(h->d_backoff);
   cudaFree(h->d_waits);
   cudaFree(h->d_lock_last);
+  cudaFree(h->d_lanes);
   cudaFree(h->grp);
   cudaFree(h->tk);
   flow_scratch_free(h->flow);
@@ -291,6 +292,10 @@ csmv_status csmv::check_stream(const csmv_bank_t* h, const csmv_bank_stream* s) 
     set_error("stream: split_round must be <= n_txn/32, with deferred_warps > 0");
     return CSMV_ERR_INVALID_ARG;
   }
+  if (s->lane_start && !s->split_round) {
+    set_error("stream: lane_start cuts the deferred queue; it needs split_round");
+    return CSMV_ERR_INVALID_ARG;
+  }
   if (s->lock_last && !(h->cfg.prevalidate == 3 && h->cfg.validate == CSMV_VALIDATE_STAMP)) {
     set_error("stream: lock_last orders the locks of group commit (prevalidate 3, stamp protocol)");
     return CSMV_ERR_INVALID_ARG;
@@ -396,11 +401,12 @@ static csmv_status launch(csmv_bank_t* h, const uint32_t* op, const uint32_t* of
                           const uint32_t* addr, uint32_t n_txn, uint32_t* txn_aborts,
                           uint32_t split_round, uint32_t deferred_warps, const uint32_t* backoff,
                           uint32_t* txn_waits, const uint8_t* lock_last, csmv_stats* out,
-                          bool serial = false) {
+                          bool serial = false, const uint32_t* lane_start = nullptr) {
   const csmv_bank_config& c = h->cfg;
   BankParams p = bank_params(h, op, off, addr, n_txn, txn_aborts);
   p.split_round = split_round;
   p.deferred_warps = deferred_warps;
+  p.lane_start = split_round ? lane_start : nullptr;
   p.backoff = backoff;
   p.lock_last = serial ? nullptr : lock_last;
   p.txn_waits = txn_waits;
@@ -450,7 +456,7 @@ extern "C" csmv_status csmv_bank_run_device(csmv_bank_t* h, const csmv_bank_stre
   CSMV_CUDA(cudaSetDevice(h->cfg.device));
   auto t0 = std::chrono::steady_clock::now();
   st = launch(h, s->op, s->off, s->addr, s->n_txn, s->txn_aborts, s->split_round,
-              s->deferred_warps, s->backoff, s->txn_waits, s->lock_last, out);
+              s->deferred_warps, s->backoff, s->txn_waits, s->lock_last, out, false, s->lane_start);
   if (out)
     out->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return st;
@@ -501,6 +507,21 @@ extern "C" csmv_status csmv_bank_run(csmv_bank_t* h, const csmv_bank_stream* s, 
   if (s->backoff)
     CSMV_CUDA(cudaMemcpyAsync(h->d_backoff, s->backoff, (size_t)s->n_txn * 4,
                               cudaMemcpyHostToDevice, h->stream));
+  if (s->lane_start) {  // host lanes: checked here, then copied
+    const uint32_t nr = s->n_txn / 32;
+    bool ok = s->deferred_warps <= 4096u && s->lane_start[0] >= s->split_round;
+    for (uint32_t i = 0; ok && i < s->deferred_warps; i++)
+      ok = s->lane_start[i] <= s->lane_start[i + 1] && s->lane_start[i + 1] <= nr;
+    if (!ok) {
+      set_error("stream: lane_start must rise from split_round to at most n_txn/32");
+      return CSMV_ERR_INVALID_ARG;
+    }
+    cudaFree(h->d_lanes);
+    h->d_lanes = nullptr;
+    CSMV_CUDA(cudaMalloc(&h->d_lanes, (size_t)(s->deferred_warps + 1) * 4));
+    CSMV_CUDA(cudaMemcpyAsync(h->d_lanes, s->lane_start, (size_t)(s->deferred_warps + 1) * 4,
+                              cudaMemcpyHostToDevice, h->stream));
+  }
   if (s->lock_last) {
     if (!h->d_lock_last) CSMV_CUDA(cudaMalloc(&h->d_lock_last, h->cfg.n_accounts));
     CSMV_CUDA(cudaMemcpyAsync(h->d_lock_last, s->lock_last, h->cfg.n_accounts,
@@ -508,7 +529,8 @@ extern "C" csmv_status csmv_bank_run(csmv_bank_t* h, const csmv_bank_stream* s, 
   }
   st = launch(h, h->d_op, h->d_off, h->d_addr, s->n_txn, s->txn_aborts ? h->d_aborts : nullptr,
               s->split_round, s->deferred_warps, s->backoff ? h->d_backoff : nullptr,
-              s->txn_waits ? h->d_waits : nullptr, s->lock_last ? h->d_lock_last : nullptr, out);
+              s->txn_waits ? h->d_waits : nullptr, s->lock_last ? h->d_lock_last : nullptr, out,
+              false, s->lane_start ? h->d_lanes : nullptr);
   if (st == CSMV_OK && (s->txn_aborts || s->txn_waits)) {
     if (s->txn_aborts)
       CSMV_CUDA(cudaMemcpyAsync(s->txn_aborts, h->d_aborts, (size_t)s->n_txn * 4,

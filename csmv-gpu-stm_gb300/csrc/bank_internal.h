@@ -47,6 +47,7 @@ struct csmv_bank_t {
   uint32_t* d_backoff = nullptr;  // host-buffer runs: the stream's backoff array, copied in
   uint32_t* d_waits = nullptr;    // host-buffer runs: per-transaction lock waits, copied out
   uint8_t* d_lock_last = nullptr; // host-buffer runs: the stream's heat classes, copied in
+  uint32_t* d_lanes = nullptr;    // host-buffer runs: the stream's lanes of the deferred queue
   uint32_t* grp = nullptr;        // group-end bitmap of the last run (log_commits)
   uint32_t* tk = nullptr;         // group commit: per account {next ticket, ticket served}
   uint32_t grp_words = 0;

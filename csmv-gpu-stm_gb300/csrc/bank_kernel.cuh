@@ -99,6 +99,8 @@ struct BankParams {
   uint32_t* txn_aborts;     // optional [n_rounds*32]: failed attempts of each transaction
   uint32_t split_round;     // rounds [split_round, n_rounds) form the deferred queue (0 = none)
   uint32_t deferred_warps;  // client warps (lowest global ids) that serve the deferred queue
+  const uint32_t* lane_start;  // optional [deferred_warps + 1]: the deferred queue as one lane of
+                               // rounds per deferred warp, each served in order by its warp
   uint32_t* grp;            // group commit with log: bit (ts-1-log_base) = ts ends a commit group
   uint32_t* txn_waits;      // optional [n_rounds*32]: 1 when the transaction's group waited for a
                             // lock another warp held (group commit)
@@ -977,12 +979,25 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
   // Deferred queue (a scheduler's likely-conflicting rounds): only the first deferred_warps
   // warps of the grid take those rounds, so at most that many run at once; they join the main
   // queue when the deferred one is empty.
+  // With lane_start, the deferred queue is one lane of rounds per deferred warp instead, served
+  // in order by that warp alone.
   const uint32_t main_end = p.split_round ? p.split_round : p.n_rounds;
-  bool serve_deferred = p.split_round != 0 && blockIdx.x * p.nc + w < p.deferred_warps;
+  const uint32_t gw = blockIdx.x * p.nc + w;
+  bool serve_deferred = p.split_round != 0 && gw < p.deferred_warps;
+  uint32_t lane_next = 0u, lane_end = 0u;
+  if (serve_deferred && p.lane_start) {
+    lane_next = max(p.lane_start[gw], p.split_round);  // never a round of the main queue
+    lane_end = min(p.lane_start[gw + 1], p.n_rounds);
+  }
   for (;;) {
     uint32_t g = 0xFFFFFFFFu;
     if (lane == 0) {
-      if (serve_deferred) {
+      if (serve_deferred && p.lane_start) {
+        if (lane_next < lane_end)
+          g = lane_next++;
+        else
+          serve_deferred = false;
+      } else if (serve_deferred) {
         g = p.split_round + atomicAdd(&p.gs->round_deferred, 1u);
         if (g >= p.n_rounds) {
           g = 0xFFFFFFFFu;

@@ -151,6 +151,7 @@ csmv_status run_noalloc(int32_t device, void* cuda_stream, uint32_t n_accounts,
     return bad("the deferred queue (split_round, deferred_warps) is not available here");
   if (dev_stream->txn_waits) return bad("txn_waits is not produced here (no group commit)");
   if (dev_stream->lock_last) return bad("lock_last orders group commit's locks (no group commit here)");
+  if (dev_stream->lane_start) return bad("the deferred queue (lane_start) is not available here");
   if (n_accounts < 2) return bad("n_accounts < 2");
   if (n_accounts > CSMV_NOALLOC_MAX_ACCOUNTS) {
     set_error("csmv_bank_run_noalloc: %u accounts exceed the fixed scratch limit of %u", n_accounts,

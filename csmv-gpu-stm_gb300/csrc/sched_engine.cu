@@ -48,6 +48,7 @@ struct csmv_sched_t {
   uint32_t *rank = nullptr, *cold_pos = nullptr, *sorted = nullptr, *rbucket = nullptr;
   uint32_t *round_order = nullptr, *bo = nullptr, *bo2 = nullptr, *max_count = nullptr;
   uint8_t* lock_last = nullptr;  // heat classes of the bank's accounts (hot_last)
+  uint32_t *lane_of = nullptr, *lane_count = nullptr, *lanes = nullptr;  // hot lanes (plan 1)
   uint32_t lock_last_n = 0;
   uint64_t chunks = 0;
   // the current chunk
@@ -76,6 +77,7 @@ extern "C" void csmv_sched_config_default(csmv_sched_config* c) {
   c->backoff_ns = 2048;
   c->hot_last = 1;
   c->key_written = 1;
+  c->hot_lanes = 16;
 }
 
 static void free_all(csmv_sched_t* s) {
@@ -84,7 +86,8 @@ static void free_all(csmv_sched_t* s) {
                   s->bucket_fill, s->order, s->perm, s->op2, s->off2, s->ro_flag, s->ro_scan,
                   s->ro_list, s->n_flagged, s->waits, s->hidx, s->key_start, s->tile_sum,
                   s->tile_off, s->rank, s->cold_pos, s->sorted, s->rbucket, s->round_order,
-                  s->bo, s->bo2, s->max_count, s->lock_last};
+                  s->bo, s->bo2, s->max_count, s->lock_last, s->lane_of, s->lane_count,
+                  s->lanes};
   for (void* b : bufs) cudaFree(b);
   for (auto& e : s->ev)
     if (e) cudaEventDestroy(e);
@@ -124,8 +127,10 @@ extern "C" csmv_status csmv_sched_create(const csmv_sched_config* cfg, csmv_sche
       {(void**)&s->y, n * 4},            {(void**)&s->p, n * 4},
       {(void**)&s->rates, kRateBins * 4}, {(void**)&s->aborts, n * 4},
       {(void**)&s->bin_stats, kRateBins * 16}, {(void**)&s->key, n * 4},
-      {(void**)&s->bucket, n * 4},       {(void**)&s->bucket_count, R * 4},
-      {(void**)&s->bucket_start, R * 4}, {(void**)&s->bucket_fill, R * 4},
+      {(void**)&s->bucket, n * 4},       {(void**)&s->bucket_count, (R + kMaxLanes) * 4},
+      {(void**)&s->bucket_start, (R + kMaxLanes) * 4}, {(void**)&s->bucket_fill, (R + kMaxLanes) * 4},
+      {(void**)&s->lane_of, (size_t)kHotNone * 4}, {(void**)&s->lane_count, 4},
+      {(void**)&s->lanes, (kMaxLanes + 1) * 4},
       {(void**)&s->order, n * 4},        {(void**)&s->perm, n * 4},
       {(void**)&s->op2, n * 4},          {(void**)&s->off2, n * 4},
       {(void**)&s->ro_flag, R * 4},      {(void**)&s->ro_scan, R * 4},
@@ -217,6 +222,7 @@ extern "C" csmv_status csmv_sched_probe(csmv_sched_t* s, csmv_bank_t* bank,
   ps.txn_waits = s->waits;
   ps.backoff = nullptr;
   ps.lock_last = nullptr;
+  ps.lane_start = nullptr;
   ps.split_round = 0;
   ps.deferred_warps = 0;
   csmv_stats bst;
@@ -281,6 +287,7 @@ extern "C" csmv_status csmv_sched_plan_run(csmv_sched_t* s, csmv_bank_t* bank,
   const uint32_t* run_op = d->op + t0;
   const uint32_t* run_off = d->off + t0;
   bool with_backoff = false, with_classes = false;
+  uint32_t lanes_split = 0, lanes_n = 0;  // plan 1 with lanes: the laned rounds' split
   if (U > 0 && s->cfg.plan == 1) {
     // grouped plan: hot accounts, keys by the two hottest accounts touched, counting sort,
     // rounds of 32 consecutive sorted transfers spread by hot account
@@ -310,27 +317,53 @@ extern "C" csmv_status csmv_sched_plan_run(csmv_sched_t* s, csmv_bank_t* bank,
     sched_group_scatter_kernel<<<grid_for(s, n1), 256, 0, s->stream>>>(
         t0, n, s->key, s->rank, s->key_start, s->cold_pos, s->sorted);
     SCHED_LAUNCH_CHECK("group scatter");
-    CSMV_CUDA(cudaMemsetAsync(s->bucket_count, 0, (size_t)(U + 1) * 4, s->stream));
-    CSMV_CUDA(cudaMemsetAsync(s->bucket_fill, 0, (size_t)(U + 1) * 4, s->stream));
+    // lanes: the rounds of the hottest written accounts go to one warp each (hot_lanes)
+    uint32_t bank_n = 0;
+    const bool group = bank_group_commit(bank, &bank_n);
+    const uint32_t K = group ? std::min(s->cfg.hot_lanes, kMaxLanes) : 0u;
+    const uint32_t B = U + K;  // round buckets: U plan positions, then one per lane
+    CSMV_CUDA(cudaMemsetAsync(s->bucket_count, 0, (size_t)(B + 1) * 4, s->stream));
+    CSMV_CUDA(cudaMemsetAsync(s->bucket_fill, 0, (size_t)(B + 1) * 4, s->stream));
+    if (K) {
+      CSMV_CUDA(cudaMemsetAsync(s->lane_count, 0, 4, s->stream));
+      sched_hot_lanes_kernel<<<grid_for(s, kHotNone), 256, 0, s->stream>>>(
+          s->key_start, std::max(1u, U >> 6), K, s->lane_count, s->lane_of);
+      SCHED_LAUNCH_CHECK("hot lanes");
+    }
     sched_round_bucket_kernel<<<grid_for(s, U), 256, 0, s->stream>>>(
-        t0, U, s->sorted, s->key, s->key_start, seed, s->rbucket, s->bucket_count);
+        t0, U, s->sorted, s->key, s->key_start, seed, K ? s->lane_of : nullptr, s->rbucket,
+        s->bucket_count);
     SCHED_LAUNCH_CHECK("round buckets");
-    if ((st = scan_multi(s, s->bucket_count, U, s->bucket_start)) != CSMV_OK) return st;
+    if ((st = scan_multi(s, s->bucket_count, B, s->bucket_start)) != CSMV_OK) return st;
     sched_round_scatter_kernel<<<grid_for(s, U), 256, 0, s->stream>>>(
         U, s->rbucket, s->bucket_start, s->bucket_fill, s->round_order);
     SCHED_LAUNCH_CHECK("round scatter");
     sched_expand_rounds_kernel<<<grid_for(s, U * 32u), 256, 0, s->stream>>>(
         U, s->round_order, s->sorted, s->order);
     SCHED_LAUNCH_CHECK("expand");
+    uint32_t laned = 0;  // rounds on lanes (the last ones of the plan)
+    if (K) {
+      uint32_t ends[2] = {0, 0};
+      CSMV_CUDA(cudaMemcpyAsync(&ends[0], s->bucket_start + U, 4, cudaMemcpyDeviceToHost, s->stream));
+      CSMV_CUDA(cudaMemcpyAsync(&ends[1], s->bucket_start + B, 4, cudaMemcpyDeviceToHost, s->stream));
+      CSMV_CUDA(cudaStreamSynchronize(s->stream));
+      laned = ends[1] - ends[0];
+    }
+    const uint32_t r_main = Rp - laned;
     sched_ro_list_kernel<<<grid_for(s, Rp), 256, 0, s->stream>>>(P, Rp, s->ro_flag, s->ro_scan,
                                                                 s->ro_list);
     SCHED_LAUNCH_CHECK("ro_list");
-    sched_emit_kernel<<<grid_for(s, n1), 256, 0, s->stream>>>(d->op, d->off, Rp, r_ro, Rp,
+    sched_emit_kernel<<<grid_for(s, n1), 256, 0, s->stream>>>(d->op, d->off, Rp, r_ro, r_main,
                                                              s->ro_list, s->order, s->perm,
                                                              s->op2, s->off2);
     SCHED_LAUNCH_CHECK("emit");
-    uint32_t bank_n = 0;
-    if (s->cfg.hot_last && bank_group_commit(bank, &bank_n)) {
+    if (laned) {
+      sched_lane_start_kernel<<<1, 128, 0, s->stream>>>(U, K, r_main, s->bucket_start, s->lanes);
+      SCHED_LAUNCH_CHECK("lane starts");
+      lanes_split = r_main;
+      lanes_n = K;
+    }
+    if (s->cfg.hot_last && group) {
       if (s->lock_last_n < bank_n) {
         cudaFree(s->lock_last);
         s->lock_last = nullptr;
@@ -406,6 +439,12 @@ extern "C" csmv_status csmv_sched_plan_run(csmv_sched_t* s, csmv_bank_t* bank,
   rs.lock_last = with_classes ? s->lock_last : nullptr;
   rs.split_round = s->split_round;
   rs.deferred_warps = s->split_round ? s->cfg.deferred_warps : 0;
+  rs.lane_start = nullptr;
+  if (lanes_n) {
+    rs.split_round = lanes_split;
+    rs.deferred_warps = lanes_n;
+    rs.lane_start = s->lanes;
+  }
   if (s->cfg.serial_lane && s->split_round) {  // the deferred rounds wait for the serial lane
     s->serial_rounds = Rp - s->split_round;
     rs.n_txn = s->split_round * 32;
@@ -445,6 +484,7 @@ extern "C" csmv_status csmv_sched_serial_run(csmv_sched_t* s, csmv_bank_t* bank,
   rs.txn_waits = nullptr;
   rs.backoff = nullptr;
   rs.lock_last = nullptr;
+  rs.lane_start = nullptr;
   rs.split_round = rs.deferred_warps = 0;
   csmv_stats bst;
   csmv_status st = s->cfg.serial_lane == 2 ? csmv_bank_run_flow_device(bank, &rs, &bst)

@@ -305,6 +305,7 @@ __global__ void sched_scan_add_kernel(uint32_t* out, uint32_t n, const uint32_t*
 constexpr uint32_t kGroupKeys = 1u << 22;
 constexpr uint32_t kColdKey = kGroupKeys - 1u;
 constexpr uint32_t kHotNone = 0xFFFFu;
+constexpr uint32_t kMaxLanes = 64;  // hot lanes of a grouped plan at most
 
 __global__ void sched_hot_flags_kernel(const uint32_t* sketch, uint32_t hot_count, uint32_t* flag) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= kSketchMask; i += gridDim.x * blockDim.x)
@@ -409,12 +410,35 @@ __global__ void sched_cold_flags_kernel(uint32_t n, const uint32_t* key, uint32_
 // Position bucket of every transfer round of the sorted list: the j-th of the n rounds that start
 // within one hot account's keys goes to (j + u) / n of the plan (u a hash of the account in
 // [0, 1)), a cold round to a hash of its index.
+// Lanes of the hottest accounts (hot_lanes): every hot index whose transfers fill at least
+// min_rounds rounds gets a lane of its own, first come first served, while lanes last (lane_of:
+// lane, or kHotNone).
+__global__ void sched_hot_lanes_kernel(const uint32_t* key_start, uint32_t min_rounds,
+                                       uint32_t n_lanes, uint32_t* lane_count, uint32_t* lane_of) {
+  for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < kHotNone; h += gridDim.x * blockDim.x) {
+    const uint32_t n = key_start[(h + 1u) << 6] - key_start[h << 6];
+    uint32_t q = kHotNone;
+    if (n_lanes && n >= 32u * min_rounds) {
+      q = atomicAdd(lane_count, 1u);
+      if (q >= n_lanes) q = kHotNone;
+    }
+    lane_of[h] = q;
+  }
+}
+
 __global__ void sched_round_bucket_kernel(uint32_t t0, uint32_t U, const uint32_t* sorted,
                                           const uint32_t* key, const uint32_t* key_start,
-                                          uint64_t seed, uint32_t* rbucket, uint32_t* bcount) {
+                                          uint64_t seed, const uint32_t* lane_of,
+                                          uint32_t* rbucket, uint32_t* bcount) {
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < U; j += gridDim.x * blockDim.x) {
     const uint32_t k = key[sorted[32u * j] - t0], h1 = k >> 6;
     float pos;
+    if (k != kColdKey && h1 < kHotNone && lane_of && lane_of[h1] != kHotNone) {
+      // a round of a laned account: bucket U + lane, after every position of the main plan
+      rbucket[j] = U + lane_of[h1];
+      atomicAdd(&bcount[U + lane_of[h1]], 1u);
+      continue;
+    }
     if (k == kColdKey || h1 >= kHotNone) {
       pos = unit_hash(seed, j);
     } else {
@@ -437,6 +461,13 @@ __global__ void sched_round_scatter_kernel(uint32_t U, const uint32_t* rbucket,
     const uint32_t b = rbucket[j];
     round_order[bstart[b] + atomicAdd(&bfill[b], 1u)] = j;
   }
+}
+
+// lane_start[q] = first planned round of lane q (the laned rounds follow the r_main others)
+__global__ void sched_lane_start_kernel(uint32_t U, uint32_t n_lanes, uint32_t r_main,
+                                        const uint32_t* bstart, uint32_t* lane_start) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q <= n_lanes) lane_start[q] = r_main + (bstart[U + q] - bstart[U]);
 }
 
 // order[32 i + lane] = sorted[32 round_order[i] + lane]

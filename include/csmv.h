@@ -103,6 +103,13 @@ typedef struct csmv_bank_stream {
                               lock at once queues, holding nothing, for its hottest account and
                               takes its other locks at the head of that queue, so a hot lock is
                               held only while its group commits (a scheduler's hot accounts) */
+  const uint32_t* lane_start; /* optional [deferred_warps + 1] (same memory kind as op), with
+                              split_round: the deferred queue is cut into deferred_warps lanes,
+                              lane i = rounds [lane_start[i], lane_start[i+1]) (absolute round
+                              indices, split_round <= lane_start[0] <= ... <= n_txn/32), each
+                              served in order by the one warp of global index i, which then
+                              joins the main queue: a hot account's rounds on one warp hold its
+                              lock back to back, with no hand-off between warps              */
 } csmv_bank_stream;
 
 /* Account-choice distributions for the workload generator. */
@@ -578,6 +585,11 @@ typedef struct csmv_sched_config {
   uint32_t key_written;       /* plan 1: 1 (default) = a transfer's group key ranks the hot
                                  accounts it writes above those it only reads (rounds share the
                                  locks they take); 0 = the hottest accounts touched           */
+  uint32_t hot_lanes;         /* plan 1 on a group-commit bank: up to this many (<= 64, default
+                                 16) of the hottest accounts, each filling at least 1/64 of the
+                                 plan's transfer rounds, get a lane: their rounds run last, in
+                                 order, on one warp each (the stream's lane_start), so a hot
+                                 account's lock passes between no warps; 0 = no lanes         */
 } csmv_sched_config;
 
 typedef struct csmv_sched_report {

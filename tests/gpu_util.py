@@ -16,7 +16,7 @@ def c1_workload(n_txn=8 * 128 * 256, seed=1, **kw):
 
 
 def run_checked(w, *, init_value=1000, check=True, stream=None, txn_aborts=None, split_round=0,
-                deferred_warps=0, **cfg):
+                deferred_warps=0, lane_start=None, **cfg):
     """Run workload w (or a given stream over its accounts) on a fresh bank; returns (stats,
     stream, bank outputs); asserts exactness."""
     s = cg.generate(w) if stream is None else stream
@@ -25,7 +25,7 @@ def run_checked(w, *, init_value=1000, check=True, stream=None, txn_aborts=None,
     with cg.Bank(n_accounts=w.n_accounts, init_value=init_value, **cfg) as bank:
         bank.load()
         st = bank.run(s, txn_aborts=txn_aborts, split_round=split_round,
-                      deferred_warps=deferred_warps)
+                      deferred_warps=deferred_warps, lane_start=lane_start)
         log_txn, outcome, result = bank.log(w.n_txn, st.final_ts)
         groups = bank.groups(st.final_ts)
         slots = bank.versions()

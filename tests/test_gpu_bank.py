@@ -256,6 +256,30 @@ def test_deferred_queue_and_per_transaction_aborts_exact(deferred_warps):
     assert int(ab0.sum()) == st0.aborts and st0.aborts > 0
 
 
+@pytest.mark.parametrize("prevalidate", [1, 3])
+def test_deferred_queue_lanes_exact(prevalidate):
+    """The deferred queue cut into lanes (lane_start): each of the first warps serves its own
+    lane of rounds in order - here one lane per hot account of a Zipf bank, as a scheduler's
+    hot lanes are, plus an empty lane - and the run replays exactly."""
+    w = c1_workload(n_txn=32 * 2048, n_accounts=1 << 14, dist=cg.DIST_ZIPF, zipf_theta=0.99,
+                    up_reads=4, pr_read_pct=20, seed=5)
+    s = cg.generate(w)
+    R = w.n_txn // 32
+    ro = (s.op.reshape(R, 32)[:, 0] & 3) == 0
+    first = s.addr[s.off].reshape(R, 32)[:, 0]  # a round's lane: its first transfer's debit
+    lanes = [np.flatnonzero(~ro & (first == a)) for a in (0, 1, 2)]
+    laned = np.concatenate(lanes)
+    rest = np.setdiff1d(np.arange(R), laned)
+    order = np.concatenate([rest] + lanes + [np.zeros(0, np.int64)])
+    perm = (order[:, None] * 32 + np.arange(32)).ravel()
+    ps = cg.Stream(np.ascontiguousarray(s.op[perm]), np.ascontiguousarray(s.off[perm]), s.addr)
+    split = len(rest)
+    bounds = np.cumsum([split] + [len(x) for x in lanes] + [0]).astype(np.uint32)
+    assert 0 < split < R and len(laned) > 0
+    run_checked(w, stream=ps, split_round=split, deferred_warps=4, lane_start=bounds, ctas=16,
+                client_warps=4, version_depth=8, prevalidate=prevalidate)
+
+
 @pytest.mark.parametrize("dist", [cg.DIST_UNIFORM, cg.DIST_ZIPF])
 def test_serial_lane_equals_stream_order_execution(dist):
     """The serial lane commits every transaction in stream order: its final balances, read-only
