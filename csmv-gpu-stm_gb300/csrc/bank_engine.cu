@@ -79,7 +79,7 @@ extern "C" void csmv_bank_config_default(csmv_bank_config* c) {
   c->max_txn = 1u << 20;
   c->spin_limit_log2 = 24;
   c->device = 0;
-  c->group_grace = 16;
+  c->group_grace = 4;
 }
 
 static csmv_status validate_config(const csmv_bank_config* c) {

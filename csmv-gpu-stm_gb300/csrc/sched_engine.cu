@@ -77,7 +77,7 @@ extern "C" void csmv_sched_config_default(csmv_sched_config* c) {
   c->backoff_ns = 2048;
   c->hot_last = 1;
   c->key_written = 1;
-  c->hot_lanes = 16;
+  c->hot_lanes = 0;
 }
 
 static void free_all(csmv_sched_t* s) {

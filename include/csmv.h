@@ -203,7 +203,7 @@ typedef struct csmv_bank_config {
   uint32_t group_grace;        /* group commit: polls (about 0.1 us each) a hot queue's head
                                   keeps trying its other locks after taking its hottest one,
                                   before the lanes whose locks are still held sit the attempt
-                                  out (default 16)                                             */
+                                  out (default 4)                                              */
 } csmv_bank_config;
 
 void csmv_bank_config_default(csmv_bank_config* cfg);
@@ -585,11 +585,11 @@ typedef struct csmv_sched_config {
   uint32_t key_written;       /* plan 1: 1 (default) = a transfer's group key ranks the hot
                                  accounts it writes above those it only reads (rounds share the
                                  locks they take); 0 = the hottest accounts touched           */
-  uint32_t hot_lanes;         /* plan 1 on a group-commit bank: up to this many (<= 64, default
-                                 16) of the hottest accounts, each filling at least 1/64 of the
-                                 plan's transfer rounds, get a lane: their rounds run last, in
-                                 order, on one warp each (the stream's lane_start), so a hot
-                                 account's lock passes between no warps; 0 = no lanes         */
+  uint32_t hot_lanes;         /* plan 1 on a group-commit bank: up to this many (<= 64) of the
+                                 hottest accounts, each filling at least 1/64 of the plan's
+                                 transfer rounds, get a lane: their rounds run last, in order,
+                                 on one warp each (the stream's lane_start), so a hot account's
+                                 lock passes between no warps; 0 (default) = no lanes        */
 } csmv_sched_config;
 
 typedef struct csmv_sched_report {
