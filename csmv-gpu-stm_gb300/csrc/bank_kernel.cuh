@@ -456,21 +456,6 @@ __device__ __forceinline__ bool group_take_seen(const BankParams& p, uint32_t x,
   return true;
 }
 
-// One look at x's lock: when it is free, the slots are read and the lock taken by a CAS at the
-// stamp seen (as group_lock_at_turn does, without waiting).
-template <int DEPTH>
-__device__ __forceinline__ bool group_try_lock(const BankParams& p, uint32_t x, uint32_t me,
-                                               uint32_t& stamp, bool& stale,
-                                               SlotEditor<DEPTH>& ed, int32_t& v) {
-  const unsigned long long w = ld_acquire_gpu(&p.cw[x]);
-  if ((w >> 32) != 0ull) return false;
-  ed.load(p.slots + (size_t)x * DEPTH);
-  if (atomicCAS(&p.cw[x], w, w | ((unsigned long long)me << 32)) != w) return false;
-  stamp = (uint32_t)w;
-  stale = !ed.find(stamp, v);
-  return true;
-}
-
 // Queue for x's lock and take it (the turn is served on, also when the wait failed).
 template <int DEPTH>
 __device__ __forceinline__ bool group_wait_lock(const BankParams& p, uint32_t x, uint32_t me,
