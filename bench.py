@@ -526,10 +526,11 @@ def memcd_section(cg, local, n_batches=40):
 def serve_section(cg, local, loads=(0.1, 0.25, 0.5, 0.75, 1.0), per_load_s=1.5):
     """Serving loop under open-loop Poisson arrivals: 2^20 sets x 8 ways, batches of U[1K, 64K]
     requests (multiples of 32), 95 % GET rounds, Zipf(0.99) keys over 4 M. The peak is the
-    closed-loop throughput (submit as fast as admission allows); each offered load is a fraction
-    of it. Latency of a batch = completion seen by the host - its scheduled arrival. The same
-    arrivals then go through the plain form - one synchronous batch call at a time - for the
-    p50/p99 at equal offered load ("plain_*" in each row)."""
+    closed-loop throughput of the loop with overlapping batches (submit as fast as admission
+    allows); each offered load is a fraction of it. Latency of a batch = completion seen by the
+    host - its scheduled arrival. The same arrivals go through the loop with one batch on the
+    device at a time (serial_batches: "p50_ms", "p99_ms"), the loop with overlapping batches
+    ("overlap_*") and the plain form - one synchronous batch call at a time ("plain_*")."""
     rng = np.random.default_rng(7)
     pool_n = 1 << 21
     pool = cg.memcd_generate(cg.memcd_workload(1 << 22, pool_n, seed=77, get_pct=95))
@@ -543,15 +544,17 @@ def serve_section(cg, local, loads=(0.1, 0.25, 0.5, 0.75, 1.0), per_load_s=1.5):
         if time.perf_counter() > t_end:
             raise TimeoutError(f"serving: {what} exceeded its time budget")
 
-    # one launch shape for both forms: the cache autotuner's pick on a 32 K-request sample
+    # one launch shape for every form: the cache autotuner's pick on a 32 K-request sample
     fill = cg.memcd_generate(cg.memcd_workload(1 << 22, 1 << 16, seed=5, get_pct=0))
     best, trials = cg.memcd_autotune(cg.requests_slice(pool, 0, 1 << 15), fill, repeats=2,
                                      n_sets=1 << 20, device=local)
     shape = dict(client_warps=best.client_warps, ctas=best.ctas)
     out["tuned"] = dict(shape, candidates=len(trials))
     progress(f"serving: tuned shape {shape}")
-    with cg.Server(n_sets=1 << 20, arena_requests=1 << 19, max_inflight_sets=1 << 16,
-                   idle_timeout_ms=5000, device=local, **shape) as srv:
+
+    def new_server(serial):
+        srv = cg.Server(n_sets=1 << 20, arena_requests=1 << 19, max_inflight_sets=1 << 16,
+                        idle_timeout_ms=5000, device=local, serial_batches=serial, **shape)
         srv.start()  # a session of fills; the measured session starts from the table it leaves
         t_end = time.perf_counter() + 30
         for _ in range(8):
@@ -562,9 +565,10 @@ def serve_section(cg, local, loads=(0.1, 0.25, 0.5, 0.75, 1.0), per_load_s=1.5):
             while srv.poll(b, results=False) is None:
                 deadline_check(t_end, "fill")
         srv.stop()
-        progress("serving: table filled")
         srv.start()
-        # closed loop: keep the ring full
+        return srv
+
+    def closed_loop(srv):
         inflight, n_done, t0 = [], 0, time.perf_counter()
         t_end = t0 + 30
         while time.perf_counter() - t0 < 1.0:
@@ -578,52 +582,69 @@ def serve_section(cg, local, loads=(0.1, 0.25, 0.5, 0.75, 1.0), per_load_s=1.5):
             deadline_check(t_end, "closed loop")
             if srv.poll(inflight[0][0], results=False) is not None:
                 n_done += inflight.pop(0)[1]
-        peak = n_done / (time.perf_counter() - t0)
-        progress(f"serving: closed-loop peak {peak:.3g} req/s")
-        out["peak_req_s"] = peak
-        mean_n = (1024 + 65536) / 2
-        rows, replay = [], []
-        for load in loads:
-            rate = load * peak / mean_n  # batches per second
-            n_b = max(20, int(rate * per_load_s))
-            arrivals = np.cumsum(rng.exponential(1.0 / rate, n_b))
-            reqs = [draw() for _ in range(n_b)]
-            lat, dev_ns, pending, inflight = [], [], 0, []
-            served = 0
-            t0 = time.perf_counter()
-            t_end = t0 + per_load_s * 4 + 10
-            while pending < n_b or inflight:
-                deadline_check(t_end, f"load {load}")
-                now = time.perf_counter() - t0
-                if pending < n_b and now >= arrivals[pending]:
-                    b = srv.submit(reqs[pending])
-                    if b is not None:
-                        inflight.append((b, arrivals[pending], reqs[pending].n_req))
-                        pending += 1
-                i = 0
-                while i < len(inflight):
-                    b, arr, n = inflight[i]
-                    r = srv.poll(b, results=False)
-                    if r is not None:
-                        lat.append(time.perf_counter() - t0 - arr)
-                        dev_ns.append(r[2])
-                        served += n
-                        inflight.pop(i)
-                    else:
-                        i += 1
-            span = time.perf_counter() - t0
-            lat = np.array(lat) * 1e3
-            dms = np.array(dev_ns) * 1e-6
-            rows.append({"offered_frac": load, "offered_req_s": load * peak,
-                         "achieved_req_s": served / span, "p50_ms": float(np.percentile(lat, 50)),
-                         "p99_ms": float(np.percentile(lat, 99)), "batches": n_b,
-                         "device_p50_ms": float(np.percentile(dms, 50)),
-                         "device_p99_ms": float(np.percentile(dms, 99))})
-            replay.append((arrivals, reqs))
-            progress(f"serving: load {load}: p50 {rows[-1]['p50_ms']:.3f} ms")
-        st = srv.stop()
-        out["loads"] = rows
-        out["abort_rate"] = st.aborts / max(1, st.aborts + st.commits)  # the measured session
+        return n_done / (time.perf_counter() - t0)
+
+    def open_loop(srv, arrivals, reqs, what):
+        lat, dev_ns, pending, inflight, served = [], [], 0, [], 0
+        n_b = len(reqs)
+        t0 = time.perf_counter()
+        t_end = t0 + per_load_s * 4 + 10
+        while pending < n_b or inflight:
+            deadline_check(t_end, what)
+            now = time.perf_counter() - t0
+            if pending < n_b and now >= arrivals[pending]:
+                b = srv.submit(reqs[pending])
+                if b is not None:
+                    inflight.append((b, arrivals[pending], reqs[pending].n_req))
+                    pending += 1
+            i = 0
+            while i < len(inflight):
+                b, arr, n = inflight[i]
+                r = srv.poll(b, results=False)
+                if r is not None:
+                    lat.append(time.perf_counter() - t0 - arr)
+                    dev_ns.append(r[2])
+                    served += n
+                    inflight.pop(i)
+                else:
+                    i += 1
+        span = time.perf_counter() - t0
+        lat = np.array(lat) * 1e3
+        dms = np.array(dev_ns) * 1e-6
+        return {"achieved_req_s": served / span, "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)),
+                "device_p50_ms": float(np.percentile(dms, 50)),
+                "device_p99_ms": float(np.percentile(dms, 99))}
+
+    # the capacity: the loop with overlapping batches, closed loop
+    srv = new_server(0)
+    peak = closed_loop(srv)
+    progress(f"serving: closed-loop peak {peak:.3g} req/s")
+    out["peak_req_s"] = peak
+    mean_n = (1024 + 65536) / 2
+    replay = []
+    for load in loads:
+        rate = load * peak / mean_n  # batches per second
+        n_b = max(20, int(rate * per_load_s))
+        replay.append((np.cumsum(rng.exponential(1.0 / rate, n_b)), [draw() for _ in range(n_b)]))
+    rows = [{"offered_frac": load, "offered_req_s": load * peak, "batches": len(r[1])}
+            for load, r in zip(loads, replay)]
+    for row, (arrivals, reqs) in zip(rows, replay):
+        r = open_loop(srv, arrivals, reqs, f"overlap load {row['offered_frac']}")
+        row.update({"overlap_" + k: v for k, v in r.items()})
+    st = srv.stop()
+    srv.close()
+    out["overlap_abort_rate"] = st.aborts / max(1, st.aborts + st.commits)
+    # one batch on the device at a time
+    srv = new_server(1)
+    for row, (arrivals, reqs) in zip(rows, replay):
+        row.update(open_loop(srv, arrivals, reqs, f"load {row['offered_frac']}"))
+        progress(f"serving: load {row['offered_frac']}: p99 {row['p99_ms']:.3f} ms "
+                 f"(overlapping {row['overlap_p99_ms']:.3f} ms)")
+    st = srv.stop()
+    srv.close()
+    out["loads"] = rows
+    out["abort_rate"] = st.aborts / max(1, st.aborts + st.commits)  # the measured session
     # the plain form at equal offered load: the same arrivals, one batch call at a time
     # (csmv_memcd_run with host buffers); a batch that arrives while another runs waits
     with cg.Memcd(n_sets=1 << 20, max_req=1 << 16, log_commits=0, device=local,

@@ -125,7 +125,7 @@ class MemcdTuneResult(C.Structure):
 class ServeConfig(C.Structure):
     _fields_ = [(n, C.c_uint32) for n in ("n_sets", "client_warps", "ctas", "arena_requests",
                                           "max_inflight_sets", "idle_timeout_ms")] + [
-        ("device", C.c_int32), ("log_cap", C.c_uint32)]
+        ("device", C.c_int32), ("log_cap", C.c_uint32), ("serial_batches", C.c_uint32)]
 
 
 class SchedConfig(C.Structure):

@@ -671,6 +671,7 @@ extern "C" csmv_status csmv_serve_create(const csmv_serve_config* cfg, csmv_serv
   sp.remaining = h->remaining;
   sp.tick = h->tick;
   sp.idle_ns = (unsigned long long)cfg->idle_timeout_ms * 1000000ull;
+  sp.serial = cfg->serial_batches ? 1u : 0u;
   cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->dev, 0, sizeof(ServeDev), h->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(&h->gs->round_next, 0, 4, h->stream);

@@ -526,6 +526,7 @@ struct ServeParams {
   uint32_t* remaining;   // [kServeSlots] rounds left per batch
   uint32_t* tick;        // [kServeSlots] LRU tick per batch
   unsigned long long idle_ns;
+  uint32_t serial;       // 1: one batch on the device at a time
 };
 
 // The admitter's loop, warp-collective: the only reader of the host's control words.
@@ -549,8 +550,11 @@ __device__ void serve_admitter(const MemcdParams& p, const ServeParams& s) {
       if (lane == 0) st_release_sys(&s.ctl->error, err);  // the host sees it without waiting
       break;
     }
-    const bool fresh = adm < sub;
-    for (uint32_t guard = 0; adm < sub && guard < kServeSlots; guard++, adm++) {
+    // one batch at a time (s.serial): the next batch's rounds are appended once every round
+    // appended so far is done, so a batch runs alone on the device, as a synchronous call would
+    const uint32_t admit_to = (s.serial && done != qt) ? adm : (s.serial ? min(sub, adm + 1u) : sub);
+    const bool fresh = adm < admit_to;
+    for (uint32_t guard = 0; adm < admit_to && guard < kServeSlots; guard++, adm++) {
       const uint32_t slot = adm % kServeSlots;
       uint32_t first = 0, n = 0, tk = 0;
       if (lane == 0) {
@@ -583,7 +587,7 @@ __device__ void serve_admitter(const MemcdParams& p, const ServeParams& s) {
       last_sub = sub;
       idle_since = now;
     }
-    if (stop && adm == sub) break;
+    if (stop && adm == sub) break;  // (serial: adm reaches sub only after the last admission)
     if (now - idle_since > s.idle_ns) {
       if (lane == 0) {
         raise_error(&p.gs->error, ERR_WAIT_REQUEST);

@@ -37,7 +37,9 @@ def _wait(srv, bid, timeout=30.0):
         time.sleep(0.0002)
 
 
-def test_serving_results_equal_the_batch_engine():
+@pytest.mark.parametrize("serial", [0, 1])
+def test_serving_results_equal_the_batch_engine(serial):
+    """(serial: one batch on the device at a time.)"""
     n_sets = 1 << 14
     rng = np.random.default_rng(1)
     keys = rng.choice(1 << 24, 1 << 14, replace=False).astype(np.uint32)
@@ -46,7 +48,8 @@ def test_serving_results_equal_the_batch_engine():
     with cg.Memcd(n_sets=n_sets, client_warps=4, max_req=1 << 14) as ref:
         ref.run(fill)
         f_ref, v_ref, _ = ref.run(gets)
-    with cg.Server(n_sets=n_sets, client_warps=4, arena_requests=1 << 15) as srv:
+    with cg.Server(n_sets=n_sets, client_warps=4, arena_requests=1 << 15,
+                   serial_batches=serial) as srv:
         srv.start()
         _wait(srv, srv.submit(fill))
         f, v, ns = _wait(srv, srv.submit(gets))
