@@ -161,10 +161,6 @@ __host__ __device__ constexpr size_t cta_shared_bytes(uint32_t nc) {
 constexpr int kGrpSlots = 128;  // power of two, >= 2 x 64
 constexpr uint32_t kGrpEmpty = 0xFFFFFFFFu;
 struct GroupScratch {
-  uint4 rec[32];              // the chain walk's inputs per lane, packed (transfers of <= 4
-                              // reads): {slots a0 | a1 << 8 | table reads << 16, the part of
-                              // the amount sum read outside the table, divisor | table read
-                              // count << 16 | always << 24, divisor magic}
   uint32_t key[kGrpSlots];    // account (kGrpEmpty = free)
   uint32_t wmask[kGrpSlots];  // lanes whose transfer may write it
   uint32_t busy[kGrpSlots];   // 1 when its lock was held by another warp at the first try
@@ -835,72 +831,16 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
         }
       }
       const uint32_t d = CSMV_OP_AMOD(op);
-      const uint32_t always = CSMV_OP_KIND(op) == CSMV_KIND_TRANSFER_ALWAYS ? 1u : 0u;
-      if constexpr (MAXR <= 4) {  // one 16-byte record per lane
-        gx.rec[lane] = make_uint4((uint32_t)s0 | ((uint32_t)s1 << 8) | ((uint32_t)tr << 16), facc,
-                                  d | (ntr << 16) | (always << 24), 0xFFFFFFFFu / d);
-      } else {
-        gx.cs[lane] = (uint32_t)s0 | ((uint32_t)s1 << 8) | (ntr << 16) | (always << 24);
-        gx.facc[lane] = facc;
-        gx.tr[lane] = tr;
-        gx.md[lane] = d;
-        gx.mm[lane] = 0xFFFFFFFFu / d;
-      }
+      gx.cs[lane] = (uint32_t)s0 | ((uint32_t)s1 << 8) | (ntr << 16) |
+                    ((CSMV_OP_KIND(op) == CSMV_KIND_TRANSFER_ALWAYS ? 1u : 0u) << 24);
+      gx.facc[lane] = facc;
+      gx.tr[lane] = tr;
+      gx.md[lane] = d;
+      gx.mm[lane] = 0xFFFFFFFFu / d;
     }
     __syncwarp();
     uint32_t hwm = hw & ~depm;
-    if constexpr (MAXR <= 4) {
-      if (lane == 0) {
-        // one 16-byte record per lane, the next one loading while this one computes (only the
-        // table values carry a dependence from one lane to the next)
-        uint32_t m = fin & (0u - (depm & (0u - depm)));  // from the first dependent lane on...
-        const uint32_t below = fin & ~m & hw;              // ...after the writes of those below
-        for (uint32_t b = below; b; b &= b - 1u) {
-          const uint32_t j = __ffs(b) - 1u, x = gx.rec[j].x;
-          gx.base[x & 0xFFu] = gx.out0[j];
-          gx.base[(x >> 8) & 0xFFu] = gx.out1[j];
-        }
-        uint32_t j = m ? __ffs(m) - 1u : 0u;
-        uint4 r = gx.rec[j];
-        int32_t o0 = gx.out0[j], o1 = gx.out1[j];
-        while (m) {
-          m &= m - 1u;
-          const uint32_t jn = m ? __ffs(m) - 1u : j;
-          const uint4 rn = gx.rec[jn];
-          const int32_t o0n = gx.out0[jn], o1n = gx.out1[jn];
-          const uint32_t x0 = r.x & 0xFFu, x1 = (r.x >> 8) & 0xFFu;
-          if (!((depm >> j) & 1u)) {  // independent: its writes, for the lanes above
-            if ((hw >> j) & 1u) {
-              gx.base[x0] = o0;
-              gx.base[x1] = o1;
-            }
-          } else {
-            const uint32_t n = (r.z >> 16) & 0xFFu, d = r.z & 0xFFFFu;
-            const int32_t v0 = gx.base[x0], v1 = gx.base[x1];
-            uint32_t acc = r.y;
-            if (n > 0u) acc += (uint32_t)gx.base[(r.x >> 16) & 0xFFu];
-            if (n > 1u) acc += (uint32_t)gx.base[r.x >> 24];
-            uint32_t q = acc - __umulhi(acc, r.w) * d;  // acc mod d (one correction suffices)
-            if (q >= d) q -= d;
-            const uint32_t amt = 1u + q;
-            if ((r.z >> 24) != 0u || v0 >= (int32_t)amt) {
-              const int32_t w0 = (int32_t)((uint32_t)v0 - amt), w1 = (int32_t)((uint32_t)v1 + amt);
-              gx.base[x0] = w0;
-              gx.base[x1] = w1;
-              gx.out0[j] = w0;
-              gx.out1[j] = w1;
-              hwm |= 1u << j;
-            } else {
-              hwm &= ~(1u << j);
-            }
-          }
-          j = jn;
-          r = rn;
-          o0 = o0n;
-          o1 = o1n;
-        }
-      }
-    } else if (lane == 0) {
+    if (lane == 0) {
       // software-pipelined: the next lane's staged inputs load while this one computes (only
       // the table values carry a dependence from one lane to the next)
       uint32_t m = fin & (0u - (depm & (0u - depm)));  // from the first dependent lane on...

@@ -521,6 +521,7 @@ extern "C" void csmv_serve_config_default(csmv_serve_config* c) {
   c->max_inflight_sets = 1u << 15;
   c->idle_timeout_ms = 10000;
   c->device = 0;
+  c->serial_batches = 1;
 }
 
 static void serve_free(csmv_serve_t* h) {

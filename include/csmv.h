@@ -472,9 +472,10 @@ typedef struct csmv_serve_config {
   uint32_t log_cap;            /* > 0: each session logs its commits (commit ts -> arena index
                                   of the request, for its first log_cap timestamps) and every
                                   request's outcome, for a replay by a checker; 0 = off       */
-  uint32_t serial_batches;     /* 1: one batch on the device at a time (the next batch's rounds
-                                  are admitted when every earlier round is done); 0: batches
-                                  overlap                                                        */
+  uint32_t serial_batches;     /* 1 (default): one batch on the device at a time (the next
+                                  batch's rounds are admitted when every earlier round is done);
+                                  0: batches overlap (more throughput at full load, longer tail
+                                  latency below it)                                            */
 } csmv_serve_config;
 typedef struct csmv_serve_t csmv_serve_t;
 void csmv_serve_config_default(csmv_serve_config* cfg);

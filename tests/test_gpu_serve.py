@@ -67,7 +67,8 @@ def test_results_same_alone_and_in_a_mix_of_overlapping_batches():
     rng = np.random.default_rng(2)
     keys = rng.choice(1 << 24, 1 << 14, replace=False).astype(np.uint32)
     kx, ky = keys[:4096], keys[4096:]
-    with cg.Server(n_sets=n_sets, client_warps=4, arena_requests=1 << 17) as srv:
+    with cg.Server(n_sets=n_sets, client_warps=4, arena_requests=1 << 17,
+                   serial_batches=0) as srv:
         srv.start()
         _wait(srv, srv.submit(_ids_requests(keys, 1, seed=5)))
         x = _ids_requests(rng.permutation(kx), 0)
@@ -116,7 +117,7 @@ def test_overlapping_batches_sharing_hot_keys_replay_exactly():
     n_sets = 1 << 10
     n_b, per = 24, 2048
     with cg.Server(n_sets=n_sets, client_warps=4, arena_requests=1 << 16,
-                   max_inflight_sets=1 << 15, log_cap=1 << 17) as srv:
+                   max_inflight_sets=1 << 15, log_cap=1 << 17, serial_batches=0) as srv:
         srv.start()  # a session of fills, then the table it leaves is the replay's start
         fill = cg.memcd_generate(cg.memcd_workload(1 << 13, 8192, seed=21, get_pct=0))
         _wait(srv, srv.submit(fill, tick=1))
