@@ -443,6 +443,20 @@ def c1_section(cg, local):
                 ms.append(st.kernel_ms)
             ms = sorted(ms[1:])[1]
             out[name] = {"tx_s": n / (ms * 1e-3), "abort_rate": st.abort_rate, "kernel_ms": ms}
+    # the same stream on the whole GPU: the autotuner's launch shape and commit method
+    best, trials = cg.autotune(s, repeats=2, n_accounts=4096, init_value=1000, device=local,
+                               max_txn=n)
+    with cg.Bank(best) as bank:
+        ms = []
+        for _ in range(4):
+            bank.load()
+            st = bank.run(s)
+            ms.append(st.kernel_ms)
+        ms = sorted(ms[1:])[1]
+    out["tuned"] = {"tx_s": n / (ms * 1e-3), "abort_rate": st.abort_rate, "kernel_ms": ms,
+                    "client_warps": best.client_warps, "ctas": best.ctas,
+                    "version_depth": best.version_depth, "prevalidate": best.prevalidate,
+                    "max_reads": best.max_reads, "candidates": len(trials)}
     return out
 
 
