@@ -723,9 +723,9 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
     if (in && k < (int)nr && rsl[k] < 0) fok &= read_latest<DEPTH>(vs, p.cw, a[k], fst[k], fv[k]);
   }
   bool ok_wait = true;
-  if (lane == 0)
-    ok_wait = bounded_wait([&] { return mail_acquire<CLUSTER>(&ms.rep) == seq; }, &p.gs->error,
-                           ERR_WAIT_REPLY, p.spin_log2);
+  if (lane == 0)  // the hottest lock is held: spin on the reply before sleeping between polls
+    ok_wait = bounded_wait_fast([&] { return mail_acquire<CLUSTER>(&ms.rep) == seq; },
+                                &p.gs->error, ERR_WAIT_REPLY, p.spin_log2);
   ok_wait = __shfl_sync(FULL, ok_wait, 0);
   if (!ok_wait) {
     failed = true;
@@ -1589,7 +1589,8 @@ __device__ void client_warp(const BankParams& p, CtaShared<MAXR, MAXW>& sm, uint
 // mail[w].{req,rep,cand,base} slots and done_warps/stat fields.
 template <class SM, bool CLUSTER = false>
 __device__ __forceinline__ uint32_t poll_mailboxes(uint32_t nc, GlobalSync* gs, SM& sm,
-                                                   uint32_t seen, uint32_t* req, bool* stop) {
+                                                   uint32_t seen, uint32_t* req, bool* stop,
+                                                   bool check_error = true) {
   const uint32_t lane = lane_id();
   *req = 0;
   if (lane < nc) *req = mail_acquire<CLUSTER>(&sm.mail[lane].req);
@@ -1599,7 +1600,9 @@ __device__ __forceinline__ uint32_t poll_mailboxes(uint32_t nc, GlobalSync* gs, 
     uint32_t done = 0, err = 0;
     if (lane == 0) {
       done = CLUSTER ? ld_acquire_cluster(&sm.done_warps) : *(volatile uint32_t*)&sm.done_warps;
-      err = ld_relaxed_gpu(&gs->error);
+      // the device error word is an L2 round trip: an idle server looks at it only now and
+      // then, so a request that arrives is seen within a shared-memory poll
+      if (check_error) err = ld_relaxed_gpu(&gs->error);
     }
     done = __shfl_sync(0xFFFFFFFFu, done, 0);
     err = __shfl_sync(0xFFFFFFFFu, err, 0);
@@ -1618,7 +1621,8 @@ __device__ void server_warp_stamp(uint32_t nc, uint32_t batch, GlobalSync* gs, S
   for (;;) {
     uint32_t req;
     bool stop;
-    uint32_t ready = poll_mailboxes<SM, CLUSTER>(nc, gs, sm, seen, &req, &stop);
+    uint32_t ready =
+        poll_mailboxes<SM, CLUSTER>(nc, gs, sm, seen, &req, &stop, (idle & 63u) == 63u);
     if (ready == 0) {
       if (stop) break;
       if (++idle > 256u) __nanosleep(64);  // spin a while first: the reply is latency-critical

@@ -127,6 +127,21 @@ __device__ __forceinline__ bool bounded_wait(Pred pred, uint32_t* err, uint32_t 
   return false;
 }
 
+// bounded_wait for a latency-critical reply: 1024 polls back to back (the device error word
+// every 256th), then short sleeps of at most 64 ns.
+template <class Pred>
+__device__ __forceinline__ bool bounded_wait_fast(Pred pred, uint32_t* err, uint32_t code,
+                                                  uint32_t limit_log2) {
+  const uint64_t limit = 1ull << limit_log2;
+  for (uint64_t it = 0; it < limit; ++it) {
+    if (pred()) return true;
+    if ((it & 255u) == 255u && ld_relaxed_gpu(err) != 0) return false;
+    if (it >= 1024) __nanosleep(64);
+  }
+  raise_error(err, code);
+  return false;
+}
+
 // 4-byte asynchronous global->shared copy (lands in shared memory; wait with cp_async_wait_all).
 __device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
