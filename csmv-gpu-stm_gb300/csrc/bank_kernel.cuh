@@ -796,9 +796,9 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
   //    lane writes any of its accounts to (every writer of an account also reads it, so two
   //    writers of one account are always dependent). When some lanes depend on lower ones, each
   //    stages what its transfer needs (table slots, the part of its amount sum read outside the
-  //    table, its divisor) and lane 0 walks the lanes in order over the table's values in shared
-  //    memory, applying the independent lanes' writes and recomputing the dependent ones (a
-  //    transfer writes a1 last): a chain of dependent shared-memory accesses.
+  //    table, its divisor) and lane 0 runs every lane from the first dependent one on, in order,
+  //    over the table's values in shared memory (a transfer writes a1 last; an independent
+  //    lane's inputs are unchanged, so it computes its result again).
   uint32_t dep = 0u;
 #pragma unroll
   for (int k = 0; k < MAXR; k++)
@@ -819,7 +819,7 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
   if (depm) {
     if (valid) {
       uint32_t facc = CSMV_OP_AMT0(op) - 1u, ntr = 0u;
-      unsigned long long tr = ~0ull;
+      unsigned long long tr = 0ull;  // unused bytes name slot 0 (read, then not counted)
 #pragma unroll
       for (int k = 2; k < MAXR; k++) {
         if (k >= (int)nr) continue;
@@ -841,8 +841,11 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
     __syncwarp();
     uint32_t hwm = hw & ~depm;
     if (lane == 0) {
-      // software-pipelined: the next lane's staged inputs load while this one computes (only
-      // the table values carry a dependence from one lane to the next)
+      // Each step's table values are loaded one step ahead, before the previous step's writes
+      // land, and patched with those two writes (a1 first: it is stored last); the transfer's
+      // condition selects its writes without a branch. A step is then a short chain of
+      // arithmetic instead of a shared-memory round trip and a branch.
+      constexpr int NT = MAXR > 2 ? MAXR - 2 : 1;
       uint32_t m = fin & (0u - (depm & (0u - depm)));  // from the first dependent lane on...
       const uint32_t below = fin & ~m & hw;              // ...after the writes of those below it
       for (uint32_t b = below; b; b &= b - 1u) {
@@ -853,48 +856,51 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
       uint32_t j = m ? __ffs(m) - 1u : 0u;
       uint32_t cs = gx.cs[j], facc = gx.facc[j], d = gx.md[j], mg = gx.mm[j];
       unsigned long long tr = gx.tr[j];
-      int32_t o0 = gx.out0[j], o1 = gx.out1[j];
+      int32_t l0 = gx.base[cs & 0xFFu], l1 = gx.base[(cs >> 8) & 0xFFu], lt[NT];
+#pragma unroll
+      for (int q = 0; q < NT; q++) lt[q] = gx.base[(tr >> (8u * q)) & 0xFFu];
+      uint32_t px0 = 0xFFFFFFFFu, px1 = 0xFFFFFFFFu;  // the previous step's slots and writes
+      int32_t pw0 = 0, pw1 = 0;
       while (m) {
         m &= m - 1u;
         const uint32_t jn = m ? __ffs(m) - 1u : j;
+        const uint32_t x0 = cs & 0xFFu, x1 = (cs >> 8) & 0xFFu, n = (cs >> 16) & 0xFFu;
+        const int32_t v0 = x0 == px1 ? pw1 : x0 == px0 ? pw0 : l0;
+        const int32_t v1 = x1 == px1 ? pw1 : x1 == px0 ? pw0 : l1;
+        uint32_t acc = facc;
+#pragma unroll
+        for (int q = 0; q < MAXR - 2; q++) {
+          const uint32_t y = (uint32_t)(tr >> (8u * q)) & 0xFFu;
+          const int32_t t = y == px1 ? pw1 : y == px0 ? pw0 : lt[q];
+          acc += (uint32_t)q < n ? (uint32_t)t : 0u;
+        }
         const uint32_t csn = gx.cs[jn], faccn = gx.facc[jn], dn = gx.md[jn], mgn = gx.mm[jn];
         const unsigned long long trn = gx.tr[jn];
-        const int32_t o0n = gx.out0[jn], o1n = gx.out1[jn];
-        const uint32_t x0 = cs & 0xFFu, x1 = (cs >> 8) & 0xFFu;
-        if (!((depm >> j) & 1u)) {  // independent: its writes, for the lanes above
-          if ((hw >> j) & 1u) {
-            gx.base[x0] = o0;
-            gx.base[x1] = o1;
-          }
-        } else {
-          const uint32_t n = (cs >> 16) & 0xFFu;
-          const int32_t v0 = gx.base[x0], v1 = gx.base[x1];
-          uint32_t acc = facc;
+        l0 = gx.base[csn & 0xFFu];
+        l1 = gx.base[(csn >> 8) & 0xFFu];
 #pragma unroll
-          for (int q = 0; q < MAXR - 2; q++)
-            if ((uint32_t)q < n) acc += (uint32_t)gx.base[(tr >> (8u * q)) & 0xFFu];
-          uint32_t r = acc - __umulhi(acc, mg) * d;  // acc mod d (one correction suffices)
-          if (r >= d) r -= d;
-          const uint32_t amt = 1u + r;
-          if ((cs >> 24) != 0u || v0 >= (int32_t)amt) {
-            const int32_t w0 = (int32_t)((uint32_t)v0 - amt), w1 = (int32_t)((uint32_t)v1 + amt);
-            gx.base[x0] = w0;
-            gx.base[x1] = w1;
-            gx.out0[j] = w0;
-            gx.out1[j] = w1;
-            hwm |= 1u << j;
-          } else {
-            hwm &= ~(1u << j);
-          }
-        }
+        for (int q = 0; q < NT; q++) lt[q] = gx.base[(trn >> (8u * q)) & 0xFFu];
+        uint32_t r = acc - __umulhi(acc, mg) * d;  // acc mod d (one correction suffices)
+        r = r >= d ? r - d : r;
+        const uint32_t amt = 1u + r;
+        const bool moved = (cs >> 24) != 0u || v0 >= (int32_t)amt;
+        const int32_t w0 = moved ? (int32_t)((uint32_t)v0 - amt) : v0;
+        const int32_t w1 = moved ? (int32_t)((uint32_t)v1 + amt) : v1;
+        gx.base[x0] = w0;
+        gx.base[x1] = w1;
+        gx.out0[j] = w0;
+        gx.out1[j] = w1;
+        hwm = moved ? (hwm | (1u << j)) : (hwm & ~(1u << j));
+        px0 = x0;
+        px1 = x1;
+        pw0 = w0;
+        pw1 = w1;
         j = jn;
         cs = csn;
         facc = faccn;
         d = dn;
         mg = mgn;
         tr = trn;
-        o0 = o0n;
-        o1 = o1n;
       }
     }
     hw = __shfl_sync(FULL, hwm, 0);
