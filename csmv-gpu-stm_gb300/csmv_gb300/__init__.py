@@ -61,7 +61,7 @@ class BankConfig(C.Structure):
                                   "cluster_size", "validate", "writeback", "batch",
                                   "prevalidate", "log_commits", "max_txn", "spin_limit_log2")
     ] + [("device", C.c_int32), ("flow_warps", C.c_uint32), ("max_reads", C.c_uint32),
-         ("group_grace", C.c_uint32)]
+         ("group_grace", C.c_uint32), ("group_read_wait", C.c_uint32)]
 
 
 class Stats(C.Structure):

@@ -80,6 +80,7 @@ extern "C" void csmv_bank_config_default(csmv_bank_config* c) {
   c->spin_limit_log2 = 24;
   c->device = 0;
   c->group_grace = 4;
+  c->group_read_wait = 8;
 }
 
 static csmv_status validate_config(const csmv_bank_config* c) {
@@ -318,6 +319,7 @@ BankParams csmv::bank_params(const csmv_bank_t* h, const uint32_t* op, const uin
   p.n_rounds = n_txn / 32;
   p.n_items = c.n_accounts;
   p.grace = c.group_grace;
+  p.read_wait = c.group_read_wait;
   p.slots = h->slots;
   p.cw = h->cw;
   p.ring = h->ring;

@@ -107,6 +107,8 @@ struct BankParams {
   uint32_t* tk;             // group commit: per account {next ticket, ticket served} of its
                             // lock's wait queue
   uint32_t grace;            // group commit: polls a head keeps trying its other locks
+  uint32_t read_wait;        // group commit: polls for an earlier group's lock on a foreign read
+                             // before the lane gives up (0 = 4096)
   const uint8_t* lock_last;  // group commit, optional [n_items]: heat class of each account
                              // (0 = none); classed accounts are locked after all others, the
                              // hottest last
@@ -744,6 +746,7 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
   if (own1) st_relaxed_gpu(&p.cw[a[1]], lock_word(st1, kPendingFlag | (base + 1u)));
   bool valid = in && fok;
   if (valid) {
+    const uint32_t wait_polls = p.read_wait ? p.read_wait : 4096u;
     unsigned long long word[MAXR];
 #pragma unroll
     for (int k = 0; k < MAXR; k++)
@@ -752,8 +755,8 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
     for (int k = 0; k < MAXR; k++) {
       if (k >= (int)nr || rsl[k] >= 0 || !valid) continue;
       unsigned long long wd = word[k];
-      bool settled = false;
-      for (uint32_t it = 0; it < 4096u; it++) {
+      bool settled = false;  // a lane that gives up leaves a hole and is retried
+      for (uint32_t it = 0; it < wait_polls; it++) {
         const uint32_t own = (uint32_t)(wd >> 32);
         bool clear;
         if (own == 0u)

@@ -204,6 +204,10 @@ typedef struct csmv_bank_config {
                                   keeps trying its other locks after taking its hottest one,
                                   before the lanes whose locks are still held sit the attempt
                                   out (default 4)                                              */
+  uint32_t group_read_wait;    /* group commit: polls (about 0.5 us each) a lane makes for an
+                                  earlier group's lock on an account it only reads before it
+                                  gives up and its transaction is retried (default 8; 0 = wait
+                                  up to 4096 polls). Short waits keep a hot lock's holds short */
 } csmv_bank_config;
 
 void csmv_bank_config_default(csmv_bank_config* cfg);
