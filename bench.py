@@ -858,11 +858,13 @@ def main():
                                     log_commits=0)
     plain, _ = run_engine(cg, dev, addr_dev, n_addr, args, local, list(range(min(n_cmp, 3))),
                           log_commits=0, **PLAIN)
-    # ablations of the learned arm, one warm-up and two timed batches each: the raw sketch-count
+    # ablations of the learned arm, one warm-up and two timed batches each (no probe falls in
+    # that window, so "learned" is the arm itself timed the same way): the raw sketch-count
     # score instead of the network, no backoff, no heat classes (plain account lock order),
     # rounds keyed by the hottest accounts touched rather than written
     ablations = {}
-    for name, over in (("sketch_score", dict(score=1)), ("no_backoff", dict(backoff_ns=0)),
+    for name, over in (("learned", {}), ("sketch_score", dict(score=1)),
+                       ("no_backoff", dict(backoff_ns=0)),
                        ("no_heat_classes", dict(hot_last=0)), ("key_touched", dict(key_written=0))):
         r = run_learned(torch, cg, dev, addr_dev, n_addr, args, local, 1, 2,
                         sched_cfg=dict(SCHED, **over))
