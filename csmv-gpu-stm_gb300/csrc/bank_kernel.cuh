@@ -910,7 +910,7 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
     __syncwarp();
   }
 
-  // 7. one version per locked account (its last writer's), then the stamp (a release store: the
+  // 7. one version per locked account (its last writer's), then the stamp (released: the
   //    version is visible first) and the unlock
   auto install = [&](int s, uint32_t x, SlotEditor<DEPTH>& ed) -> uint32_t {
     const uint32_t wr = gx.wmask[s] & hw;
@@ -925,8 +925,11 @@ __device__ uint32_t group_attempt(const BankParams& p, CtaShared<MAXR, MAXW>& sm
   uint32_t pub0 = 0u, pub1 = 0u;
   if (own0) pub0 = install(s0, a[0], ed0);
   if (own1) pub1 = install(s1, a[1], ed1);
-  if (own0) st_release_gpu(&p.cw[a[0]], (unsigned long long)(pub0 ? pub0 : st0));
-  if (own1) st_release_gpu(&p.cw[a[1]], (unsigned long long)(pub1 ? pub1 : st1));
+  // one fence releases both words (a fence then relaxed stores is a release): two release
+  // stores in a row would wait for the first to land before the second
+  if (own0 || own1) fence_acq_rel_gpu();
+  if (own0) st_relaxed_gpu(&p.cw[a[0]], (unsigned long long)(pub0 ? pub0 : st0));
+  if (own1) st_relaxed_gpu(&p.cw[a[1]], (unsigned long long)(pub1 ? pub1 : st1));
 
   // 8. log, outcomes, the group's end, completion
   if (p.log && in) {
