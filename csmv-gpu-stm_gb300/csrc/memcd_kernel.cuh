@@ -415,10 +415,10 @@ __device__ bool memcd_round(const MemcdParams& p, MemcdShared& sm, MemcdMail& ms
         p.val_out[2 * r] = make_uint4(0, 0, 0, 0);
         p.val_out[2 * r + 1] = make_uint4(0, 0, 0, 0);
       }
-      __threadfence();
+      __threadfence();  // with the relaxed store below, the release of the stamp
       if (cand_me) {
         if (valid)
-          st_release_gpu(&p.cw[target], (unsigned long long)my_ts);
+          st_relaxed_gpu(&p.cw[target], (unsigned long long)my_ts);
         else
           st_relaxed_gpu(owner_word(p.cw, target), 0u);
       }
