@@ -31,7 +31,8 @@ Comparison arms on the same batches (reported beside the headline, not in it):
                      (labelled as such; not CSMV)
 Extra sections: "hotspot" (learned vs plain on a shifting hotspot), "uniform", "c1" (the small
 bank of the reference's own configuration), "variants" (the engine's validation / batching /
-write-back / cluster modes on uniform and Zipf banks), "memcd", "serving", "atomics" (the L2
+write-back / cluster modes on uniform and Zipf banks), "alternatives" (another STM on the same
+batches: the reference's naive JVSTM-style baseline), "memcd", "serving", "atomics" (the L2
 atomic rates of the GPU, the engine's roofline).
 
 --impl reference runs the reference arm: the path's CPU execution (the oracle port, striped
@@ -421,6 +422,42 @@ def uniform_section(torch, cg, args, local):
                             log_commits=0, **over)
         out[name] = {"tx_s": res["tx_s"], "abort_rate": res["abort_rate"]}
     out["workload"] = "same bank, uniform account choice, engine alone, 3 batches of 2^20"
+    return out
+
+
+def alternatives_section(torch, cg, dev, addr_dev, n_addr, args, local):
+    """Another STM on the same batches: the reference's naive baseline (bank/baseline, JVSTM
+    style: snapshot reads, validation against the commit records written since, one global
+    commit section; csmv_bank_run_baseline_device) on the Zipf bench batches and on uniform
+    batches; committed tx/s on device time and abort rate, at the learned arm's launch shape.
+    Each runs a warm-up on 2^12 transactions of its first batch, then a prefix of each later
+    batch sized to about half a second at the warm-up's rate (at most the whole batch)."""
+    def run(batches, addr, n_a, order):
+        bank = new_bank(cg, args, local, args.batch, log_commits=0)
+
+        def prefix(b, n):
+            return cg.BankStream(n, b.t[0].data_ptr(), b.t[1].data_ptr(), addr.data_ptr(), n_a)
+        st = bank.run_baseline_device(prefix(batches[order[0]], 1 << 12))
+        rate = st.commits / max(st.kernel_ms * 1e-3, 1e-6)
+        n = min(batches[order[0]].n, max(1 << 12, int(rate * 0.5) // 32 * 32))
+        ms = commits = aborts = 0
+        for i in order[1:]:
+            st = bank.run_baseline_device(prefix(batches[i], n))
+            ms += st.kernel_ms
+            commits += st.commits
+            aborts += st.aborts
+        bank.close()
+        return {"tx_s": commits / (ms * 1e-3), "abort_rate": aborts / max(1, aborts + commits),
+                "txn_per_batch": n}
+
+    out = {"method": "the reference's naive baseline STM (no commit server; validation against "
+                     "commit records; one global commit section, taken once per warp)",
+           "workload": "2^20 accounts r4/w2, 20% read-only scans of 32, batches of 2^20; "
+                       f"{args.client_warps} client warps x {args.ctas} CTAs, depth {args.depth}"}
+    out["zipf"] = run(dev, addr_dev, n_addr, [0, 1])
+    s, bs = generate_batches("uniform", args.batch, 3, pinned=False)
+    addr = torch.from_numpy(s.addr.view(np.int32)).cuda()
+    out["uniform"] = run([DevBatch(torch, b) for b in bs], addr, int(s.addr.shape[0]), [0, 1, 2])
     return out
 
 
@@ -958,6 +995,8 @@ def main():
                     ("dataflow_lane", lambda: dataflow_section(torch, cg, dev, addr_dev, n_addr,
                                                                args, local)),
                     ("variants", lambda: variants_section(cg, local)),
+                    ("alternatives", lambda: alternatives_section(torch, cg, dev, addr_dev,
+                                                                  n_addr, args, local)),
                     ("memcd", lambda: memcd_section(cg, local)),
                     ("serving", lambda: serve_section(cg, local))]
         for name, fn in sections:

@@ -237,6 +237,7 @@ def lib() -> C.CDLL:
         "csmv_sched_serial_run": (I32, [P, P, C.POINTER(BankStream), C.POINTER(SchedReport)]),
         "csmv_bank_run_serial_device": (I32, [P, C.POINTER(BankStream), C.POINTER(Stats)]),
         "csmv_bank_run_flow_device": (I32, [P, C.POINTER(BankStream), C.POINTER(Stats)]),
+        "csmv_bank_run_baseline_device": (I32, [P, C.POINTER(BankStream), C.POINTER(Stats)]),
         "csmv_sched_read_plan": (I32, [P, P, U32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
         "csmv_sched_mlp": (P, [P]),
         "csmv_sched_destroy": (None, [P]),
@@ -476,6 +477,15 @@ class Bank:
         rc = lib().csmv_bank_run_flow_device(self._h, C.byref(dev_stream), C.byref(st))
         self.last_stats = st
         _check(rc, "csmv_bank_run_flow_device")
+        return st
+
+    def run_baseline_device(self, dev_stream: BankStream) -> Stats:
+        """The reference's naive baseline STM on this bank: snapshot reads, validation against
+        commit records, one global commit section (csmv_bank_run_baseline_device)."""
+        st = Stats()
+        rc = lib().csmv_bank_run_baseline_device(self._h, C.byref(dev_stream), C.byref(st))
+        self.last_stats = st
+        _check(rc, "csmv_bank_run_baseline_device")
         return st
 
     def values(self) -> np.ndarray:

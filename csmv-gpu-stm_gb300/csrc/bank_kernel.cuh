@@ -70,6 +70,8 @@ struct alignas(128) GlobalSync {
   alignas(128) uint32_t round_next;      // next unclaimed round of the stream (main queue)
   alignas(128) uint32_t round_deferred;  // next unclaimed round of the deferred queue
   alignas(128) uint32_t error;           // first device error (ERR_*)
+  alignas(128) uint32_t section;         // baseline arm: next ticket of the commit section
+  alignas(128) uint32_t section_serving; // baseline arm: the ticket whose warp holds the section
 };
 
 struct BankParams {

@@ -272,6 +272,17 @@ csmv_status csmv_bank_run_serial_device(csmv_bank_t* h, const csmv_bank_stream* 
 csmv_status csmv_bank_run_flow_device(csmv_bank_t* h, const csmv_bank_stream* dev_stream,
                                       csmv_stats* out);
 
+/* csmv_bank_run_baseline_device - the reference's naive baseline STM (bank/baseline, JVSTM
+ * style; TXRead / TXValidate / TXAddToRecordNaive at bank/baseline/API.cu:3-140, 228-316) as a
+ * comparison arm on the same bank: no commit server; every transaction reads at its snapshot,
+ * validates against the commit records written since, and commits inside one global critical
+ * section, taken here once per warp (the warp's passing transactions commit in lane order).
+ * Same device stream, state, log, outcomes and results as csmv_bank_run_device (stamp protocol
+ * handles only; no deferred queue, lanes, heat classes or backoff), so its runs replay in the
+ * oracle and interleave with the engine's on one bank. Grid: the handle's CTAs x client warps. */
+csmv_status csmv_bank_run_baseline_device(csmv_bank_t* h, const csmv_bank_stream* dev_stream,
+                                          csmv_stats* out);
+
 /* ------------------------------------------------------------------------------------------
  * On-disk streams and commit logs, so CPU and GPU runs replay identical inputs and a run's
  * commit order can be kept (the reference stores raw arrays without a header,
