@@ -307,9 +307,10 @@ def run_learned(torch, cg, dev, addr_dev, n_addr, args, local, warm, timed, sche
 def tune_learned(torch, cg, dev, addr_dev, n_addr, args, local):
     """Client warps per CTA x versions per account for the learned arm: each candidate runs the
     whole arm (probe, plan, group commit) on batch 0 (warm-up) and batch 1 (timed); the fastest
-    is kept in args. The grid stays one CTA per SM."""
+    is kept in args. The grid stays one CTA per SM (at most 15 client warps beside the commit
+    server in its 512 threads)."""
     trials = []
-    for cw, depth in ((1, 8), (2, 8), (1, 4), (2, 4)):
+    for cw, depth in ((2, 8), (4, 8), (8, 8), (12, 8), (15, 8), (12, 4)):
         args.client_warps, args.depth = cw, depth
         r = run_learned(torch, cg, dev, addr_dev, n_addr, args, local, 1, 1)
         trials.append({"client_warps": cw, "version_depth": depth, "tx_s": r["tx_s"]})
