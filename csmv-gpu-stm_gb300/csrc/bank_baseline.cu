@@ -150,6 +150,7 @@ __global__ void __launch_bounds__(512, 1) baseline_kernel(BankParams p) {
         }
         turn = __shfl_sync(FULL, turn, 0);
         hi = __shfl_sync(FULL, hi, 0);
+        __syncwarp();  // the records up to hi are read after lane 0's acquire of ts_next
         scan(hi);
         if (turn) {
           got = true;
@@ -163,6 +164,7 @@ __global__ void __launch_bounds__(512, 1) baseline_kernel(BankParams p) {
         failed = true;
         break;
       }
+      __syncwarp();  // every lane's loads and stores below follow lane 0's acquire of the turn
       uint32_t head = 0;
       if (lane == 0) head = ld_relaxed_gpu(&p.gs->ts_next);
       head = __shfl_sync(FULL, head, 0);
