@@ -370,8 +370,9 @@ def e2e_learned(torch, cg, host, s_addr, args, local, warm, timed):
 def hotspot_section(torch, cg, args, local):
     """Learned vs plain on the shifting hotspot: batches of 2^20 transactions. Arms: plain (the
     reference's commit method, stream order), group commit in stream order, the learned
-    scheduler with group commit, and two ablations of it (the raw sketch-count score instead of
-    the network; no backoff); tx/s on the host clock with planning and training included."""
+    scheduler with group commit (probing and training on every third chunk, as in the headline
+    arm), and two ablations of it (the raw sketch-count score instead of the network; no
+    backoff); tx/s on the host clock with planning and training included."""
     chunk, count = 1 << 20, 6
     s, bs = generate_batches("hotspot", chunk, count, pinned=False, seed=3, pr_read_pct=10,
                              ro_reads=8, up_reads=2, hot_frac=0.01, hot_prob=0.3,
@@ -379,9 +380,11 @@ def hotspot_section(torch, cg, args, local):
     addr = torch.from_numpy(s.addr.view(np.int32)).cuda()
     dev = [DevBatch(torch, b) for b in bs]
     out = {}
+    probe = dict(probe_rounds_pct=SCHED["probe_rounds_pct"], probe_every=SCHED["probe_every"])
     for arm, over, learned in (("plain", PLAIN, False), ("group_stream", ENGINE, False),
-                               ("learned", ENGINE, {}), ("learned_sketch_score", ENGINE, {"score": 1}),
-                               ("learned_no_backoff", ENGINE, {"backoff_ns": 0})):
+                               ("learned", ENGINE, probe),
+                               ("learned_sketch_score", ENGINE, dict(probe, score=1)),
+                               ("learned_no_backoff", ENGINE, dict(probe, backoff_ns=0))):
         bank = cg.Bank(n_accounts=N_ACCOUNTS, version_depth=8, client_warps=2, ctas=152,
                        max_txn=chunk, log_commits=0, device=local, **over)
         bank.load()
