@@ -113,3 +113,46 @@ def test_devtest_library_exports():
     assert {"csmv_devtest_read", "csmv_devtest_prevalidate", "csmv_devtest_writeback",
             "csmv_devtest_bounded_wait"} <= names
     C.CDLL(str(b.DEVTEST_LIB))
+
+
+# the binding's ctypes mirrors of the header's structs
+MIRRORS = {
+    "BankWorkload": "csmv_bank_workload", "BankStream": "csmv_bank_stream",
+    "BankConfig": "csmv_bank_config", "Stats": "csmv_stats",
+    "MemcdWorkload": "csmv_memcd_workload", "MemcdBatch": "csmv_memcd_batch",
+    "MemcdConfig": "csmv_memcd_config", "TuneTrial": "csmv_tune_trial",
+    "TuneResult": "csmv_tune_result", "MemcdTuneResult": "csmv_memcd_tune_result",
+    "ServeConfig": "csmv_serve_config", "SchedConfig": "csmv_sched_config",
+    "SchedReport": "csmv_sched_report", "AtomicRates": "csmv_atomic_rates",
+}
+
+
+def test_binding_structs_match_the_header(tmp_path):
+    """Every ctypes struct of the binding has the size, field offsets and field sizes of its C
+    struct, as a C compiler lays it out from include/csmv.h (a field added to one side only
+    would shift every later field the library reads)."""
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "csmv.h"', "int main(void) {"]
+    for py, c in MIRRORS.items():
+        cls = getattr(cg, py)
+        lines.append(f'  printf("{py} . %zu 0\\n", sizeof({c}));')
+        for name, *_ in cls._fields_:
+            lines.append(f'  printf("{py} {name} %zu %zu\\n", offsetof({c}, {name}), '
+                         f"sizeof((({c}*)0)->{name}));")
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    seen = 0
+    for ln in out.splitlines():
+        py, name, a, bsz = ln.split()
+        cls = getattr(cg, py)
+        if name == ".":
+            assert C.sizeof(cls) == int(a), (py, C.sizeof(cls), int(a))
+        else:
+            f = getattr(cls, name)
+            assert (f.offset, f.size) == (int(a), int(bsz)), (py, name, f.offset, f.size, a, bsz)
+        seen += 1
+    assert seen == sum(len(getattr(cg, py)._fields_) + 1 for py in MIRRORS)
