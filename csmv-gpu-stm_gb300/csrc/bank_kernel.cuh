@@ -1659,10 +1659,11 @@ __device__ void server_warp_stamp(uint32_t nc, uint32_t batch, GlobalSync* gs, S
     }
     const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
     uint32_t t0 = 0;
-    // release: the draw follows the lock marks the requests carried; acquire: the validations
-    // that follow it see every mark made before an earlier draw (the draws form one chain of
-    // read-modify-writes on the word)
-    if (lane == 0) t0 = atom_add_acq_rel_gpu(&gs->ts_next, total);
+    if (lane == 0) {  // fences on both sides order the draw after the observed locks and
+      __threadfence();  // before the validations that follow it
+      t0 = atomicAdd(&gs->ts_next, total);
+      __threadfence();
+    }
     t0 = __shfl_sync(0xFFFFFFFFu, t0, 0);
     if (mine) {
       sm.mail[lane].base = t0 + incl - cnt;
